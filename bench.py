@@ -1,0 +1,340 @@
+#!/usr/bin/env python3
+"""Benchmark of the node-evolution hot path on GB300.
+
+Metric: node-timesteps/s (accepted adaptive Cash-Karp steps of one node per
+second) of the batched isolated-halo step: 65,536 halos per GPU, each
+advanced over one timestep at relative tolerance 1e-3 (P-std physics).  A
+"step" of this benchmark is one evolve pass over the whole batch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs one process per GPU under torch.distributed.run; every rank
+evolves its own batch (independent halos, no collective on the data path;
+weak scaling) and rank 0 prints the JSON line with the max-over-ranks time.
+
+`--impl reference` times the reference algorithm on the host CPU.  The
+Fortran reference cannot be built in this environment (no gfortran, GSL,
+HDF5 or FoX), so that arm runs the C++ restatement in oracle/ with every
+host thread.
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "node-timesteps/s on 1 GB300: batched+surrogate vs plain GPU at <=1e-3 mass error"
+UNIT = "node-timesteps/s"
+N_NODES = 65536
+WORKLOAD = "isolated-halo step: 65,536 halos/GPU, M 1e10-1e14 Msun, dt 0.01-1 Gyr, rel tol 1e-3, P-std physics (plain FP64)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nodes", type=int, default=N_NODES)
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle sampling during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def algorithmic_flops_per_step(params, table, batch, weights_path, sample=512):
+    """Weighted FP64 flops per accepted node-timestep, counted by the oracle's
+    counting scalar on a sample of the batch (closed-form cooling radius, as
+    the kernel computes it)."""
+    from oracle import oracle
+    with open(weights_path) as f:
+        w = json.load(f)
+    weights = np.array([w[k] for k in w["order"]], dtype=np.float64)
+    total, steps = 0.0, 0
+    idx = np.linspace(0, batch.n - 1, min(sample, batch.n)).astype(int)
+    for i in idx:
+        ops, counters = oracle.count_flops(params, table, batch.param[:, i], batch.state[:, i], batch.t_start[i],
+                                           batch.t_end[i], batch.step[i])
+        total += float(np.dot(ops.astype(np.float64), weights))
+        steps += int(counters[0])
+    return total / max(steps, 1)
+
+
+def cpu_baseline(params, table, batch, seconds=10.0):
+    """The oracle on every host core over repeats of the full batch."""
+    from oracle import oracle
+    cores = os.cpu_count() or 1
+    t_start = time.perf_counter()
+    steps = reps = 0
+    while True:
+        _, _, status, counters = oracle.evolve_batch(params, table, batch.state, batch.param, batch.t_start,
+                                                     batch.t_end, batch.step, threads=cores, brent=True)
+        steps += int(counters[0].sum())
+        reps += 1
+        elapsed = time.perf_counter() - t_start
+        if elapsed >= seconds:
+            break
+    return {"value": steps / elapsed, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{reps} passes over the {batch.n}-halo batch ({elapsed:.1f} s, Brent cooling radius as in the reference)"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from galacticus_gb300 import workloads
+    from galacticus_gb300.cie_tables import CieTable
+    from oracle import oracle
+    params = workloads.isolated_params()
+    table = CieTable()
+    batch = workloads.isolated_halos(n=args.nodes, seed=2)
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        oracle.evolve_batch(params, table, batch.state, batch.param, batch.t_start, batch.t_end, batch.step, threads=cores)
+    times, steps = [], 0
+    # Each step is a bounded sample: the full batch (about 0.1 s of CPU work per pass).
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, _, _, counters = oracle.evolve_batch(params, table, batch.state, batch.param, batch.t_start, batch.t_end,
+                                                batch.step, threads=cores, brent=True)
+        times.append(time.perf_counter() - t0)
+        steps += int(counters[0].sum())
+    value = steps / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox halos)",
+        "config": {"workload": WORKLOAD, "nodes": args.nodes, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} passes over the {args.nodes}-halo batch; C++ restatement of the "
+                                   "reference algorithm (the Fortran reference is not buildable here)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from galacticus_gb300 import _abi, workloads
+    from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+
+    params = workloads.isolated_params()
+    ev = MergerTreeNodeEvolverStandard(params=params)
+    lib, ctx = ev.lib, ev.ctx
+    batch = workloads.isolated_halos(n=args.nodes, seed=2 + rank)
+    n = batch.n
+
+    def dev_tensor(a, dtype=torch.float64):
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dtype)
+
+    pristine_state = dev_tensor(batch.state)
+    pristine_step = dev_tensor(batch.step)
+    state = pristine_state.clone()
+    step = pristine_step.clone()
+    param = dev_tensor(batch.param)
+    t0 = dev_tensor(batch.t_start)
+    t1 = dev_tensor(batch.t_end)
+    status = torch.zeros(n, dtype=torch.int32, device=dev)
+    counters = torch.zeros((3, n), dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
+    stream = torch.cuda.Stream(dev)  # one non-default stream orders copies, flush, events and our kernel
+    torch.cuda.set_stream(stream)
+
+    def launch():
+        rc = lib.gal_gpu_evolve_batch_device(ctx, n, state.data_ptr(), param.data_ptr(), t0.data_ptr(), t1.data_ptr(),
+                                             step.data_ptr(), status.data_ptr(), counters.data_ptr(), stream.cuda_stream)
+        if rc:
+            raise RuntimeError(f"gal_gpu_evolve_batch_device failed: {rc}")
+
+    def one_step(ev0=None, ev1=None, evk0=None, evk1=None):
+        flush.zero_()  # evict the previous step's data from L2 (between timed iterations)
+        if ev0 is not None:
+            ev0.record(stream)
+        state.copy_(pristine_state)  # every step evolves the same halos from the same initial state
+        step.copy_(pristine_step)
+        if evk0 is not None:
+            evk0.record(stream)
+        launch()
+        if evk1 is not None:
+            evk1.record(stream)
+        if ev1 is not None:
+            ev1.record(stream)
+
+    for _ in range(max(args.warmup, 3)):
+        one_step()
+    torch.cuda.synchronize()
+    assert int((status != 0).sum()) == 0, "node evolution failed during warm-up"
+    accepted_per_step = int(counters[0].sum())
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+            torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = lib.gal_gpu_launch_count(ctx)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        wall0 = time.perf_counter()
+        for e in evs:
+            one_step(*e)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    if dist:
+        dist.barrier()
+    launches = lib.gal_gpu_launch_count(ctx) - launches0
+    step_ms = [a.elapsed_time(b) for a, b, _, _ in evs]
+    kernel_ms = [a.elapsed_time(b) for _, _, a, b in evs]
+    total_ms = sum(step_ms)
+    if dist:
+        tt = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+        acc = torch.tensor([accepted_per_step], device=dev, dtype=torch.int64)
+        dist.all_reduce(acc, op=dist.ReduceOp.SUM)
+        accepted_all = int(acc.item())
+    else:
+        accepted_all = accepted_per_step
+    value = accepted_all * args.steps / (total_ms * 1e-3)
+
+    # End-to-end through the public host API with pinned host buffers.
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    h_state, h_param, h_t0, h_t1, h_step = pin(batch.state), pin(batch.param), pin(batch.t_start), pin(batch.t_end), pin(batch.step)
+    h_status = pin(np.zeros(n, dtype=np.int32))
+    h_counters = pin(np.zeros((3, n), dtype=np.uint32))
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        np.copyto(h_state, batch.state)
+        np.copyto(h_step, batch.step)
+        tb = time.perf_counter()
+        rc = lib.gal_gpu_evolve_batch(ctx, n, dp(h_state), dp(h_param), dp(h_t0), dp(h_t1), dp(h_step),
+                                      h_status.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                      h_counters.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+        te = time.perf_counter() - tb
+        if rc:
+            raise RuntimeError("gal_gpu_evolve_batch failed")
+        if i >= args.warmup:
+            e2e_times.append(te)
+    e2e_total = sum(e2e_times)
+    if dist:
+        tt = torch.tensor([e2e_total], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_total = float(tt.item())
+    e2e_value = accepted_all * args.steps / e2e_total
+    h2d = n * (_abi.NY + _abi.NP + 3) * 8
+    d2h = n * (_abi.NY + 1) * 8 + n * 4 + n * 12
+
+    if rank == 0:
+        from galacticus_gb300.cie_tables import CieTable
+        flops_peak, calib_ms = ctypes.c_double(), ctypes.c_double()
+        lib.gal_calibrate_fp64(ctypes.byref(flops_peak), ctypes.byref(calib_ms))
+        f_step = algorithmic_flops_per_step(params, ev.table, batch, os.path.join(ROOT, "oracle", "flop_weights.json"))
+        k_ms = statistics.mean(kernel_ms)
+        achieved = f_step * accepted_per_step / (k_ms * 1e-3)
+        bytes_launch = n * ((_abi.NY + _abi.NP + 3) * 8 + (_abi.NY + 1) * 8 + 4 + 12)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded Philox halos; reference datasets absent)",
+            "config": {"workload": WORKLOAD, "nodes_per_gpu": n, "form": "plain (FP64 CIE table)",
+                       "l2": "flushed between timed iterations (256 MB memset outside the event pair)",
+                       "launch": list(ev.get_launch()), "accepted_steps_per_pass": accepted_per_step},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": flops_peak.value / 1e12, "unit": "TFLOP/s",
+                         "frac": achieved / flops_peak.value, "traffic": None,
+                         "peak_source": "measured by gal_calibrate_fp64 (DFMA loop on all SMs); MEASURED_PEAKS.json has no FP64 figure",
+                         "flops_per_node_timestep": f_step, "kernel_ms": k_ms,
+                         "hbm_gbs": bytes_launch / (k_ms * 1e-3) / 1e9, "hbm_bytes_per_launch": bytes_launch},
+            "wall_ms_timed_region": wall * 1e3,
+            "clocks": clocks.summary(),
+        }
+        line["cpu_baseline"] = cpu_baseline(params, ev.table, workloads.isolated_halos(n=args.nodes, seed=2))
+        print(json.dumps(line), flush=True)
+    ev.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

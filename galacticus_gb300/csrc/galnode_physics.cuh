@@ -1,0 +1,463 @@
+// galnode_physics.cuh -- device physics of the P-std node ODE system.
+//
+// One thread evaluates the full right-hand side of one node.  Quantities
+// that do not change during an evolve call (halo scales, galaxy sizes,
+// star-formation timescales, outflow loading factors, the temperature
+// coordinate of the CIE tables) are computed once per node in
+// node_setup(); the right-hand side only does the state-dependent work.
+// Reference sources are cited per function (paths relative to the
+// Galacticus repository root).
+#pragma once
+
+#include <cstdint>
+#include "../../include/galnode.h"
+
+namespace gal {
+
+// ---- physical constants (source/numerical/constants/*.F90; GSL MKSA values)
+namespace k {
+constexpr double Pi = 3.14159265358979323846;
+constexpr double gravitationalConstant = 6.673e-11;
+constexpr double massSolar = 1.98892e30;
+constexpr double megaParsec = 1.0e6 * 3.08567758135e16;
+constexpr double gigaYear = 1.0e9 * 3.15581497635456e7;
+constexpr double boltzmannsConstant = 1.3806504e-23;
+constexpr double atomicMassUnit = 1.660538782e-27;
+constexpr double speedLight = 2.99792458e8;
+constexpr double thomsonCrossSection = 6.65245893699e-29;
+constexpr double atomicMassHydrogen = 1.0078250322;
+constexpr double atomicMassHelium = 4.0026032545;
+constexpr double massHydrogenAtom = atomicMassHydrogen * atomicMassUnit;
+constexpr double hydrogenByMassPrimordial = 0.7514;
+constexpr double heliumByMassPrimordial = 0.2486;
+constexpr double hydrogenByMassSolar = 0.7070;
+constexpr double heliumByMassSolar = 0.2740;
+constexpr double metallicitySolar = 0.0188;
+constexpr double meanAtomicMassPrimordial =
+    1.0 / (2.0 * hydrogenByMassPrimordial / atomicMassHydrogen + 3.0 * heliumByMassPrimordial / atomicMassHelium);
+constexpr double kilo = 1.0e3, hecto = 1.0e2, ergs = 1.0e-7;
+constexpr double gravitationalConstantInternal = gravitationalConstant * massSolar / (kilo * kilo) / megaParsec;
+constexpr double MpcPerKmPerSToGyr = megaParsec / kilo / gigaYear;
+constexpr double feedbackEnergyInputAtInfinityCanonical = 4.517e5;
+// n_H per (rho X_H) with rho in Msun/Mpc^3 and n_H in cm^-3 (cooling_time/simple.F90:150-155).
+constexpr double densityToHydrogenNumber =
+    massSolar / massHydrogenAtom / (hecto * hecto * hecto) / (megaParsec * megaParsec * megaParsec);
+// Eddington rate per unit black-hole mass (black_holes/fundamentals.F90:123-138).
+constexpr double eddingtonPerMass = 4.0 * Pi * gravitationalConstant * massHydrogenAtom * gigaYear / thomsonCrossSection / speedLight;
+// Bondi-Hoyle-Lyttleton prefactor (accretion/Bondi_Hoyle_Lyttleton.F90:34-59).
+constexpr double bhlPrefactor = kilo * gigaYear / megaParsec * 4.0 * Pi;
+}  // namespace k
+
+// Constants shared by every node, derived on the host from gal_params.
+struct Globals {
+  gal_params p;
+  int nT, nZ;                 // table shape
+  int firstZero;              // first metallicity row is Z = 0
+  double firstNonZero;        // Z/Zsun of the first non-zero row
+  double Tmin, Tmax, Zmin, Zmax;
+  double soundSpeedSpheroid;  // km/s at bh_temperature_spheroid
+  double jeansPrefactor;      // c_s/sqrt(G) for the spheroid gas
+  double bhSpheroidCoef;      // enhancement * bhl * G^2 / c_s^3
+  double bhRadiusSpheroidCoef;  // G / c_s^2
+  double coolingCoef;         // (dof/2) k_B / ergs / Gyr / densityToHydrogenNumber
+  double accretionFraction;   // Omega_b / Omega_m
+};
+
+// Per-node constants of one evolve call.
+struct NodeC {
+  double massHalo;            // basic mass at the start (tolerance scale)
+  double tdyn;                // halo dynamical time r_vir/V_vir (Gyr)
+  double rcore;               // beta-profile core radius (Mpc)
+  double rho0PerMass;         // central beta-profile density per unit hot mass
+  double rOuter;              // hot-halo outer radius = virial radius (Mpc)
+  double onePlusXOuter2;      // 1 + (r_outer/r_core)^2
+  double coolingTimeCoef;     // coolingCoef * T_vir
+  double hT;                  // temperature interpolation weight
+  int iT;                     // temperature cell of T_vir
+  int coolingAllowed;         // V_vir <= velocity cut-off
+  double sfrDisk, sfrSph;     // 1/tau_* of the disk and spheroid (0: none)
+  double outDisk, outSph;     // outflow rate per unit SFR
+  double outDiskMax, outSph_max; // 1/(t_dyn f_min) of the rate limit (<0: no limit)
+  double aSph;                // spheroid scale radius (Mpc)
+  double rhoSphPerMass;       // 1/(2 pi a^3)
+  double radiusDisk;          // disk radius (Mpc)
+  double bhRadiusHotCoef;     // G / c_s(T_vir)^2
+  double bhHotCoef;           // enhancement * bhl * c_s(T_vir)
+  double bhHotMaxCoef;        // c_s/(r_outer MpcPerKmPerSToGyr)
+  double accretionRate;       // hot-gas accretion rate (Msun/Gyr)
+  double rvir;
+};
+
+__device__ __forceinline__ double mass_fraction(double metals, double mass) {
+  // Abundances_Mass_To_Mass_Fraction_Packed (objects/abundances.F90:781-809)
+  return metals > mass ? 1.0 : (metals <= 0.0 ? 0.0 : metals / mass);
+}
+
+// Largest i with g[i] <= x, kept in [0, n-2]; g in shared memory.
+__device__ __forceinline__ int locate(const double* g, int n, double x) {
+  if (!(x >= g[0])) return 0;
+  if (x >= g[n - 1]) return n - 2;
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (g[mid] <= x) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Set up the per-node constants (node_setup in the oracle; each line
+// restates the cited reference function for a node whose scales are fixed
+// over the call).
+__device__ __forceinline__ void node_setup(const Globals& G, const double* sLnT, const double* prm, NodeC& c) {
+  const gal_params& p = G.p;
+  const double M = prm[GAL_P_MASS], Mdot = prm[GAL_P_MASS_RATE];
+  const double rvir = prm[GAL_P_RADIUS_VIRIAL], vvir = prm[GAL_P_VELOCITY_VIRIAL], spin = prm[GAL_P_SPIN];
+  c.massHalo = M;
+  c.rvir = rvir;
+  // virialDensityContrastDefinition{VirialTemperature,DynamicalTimescale} (virial_density_contrast.F90:195-262)
+  const double T = 0.5 * k::atomicMassUnit * k::meanAtomicMassPrimordial * (k::kilo * vvir) * (k::kilo * vvir) / k::boltzmannsConstant;
+  c.tdyn = rvir / vvir * k::MpcPerKmPerSToGyr;
+  c.rcore = p.core_radius_fraction * rvir;
+  c.rOuter = rvir;  // outer radius clamp of hot_halo/standard/_class.F90:430-450
+  const double x = c.rOuter / c.rcore;
+  const double norm = x < 1.0e-6 ? 3.0 / (x * x * x) + 9.0 / 5.0 / x - 36.0 * x / 175.0 : 1.0 / (x - atan(x));
+  c.rho0PerMass = norm / (4.0 * k::Pi) / (c.rcore * c.rcore * c.rcore);
+  c.onePlusXOuter2 = 1.0 + x * x;
+  // Temperature coordinate of the CIE tables ("extrapolate" in T = clamp).
+  const double Tc = fmin(fmax(T, G.Tmin), G.Tmax);
+  const double lnT = log(Tc);
+  c.iT = locate(sLnT, G.nT, lnT);
+  c.hT = (lnT - sLnT[c.iT]) / (sLnT[c.iT + 1] - sLnT[c.iT]);
+  c.coolingTimeCoef = G.coolingCoef * T;
+  c.coolingAllowed = !(vvir > p.cooling_velocity_cutoff);
+  // galacticStructureSolverFixed: r = f lambda r_vir, V = V_vir.
+  const double Rd = p.radius_factor_disk * spin * rvir, Rs = p.radius_factor_spheroid * spin * rvir;
+  c.radiusDisk = Rd;
+  c.aSph = Rs;
+  c.rhoSphPerMass = Rs > 0.0 ? 1.0 / (2.0 * k::Pi) / (Rs * Rs * Rs) : 0.0;
+  // Star-formation timescales (star_formation/timescales/dynamical_time.F90:121-189).
+  auto timescale = [&](const gal_star_formation& sf, double R) -> double {
+    if (sf.timescale_type == GAL_SF_TIMESCALE_FIXED) return sf.timescale_fixed;
+    if (vvir <= 0.0 || sf.efficiency == 0.0) return 0.0;
+    const double t = k::MpcPerKmPerSToGyr * R / vvir;
+    return fmax(t * pow(vvir / 200.0, sf.exponent_velocity) / sf.efficiency, sf.timescale_minimum);
+  };
+  const double tsD = timescale(p.sf_disk, Rd), tsS = timescale(p.sf_spheroid, Rs);
+  c.sfrDisk = tsD > 0.0 ? 1.0 / tsD : 0.0;
+  c.sfrSph = tsS > 0.0 ? 1.0 / tsS : 0.0;
+  // Outflow loading (power_law/_class.F90:118-164, fixed.F90) and rateLimit (rate_limit.F90).
+  auto loading = [&](const gal_outflow& o) -> double {
+    if (o.type == GAL_OUTFLOW_FIXED) return o.fraction;
+    if (vvir <= 0.0) return 0.0;
+    return pow(o.velocity_characteristic / vvir, o.exponent);
+  };
+  auto limit = [&](const gal_outflow& o, double R) -> double {
+    if (!(o.timescale_fractional_minimum > 0.0)) return -1.0;
+    const double t = (vvir <= 0.0 || R <= 0.0) ? 1.0 : k::MpcPerKmPerSToGyr * R / vvir;
+    return 1.0 / t / o.timescale_fractional_minimum;
+  };
+  c.outDisk = loading(p.outflow_disk);
+  c.outSph = loading(p.outflow_spheroid);
+  c.outDiskMax = limit(p.outflow_disk, Rd);
+  c.outSph_max = limit(p.outflow_spheroid, Rs);
+  // Hot-halo Bondi accretion constants at the virial temperature.
+  const double cs = sqrt(5.0 * k::boltzmannsConstant * T / 3.0 / k::meanAtomicMassPrimordial / k::atomicMassUnit) / k::kilo;
+  c.bhRadiusHotCoef = T > 0.0 ? k::gravitationalConstantInternal / (cs * cs) : 0.0;
+  c.bhHotCoef = p.bh_enhancement_hot_halo * k::bhlPrefactor * cs;
+  c.bhHotMaxCoef = cs / (c.rOuter * k::MpcPerKmPerSToGyr);
+  c.accretionRate = Mdot > 0.0 ? G.accretionFraction * Mdot : 0.0;
+}
+
+// Hydrogen mass and number fractions of gas of metal mass fraction Z
+// (objects/abundances.F90:830-883).
+__device__ __forceinline__ void hydrogen_fractions(double Z, double& xMass, double& xNumber) {
+  const double zs = Z * (1.0 / k::metallicitySolar);
+  const double xH = fmin(fmax(zs * (k::hydrogenByMassSolar - k::hydrogenByMassPrimordial) + k::hydrogenByMassPrimordial, 0.7),
+                         k::hydrogenByMassPrimordial);
+  const double yHe = fmin(zs * (k::heliumByMassSolar - k::heliumByMassPrimordial) + k::heliumByMassPrimordial, k::heliumByMassPrimordial);
+  const double nH = xH * (1.0 / k::atomicMassHydrogen), nHe = yHe * (1.0 / k::atomicMassHelium);
+  xMass = xH;
+  xNumber = nH / (nH + nHe);
+}
+
+// Interpolated cooling function (erg cm^3 s^-1, without the n_H^2 factor)
+// and n_e/n_H at the node temperature and metallicity Z/Zsun
+// (cooling_function/CIE_file.F90:238-317, 665-735; chemical/state/
+// CIE_file.F90:245-320).  `tab` interleaves (ln Lambda, ln n_e/n_H).
+__device__ __forceinline__ void cie_lookup(const Globals& G, const double2* tab, const double* sLnZ, const NodeC& c,
+                                          double zSolar, double& lambda, double& electrons) {
+  zSolar = fmin(fmax(zSolar, G.Zmin), G.Zmax);  // "fix" extrapolation in metallicity
+  const double zUse = fmax(zSolar, 0.0);
+  int iZ;
+  double hZ;
+  if (G.firstZero && zUse < G.firstNonZero) {
+    iZ = 0;
+    hZ = zUse / G.firstNonZero;
+  } else {
+    const double lnZ = log(zUse);
+    iZ = locate(sLnZ, G.nZ, lnZ);
+    hZ = (lnZ - sLnZ[iZ]) / (sLnZ[iZ + 1] - sLnZ[iZ]);
+  }
+  const int nT = G.nT;
+  const double2 a = tab[iZ * nT + c.iT], b = tab[(iZ + 1) * nT + c.iT];
+  const double2 d = tab[iZ * nT + c.iT + 1], e = tab[(iZ + 1) * nT + c.iT + 1];
+  const double hT = c.hT;
+  const double w00 = (1.0 - hT) * (1.0 - hZ), w01 = (1.0 - hT) * hZ, w10 = hT * (1.0 - hZ), w11 = hT * hZ;
+  lambda = exp(a.x * w00 + b.x * w01 + d.x * w10 + e.x * w11);
+  electrons = exp(a.y * w00 + b.y * w01 + d.y * w10 + e.y * w11);
+}
+
+// Cooling radius (cooling_radius/simple.F90:313-427) in closed form.  At
+// fixed temperature and metallicity the cooling time is proportional to
+// 1/rho (Lambda scales as n_H^2, n_e as n_H), so t_cool(r) = t_avail solves
+// as r = r_core sqrt(t_avail/t_cool(0) - 1) inside the bracket [0, r_outer]
+// that the reference's root finder searches.  t_avail = t_dyn
+// (coolingTimeAvailableWhiteFrenk1991 with ageFactor = 0).
+__device__ __forceinline__ double cooling_radius(const Globals& G, const double2* tab, const double* sLnZ, const NodeC& c,
+                                                double massHot, double metalsHot) {
+  const double Z = mass_fraction(metalsHot, massHot);
+  double xMass, xNumber;
+  hydrogen_fractions(Z, xMass, xNumber);
+  double lambda, electrons;
+  cie_lookup(G, tab, sLnZ, c, Z * (1.0 / k::metallicitySolar), lambda, electrons);
+  const double rho0 = massHot > 0.0 ? massHot * c.rho0PerMass : 0.0;
+  // t_cool(0) = (dof/2) k T (n_H/x_num + n_e) / ergs / (Lambda n_H^2) / Gyr, n_H = rho X_H conv.
+  const double nH0 = rho0 * xMass;  // in units of densityToHydrogenNumber
+  const double denominator = lambda * nH0;
+  const double tcool0 = denominator > 0.0 ? c.coolingTimeCoef * (1.0 / xNumber + electrons) / denominator : 1.0e10;
+  const double tAvail = c.tdyn;
+  if (tcool0 * c.onePlusXOuter2 < tAvail) return c.rOuter;
+  if (tcool0 > tAvail) return 0.0;
+  return c.rcore * sqrt(tAvail / tcool0 - 1.0);
+}
+
+// Right-hand side of the node ODE system: the node operators of
+// nodeOperatorMulti (nodes/operators/multi.F90:313-332) in the order of
+// parameters/quickTest.xml.  Same logic, branch by branch, as the oracle.
+__device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const double* sLnZ, const NodeC& c,
+                                   const double* y, double* dydt) {
+  const gal_params& p = G.p;
+  const uint32_t ph = p.physics;
+#pragma unroll
+  for (int i = 0; i < GAL_NY; ++i) dydt[i] = 0.0;
+  const double massHot = y[GAL_Y_HOT_MASS], metalsHot = y[GAL_Y_HOT_METALS];
+  const double gasDisk = y[GAL_Y_DISK_GAS], gasSph = y[GAL_Y_SPHEROID_GAS];
+  bool coolingRadiusKnown = false;
+  double rCool = 0.0;
+
+  // starFormationDisks (star_formation/disks.F90:200-324) + instantaneous populations
+  // (stellar_populations/properties/instantaneous.F90:133-219).
+  const bool diskOk = !(c.radiusDisk < 0.0 || gasDisk < 0.0);
+  const double sfrDisk = diskOk ? gasDisk * c.sfrDisk : 0.0;
+  const double zDisk = mass_fraction(y[GAL_Y_DISK_GAS_METALS], gasDisk);
+  if ((ph & GAL_PHYS_STAR_FORMATION_DISK) && diskOk) {
+    const double rateStars = (1.0 - p.recycled_fraction) * sfrDisk;
+    const double rateMetals = zDisk * rateStars;
+    dydt[GAL_Y_DISK_STARS] += rateStars;
+    dydt[GAL_Y_DISK_GAS] += -rateStars;
+    dydt[GAL_Y_DISK_STARS_METALS] += rateMetals;
+    dydt[GAL_Y_DISK_GAS_METALS] += -rateMetals + p.metal_yield * sfrDisk;
+  }
+  // starFormationSpheroids (star_formation/spheroids.F90:152-)
+  const bool sphOk = !(c.aSph < 1.0e-12 || gasSph < 1.0e-6);
+  const double sfrSph = sphOk ? gasSph * c.sfrSph : 0.0;
+  const double zSph = mass_fraction(y[GAL_Y_SPHEROID_GAS_METALS], gasSph);
+  if ((ph & GAL_PHYS_STAR_FORMATION_SPHEROID) && sphOk) {
+    const double rateStars = (1.0 - p.recycled_fraction) * sfrSph;
+    dydt[GAL_Y_SPHEROID_STARS] += rateStars;
+    dydt[GAL_Y_SPHEROID_GAS] += -rateStars;
+    dydt[GAL_Y_SPHEROID_GAS_METALS] += -(zSph * rateStars) + p.metal_yield * sfrSph;
+  }
+  // stellarFeedbackDisks (stellar_feedback/disks.F90:116-205)
+  if ((ph & GAL_PHYS_FEEDBACK_DISK) && diskOk) {
+    double total = c.outDisk * sfrDisk;
+    if (c.outDiskMax >= 0.0) {
+      const double maximum = fmax(gasDisk * c.outDiskMax, 0.0);
+      if (total > maximum) total = total * maximum / total;
+    }
+    if (total > 0.0) {
+      const double metals = gasDisk > 0.0 ? zDisk * total : 0.0;
+      dydt[GAL_Y_OUTFLOWED_MASS] += total;
+      dydt[GAL_Y_DISK_GAS] += -total;
+      dydt[GAL_Y_OUTFLOWED_METALS] += metals;
+      dydt[GAL_Y_DISK_GAS_METALS] += -metals;
+    }
+  }
+  // stellarFeedbackSpheroids (stellar_feedback/spheroids.F90:116-208)
+  if ((ph & GAL_PHYS_FEEDBACK_SPHEROID) && sphOk) {
+    double total = c.outSph * sfrSph;
+    if (c.outSph_max >= 0.0) {
+      const double maximum = fmax(gasSph * c.outSph_max, 0.0);
+      if (total > maximum) total = total * maximum / total;
+    }
+    if (total > 0.0) {
+      const double metals = gasSph > 0.0 ? zSph * total : 0.0;
+      dydt[GAL_Y_OUTFLOWED_MASS] += total;
+      dydt[GAL_Y_SPHEROID_GAS] += -total;
+      dydt[GAL_Y_OUTFLOWED_METALS] += metals;
+      dydt[GAL_Y_SPHEROID_GAS_METALS] += -metals;
+    }
+  }
+  // blackHolesAccretion (black_holes/accretion.F90:113-174) with
+  // blackHoleAccretionRateStandard (black_holes/accretion_rates/standard.F90:221-440).
+  const double massBH = y[GAL_Y_BLACK_HOLE];
+  if ((ph & GAL_PHYS_BLACK_HOLE_ACCRETION) && massBH > 0.0) {
+    const double eps = p.bh_efficiency_radiative;
+    const double eddingtonCap = eps > 0.0 ? k::eddingtonPerMass * massBH / eps : 0.0;
+    double rateSph = 0.0;
+    {
+      const double rAcc = fmax(G.bhRadiusSpheroidCoef * massBH, 0.0);
+      double rho = 0.0;
+      if (gasSph > 0.0 && c.aSph > 0.0) {
+        const double xx = rAcc / c.aSph, opx = 1.0 + xx;
+        rho = gasSph * c.rhoSphPerMass / xx / (opx * opx * opx);
+      }
+      if (rho > 1.0) {
+        double jeans = G.jeansPrefactor / sqrt(rho);
+        jeans = fmin(jeans, c.aSph);
+        if (jeans > rAcc) {
+          const double xx = jeans / c.aSph, opx = 1.0 + xx;
+          rho = gasSph * c.rhoSphPerMass / xx / (opx * opx * opx);
+        }
+        rateSph = fmax(G.bhSpheroidCoef * massBH * massBH * rho, 0.0);
+        if (eps > 0.0) rateSph = fmin(rateSph, eddingtonCap);
+      }
+    }
+    double rateHot = 0.0;
+    {
+      double rAcc = c.bhRadiusHotCoef > 0.0 ? c.bhRadiusHotCoef * massBH : HUGE_VAL;
+      rAcc = fmin(rAcc, c.rOuter);
+      double fractionHot = 1.0;
+      if (p.bh_hot_mode_only) {
+        // standardHotModeFraction (accretion_rates/standard.F90:442-468)
+        rCool = cooling_radius(G, tab, sLnZ, c, massHot, metalsHot);
+        coolingRadiusKnown = true;
+        const double xx = rCool / c.rvir;
+        if (xx < 0.9) fractionHot = 1.0;
+        else if (xx > 1.0) fractionHot = 0.0;
+        else {
+          const double u = (xx - 0.9) / 0.1;
+          fractionHot = u * u * (2.0 * u - 3.0) + 1.0;
+        }
+      }
+      double rho = 0.0;
+      if (massHot > 0.0 && !(rAcc > c.rOuter)) {
+        const double xx = rAcc / c.rcore;
+        rho = massHot * c.rho0PerMass / (1.0 + xx * xx);
+      }
+      rho *= fractionHot;
+      if (rho > 1.0) {
+        rateHot = fmax(c.bhHotCoef * rAcc * rAcc * rho, 0.0);
+        rateHot = fmin(rateHot, fmax(massHot * c.bhHotMaxCoef, 0.0));
+        if (eps > 0.0) rateHot = fmin(rateHot, eddingtonCap);
+      }
+    }
+    const double total = rateSph + rateHot;
+    if (total > 0.0) {
+      const double reduced = total * (1.0 - p.bh_efficiency_radiative - p.bh_efficiency_jet);
+      dydt[GAL_Y_BLACK_HOLE] += reduced;
+      // spheroid gas sink (spheroid/standard/_class.F90:638-671)
+      if (rateSph != 0.0 && gasSph > 0.0 && gasSph + y[GAL_Y_SPHEROID_STARS] > 0.0) {
+        dydt[GAL_Y_SPHEROID_GAS] += -rateSph;
+        dydt[GAL_Y_SPHEROID_GAS_METALS] += (-rateSph / gasSph) * y[GAL_Y_SPHEROID_GAS_METALS];
+      }
+      // hot-halo mass sink (hot_halo/standard/_class.F90:771-799)
+      if (rateHot != 0.0 && massHot > 0.0) {
+        dydt[GAL_Y_HOT_MASS] += -rateHot;
+        dydt[GAL_Y_HOT_METALS] += metalsHot * (-rateHot / massHot);
+      }
+    }
+  }
+  // CGMAccretion (circumgalactic_medium/accretion.F90:517-593; accretion/halo/simple.F90:281-319)
+  if (ph & GAL_PHYS_CGM_ACCRETION) dydt[GAL_Y_HOT_MASS] += c.accretionRate;
+  // CGMOutflowReincorporation (circumgalactic_medium/outflow_reincorporation.F90:272-349;
+  // hot_halo/outflow_reincorporation/halo_dynamical_time.F90:113-128)
+  if (ph & GAL_PHYS_REINCORPORATION) {
+    const double massOut = y[GAL_Y_OUTFLOWED_MASS];
+    if (massOut > 0.0) {
+      const double rate = massOut * p.reincorporation_multiplier / c.tdyn;
+      const double metals = rate * y[GAL_Y_OUTFLOWED_METALS] / massOut;
+      dydt[GAL_Y_OUTFLOWED_MASS] += -rate;
+      dydt[GAL_Y_OUTFLOWED_METALS] += -metals;
+      dydt[GAL_Y_HOT_MASS] += rate;
+      dydt[GAL_Y_HOT_METALS] += metals;
+    }
+  }
+  // CGMCoolingHeating (circumgalactic_medium/cooling_heating.F90:216-381) with
+  // coolingRateWhiteFrenk1991 (cooling/cooling_rate/White-Frenk.F90:132-185).
+  if ((ph & GAL_PHYS_COOLING) && massHot > 0.0 && c.rOuter > 0.0) {
+    double rate = 0.0;
+    if (c.coolingAllowed) {
+      if (!coolingRadiusKnown) rCool = cooling_radius(G, tab, sLnZ, c, massHot, metalsHot);
+      if (rCool >= c.rOuter) {
+        rate = massHot / c.tdyn;
+      } else if (rCool > 0.0) {
+        // 4 pi r^2 rho(r) dr_cool/dt with dr/dt = r/t_avail/(2x^2/(1+x^2))
+        // (cooling_radius/simple.F90:229-311, isothermal gas).
+        const double xx = rCool / c.rcore;
+        const double slope = 2.0 * xx * xx / (xx * xx + 1.0);
+        const double growth = rCool / c.tdyn / slope;
+        rate = 4.0 * k::Pi * rCool * rCool * (massHot * c.rho0PerMass / (1.0 + xx * xx)) * growth;
+      }
+    }
+    if (rate > 0.0) {
+      const double metals = rate * metalsHot / massHot;
+      dydt[GAL_Y_HOT_MASS] += -rate;
+      dydt[GAL_Y_HOT_METALS] += -metals;
+      dydt[GAL_Y_DISK_GAS] += rate;
+      dydt[GAL_Y_DISK_GAS_METALS] += metals;
+    }
+  }
+}
+
+// Post-step clamps of the standard components (hot_halo/standard/_class.F90:
+// 455-530, disk/standard/_class.F90:473-677, spheroid/standard/_class.F90:
+// 464-636); all return GSL_Continue, so the evolver is not reset.
+__device__ __forceinline__ void post_step(double* y) {
+  if (y[GAL_Y_HOT_MASS] < 0.0) y[GAL_Y_HOT_MASS] = 0.0;
+  if (y[GAL_Y_DISK_GAS] < 0.0) {
+    if (y[GAL_Y_DISK_GAS] + y[GAL_Y_DISK_STARS] == 0.0) {
+      y[GAL_Y_DISK_STARS] = 0.0;
+      y[GAL_Y_DISK_STARS_METALS] = 0.0;
+    }
+    y[GAL_Y_DISK_GAS] = 0.0;
+    y[GAL_Y_DISK_GAS_METALS] = 0.0;
+  }
+  if (y[GAL_Y_DISK_STARS] < 0.0) {
+    if (y[GAL_Y_DISK_GAS] + y[GAL_Y_DISK_STARS] == 0.0) {
+      y[GAL_Y_DISK_GAS] = 0.0;
+      y[GAL_Y_DISK_GAS_METALS] = 0.0;
+    }
+    y[GAL_Y_DISK_STARS] = 0.0;
+    y[GAL_Y_DISK_STARS_METALS] = 0.0;
+  }
+  if (y[GAL_Y_SPHEROID_GAS] < 0.0) {
+    if (y[GAL_Y_SPHEROID_GAS] + y[GAL_Y_SPHEROID_STARS] == 0.0) y[GAL_Y_SPHEROID_STARS] = 0.0;
+    y[GAL_Y_SPHEROID_GAS] = 0.0;
+    y[GAL_Y_SPHEROID_GAS_METALS] = 0.0;
+  }
+  if (y[GAL_Y_SPHEROID_STARS] < 0.0) {
+    if (y[GAL_Y_SPHEROID_GAS] + y[GAL_Y_SPHEROID_STARS] == 0.0) {
+      y[GAL_Y_SPHEROID_GAS] = 0.0;
+      y[GAL_Y_SPHEROID_GAS_METALS] = 0.0;
+    }
+    y[GAL_Y_SPHEROID_STARS] = 0.0;
+  }
+}
+
+// Absolute-tolerance scales from the initial state (scaleSetTask hooks of
+// hot_halo :804-850, disk :735-824, spheroid :804-897, black hole :195-257).
+__device__ __forceinline__ void scales(const double* y, double massHalo, double* s) {
+  const double hot = massHalo * 1.0e-3;
+  s[GAL_Y_HOT_MASS] = s[GAL_Y_HOT_METALS] = s[GAL_Y_OUTFLOWED_MASS] = s[GAL_Y_OUTFLOWED_METALS] = hot;
+  const double mass = fmax(fabs(y[GAL_Y_DISK_GAS]) + fabs(y[GAL_Y_SPHEROID_GAS]) + fabs(y[GAL_Y_DISK_STARS]) +
+                               fabs(y[GAL_Y_SPHEROID_STARS]), 1.0);
+  const double metals = fmax(fabs(y[GAL_Y_DISK_GAS_METALS]) + fabs(y[GAL_Y_DISK_STARS_METALS]) + fabs(y[GAL_Y_SPHEROID_GAS_METALS]),
+                             fmax(mass * 1.0e-4, 1.0));
+  s[GAL_Y_DISK_GAS] = s[GAL_Y_DISK_STARS] = s[GAL_Y_SPHEROID_GAS] = s[GAL_Y_SPHEROID_STARS] = mass;
+  s[GAL_Y_DISK_GAS_METALS] = s[GAL_Y_DISK_STARS_METALS] = s[GAL_Y_SPHEROID_GAS_METALS] = metals;
+  const double stars = y[GAL_Y_SPHEROID_STARS] > 0.0 ? y[GAL_Y_SPHEROID_STARS] : 0.0;
+  s[GAL_Y_BLACK_HOLE] = fmax(fmax(1.0, 1.0e-4 * stars), y[GAL_Y_BLACK_HOLE]);
+}
+
+}  // namespace gal

@@ -1,0 +1,124 @@
+"""Synthetic node batches with the shapes of the benchmark configurations.
+
+There are no merger-tree or halo catalogues to read, so the inputs are drawn
+from seeded counter-based streams (numpy's Philox4x32 bit generator keyed by
+the configuration seed) with the documented distributions.  Host-side only;
+nothing here is timed.
+
+Cosmology is the flat matter + cosmological-constant model of
+``cosmologyFunctionsMatterLambda`` with the configuration's parameters;
+virial quantities use the Bryan & Norman (1998) density contrast
+(source/structure_formation/virial_density_contrast/Bryan_Norman.F90:172-196)
+relative to the mean matter density.
+"""
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+
+G_INTERNAL = 6.673e-11 * 1.98892e30 / 1.0e6 / (1.0e6 * 3.08567758135e16)  # km^2 s^-2 Mpc / Msun
+MPC_PER_KM_PER_S_TO_GYR = 1.0e6 * 3.08567758135e16 / 1.0e3 / (1.0e9 * 3.15581497635456e7)
+
+
+@dataclass
+class Cosmology:
+    omega_matter: float = 0.3
+    omega_lambda: float = 0.7
+    omega_baryon: float = 0.045
+    hubble: float = 70.0  # km/s/Mpc
+    sigma8: float = 0.8
+    n_s: float = 0.96
+
+    @property
+    def hubble_gyr(self):
+        return self.hubble / MPC_PER_KM_PER_S_TO_GYR
+
+    def time(self, z):
+        """Cosmic time (Gyr) at redshift z for a flat matter+Lambda model."""
+        a = 1.0 / (1.0 + np.asarray(z, dtype=np.float64))
+        return (2.0 / (3.0 * self.hubble_gyr * np.sqrt(self.omega_lambda))
+                * np.arcsinh(np.sqrt(self.omega_lambda / self.omega_matter) * a ** 1.5))
+
+    def redshift(self, t):
+        """Inverse of time()."""
+        x = np.sinh(1.5 * self.hubble_gyr * np.sqrt(self.omega_lambda) * np.asarray(t, dtype=np.float64))
+        a = (x / np.sqrt(self.omega_lambda / self.omega_matter)) ** (2.0 / 3.0)
+        return 1.0 / a - 1.0
+
+    def density_mean(self, z):
+        rho_crit0 = 3.0 * self.hubble ** 2 / (8.0 * np.pi * G_INTERNAL)  # Msun/Mpc^3
+        return self.omega_matter * rho_crit0 * (1.0 + np.asarray(z)) ** 3
+
+    def virial_contrast_mean(self, z):
+        z = np.asarray(z, dtype=np.float64)
+        om = self.omega_matter * (1 + z) ** 3 / (self.omega_matter * (1 + z) ** 3 + self.omega_lambda)
+        x = om - 1.0
+        return (18.0 * np.pi ** 2 + 82.0 * x - 39.0 * x ** 2) / (x + 1.0)
+
+    def virial(self, mass, z):
+        """Virial radius (Mpc) and velocity (km/s) of halos of the given mass."""
+        rho = self.virial_contrast_mean(z) * self.density_mean(z)
+        r = np.cbrt(3.0 * mass / (4.0 * np.pi * rho))
+        v = np.sqrt(G_INTERNAL * mass / r)
+        return r, v
+
+
+SPIN_DEFAULT = 0.04326  # peak of the Bett et al. (2007) spin distribution (parameters/quickTest.xml)
+
+
+@dataclass
+class Batch:
+    state: np.ndarray   # [NY][n]
+    param: np.ndarray   # [NP][n]
+    t_start: np.ndarray
+    t_end: np.ndarray
+    step: np.ndarray
+
+    @property
+    def n(self):
+        return self.state.shape[1]
+
+    def copy(self):
+        return Batch(self.state.copy(), self.param.copy(), self.t_start.copy(), self.t_end.copy(), self.step.copy())
+
+    def subset(self, idx):
+        return Batch(self.state[:, idx].copy(), self.param[:, idx].copy(), self.t_start[idx].copy(),
+                     self.t_end[idx].copy(), self.step[idx].copy())
+
+
+def isolated_halos(n=65536, seed=2, cosmology=None, spin=SPIN_DEFAULT):
+    """Batched isolated step: n independent halos, each advanced over one
+    timestep.  Halo mass log-uniform in 1e10-1e14 Msun; hot gas
+    (Omega_b/Omega_m) M U(0.5,1); metallicity log-uniform 1e-4-0.02 (mass
+    fraction); disk and spheroid empty; black hole 1e5 Msun; redshift
+    uniform in 0-4; timestep log-uniform in 0.01-1 Gyr."""
+    cosmo = cosmology or Cosmology()
+    rng = np.random.Generator(np.random.Philox(key=seed))
+    u = rng.random((6, n))
+    mass = 10.0 ** (10.0 + 4.0 * u[0])
+    z = 4.0 * u[1]
+    hot = cosmo.omega_baryon / cosmo.omega_matter * mass * (0.5 + 0.5 * u[2])
+    metallicity = 10.0 ** (-4.0 + np.log10(200.0) * u[3])
+    dt = 10.0 ** (-2.0 + 2.0 * u[4])
+    r, v = cosmo.virial(mass, z)
+    state = np.zeros((_abi.NY, n))
+    state[_abi.Y_HOT_MASS] = hot
+    state[_abi.Y_HOT_METALS] = metallicity * hot
+    state[_abi.Y_BLACK_HOLE] = 1.0e5
+    param = np.zeros((_abi.NP, n))
+    param[_abi.P_MASS] = mass
+    param[_abi.P_MASS_RATE] = 0.0
+    param[_abi.P_RADIUS_VIRIAL] = r
+    param[_abi.P_VELOCITY_VIRIAL] = v
+    param[_abi.P_SPIN] = spin
+    t0 = cosmo.time(z)
+    return Batch(state, param, t0, t0 + dt, np.full(n, -1.0))
+
+
+def isolated_params(tolerance_relative=1.0e-3):
+    """P-std parameters with the batched-isolated-step tolerances."""
+    p = _abi.default_params()
+    p.ode_tolerance_relative = tolerance_relative
+    return p

@@ -1,0 +1,243 @@
+/*
+ * galnode.h -- C ABI of the GB300 node evolver.
+ *
+ * This library replaces the per-node ODE evolution step of Galacticus, the
+ * `mergerTreeNodeEvolver` class with its default `standard` implementation
+ * (source/merger_trees/node_evolver/_class.F90:41-57, method `evolve`;
+ * implementation source/merger_trees/node_evolver/standard.F90:385-755).
+ * The reference serialises one node's evolvable properties into an FP64
+ * vector and integrates them with GSL's embedded Cash-Karp stepper through a
+ * scaled error controller (source/external/gslODEInitVal2/driver2.c:148-250,
+ * cscal2.c:93-169).  Here a whole batch of nodes is integrated on one GPU by
+ * hand-written sm_103a kernels; the per-node semantics (tolerances, scales,
+ * trial halving, step-size reuse, post-step clamps) are the reference's.
+ *
+ * Conventions
+ *  - Plain C types only.  Every array is caller-owned.  Functions whose name
+ *    contains `_device` take device pointers and a cudaStream_t passed as
+ *    `void*`; all others take host pointers and copy inside the call.
+ *  - Node data is structure-of-arrays: `state[v*n + i]` is property v of
+ *    node i.  The property order is the GAL_Y_* enumeration below.
+ *  - Return value 0 means success; a non-zero value is a GAL_ERR_* code and
+ *    gal_gpu_last_error() gives the message.  The library never aborts.
+ *  - Per-node status uses the reference's integer codes (errorStatus* in
+ *    source/error/_module.F90:66-75).
+ *  - A context is used by one host thread at a time; it owns one CUDA stream.
+ */
+#ifndef GALNODE_H
+#define GALNODE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- evolved node properties (one FP64 value each) --------------------
+ * The serialisation order of the standard hot halo, disk, spheroid and
+ * black hole components for the "P-std" physics profile.  Angular momenta
+ * are not evolved: the `fixed` galactic structure solver sizes galaxies from
+ * the halo spin, not from their angular momentum. */
+enum {
+  GAL_Y_HOT_MASS = 0,          /* hotHalo%mass                         */
+  GAL_Y_HOT_METALS = 1,        /* hotHalo%abundances (metals)          */
+  GAL_Y_OUTFLOWED_MASS = 2,    /* hotHalo%outflowedMass                */
+  GAL_Y_OUTFLOWED_METALS = 3,  /* hotHalo%outflowedAbundances          */
+  GAL_Y_DISK_GAS = 4,          /* disk%massGas                         */
+  GAL_Y_DISK_GAS_METALS = 5,   /* disk%abundancesGas                   */
+  GAL_Y_DISK_STARS = 6,        /* disk%massStellar                     */
+  GAL_Y_DISK_STARS_METALS = 7, /* disk%abundancesStellar               */
+  GAL_Y_SPHEROID_GAS = 8,      /* spheroid%massGas                     */
+  GAL_Y_SPHEROID_GAS_METALS = 9, /* spheroid%abundancesGas             */
+  GAL_Y_SPHEROID_STARS = 10,   /* spheroid%massStellar                 */
+  GAL_Y_BLACK_HOLE = 11,       /* blackHole%mass                       */
+  GAL_NY = 12
+};
+
+/* ---- per-node inputs that are not evolved ------------------------------ */
+enum {
+  GAL_P_MASS = 0,        /* basic%mass at the start time (Msun)                 */
+  GAL_P_MASS_RATE = 1,   /* basic%accretionRate (Msun/Gyr); mass is linear in t */
+  GAL_P_RADIUS_VIRIAL = 2,   /* virial radius (Mpc)                             */
+  GAL_P_VELOCITY_VIRIAL = 3, /* virial velocity (km/s)                          */
+  GAL_P_SPIN = 4,        /* halo spin parameter lambda                          */
+  GAL_NP = 5
+};
+
+/* ---- per-node status codes (reference values) --------------------------- */
+enum {
+  GAL_STATUS_SUCCESS = 0,     /* errorStatusSuccess                            */
+  GAL_STATUS_UNDERFLOW = 15,  /* errorStatusUnderflow: all ODE trials failed   */
+  GAL_STATUS_XCPU = 1025,     /* errorStatusXCPU: per-node step budget used up */
+  GAL_STATUS_NOT_FINITE = 2001 /* a state value became NaN or infinite       */
+};
+
+/* ---- library error codes ------------------------------------------------- */
+enum {
+  GAL_OK = 0,
+  GAL_ERR_ARGUMENT = 1,
+  GAL_ERR_CUDA = 2,
+  GAL_ERR_TABLE = 3,
+  GAL_ERR_NO_DEVICE = 4,
+  GAL_ERR_TOO_LARGE = 5
+};
+
+/* ---- physics switches (bit mask in gal_params.physics) -------------------
+ * Each bit enables one node operator of the reference's `nodeOperatorMulti`
+ * list (source/nodes/operators/multi.F90:313-332). */
+enum {
+  GAL_PHYS_STAR_FORMATION_DISK = 1 << 0,     /* starFormationDisks          */
+  GAL_PHYS_STAR_FORMATION_SPHEROID = 1 << 1, /* starFormationSpheroids      */
+  GAL_PHYS_FEEDBACK_DISK = 1 << 2,           /* stellarFeedbackDisks        */
+  GAL_PHYS_FEEDBACK_SPHEROID = 1 << 3,       /* stellarFeedbackSpheroids    */
+  GAL_PHYS_BLACK_HOLE_ACCRETION = 1 << 4,    /* blackHolesAccretion         */
+  GAL_PHYS_CGM_ACCRETION = 1 << 5,           /* CGMAccretion                */
+  GAL_PHYS_REINCORPORATION = 1 << 6,         /* CGMOutflowReincorporation   */
+  GAL_PHYS_COOLING = 1 << 7,                 /* CGMCoolingHeating           */
+  GAL_PHYS_ALL = 0xff
+};
+
+/* Star-formation timescale and outflow classes. */
+enum {
+  GAL_SF_TIMESCALE_DYNAMICAL = 0, /* starFormationTimescaleDynamicalTime */
+  GAL_SF_TIMESCALE_FIXED = 1      /* starFormationTimescaleFixed         */
+};
+enum {
+  GAL_OUTFLOW_POWER_LAW = 0, /* stellarFeedbackOutflowsPowerLaw */
+  GAL_OUTFLOW_FIXED = 1      /* stellarFeedbackOutflowsFixed    */
+};
+
+/* Star formation in one component (disk or spheroid).
+ * Reference: source/star_formation/timescales/dynamical_time.F90:121-189,
+ * source/star_formation/rates/disks/timescale.F90:109-130. */
+typedef struct gal_star_formation {
+  int32_t timescale_type;    /* GAL_SF_TIMESCALE_*                        */
+  int32_t pad;
+  double efficiency;         /* epsilon_* (dynamicalTime: 0.01)             */
+  double exponent_velocity;  /* alpha_* (dynamicalTime: -1.5)              */
+  double timescale_minimum;  /* Gyr (1e-3)                                  */
+  double timescale_fixed;    /* Gyr, used by GAL_SF_TIMESCALE_FIXED         */
+} gal_star_formation;
+
+/* Stellar-feedback outflows from one component, wrapped by `rateLimit`.
+ * Reference: source/stellar_feedback/outflows/power_law/_class.F90:118-164,
+ * fixed.F90, rate_limit.F90. */
+typedef struct gal_outflow {
+  int32_t type;                /* GAL_OUTFLOW_*                               */
+  int32_t pad;
+  double velocity_characteristic; /* km/s (disk 250, spheroid 100)          */
+  double exponent;             /* power-law exponent (3.5)                   */
+  double fraction;             /* GAL_OUTFLOW_FIXED mass-loading fraction    */
+  double timescale_fractional_minimum; /* rateLimit; <= 0 disables the limit */
+} gal_outflow;
+
+/* All parameters of one evolution context.  gal_params_default() fills the
+ * values of the "P-std" profile (the reference's default classes, with the
+ * documented substitutions); callers may change any field before
+ * gal_gpu_init(). */
+typedef struct gal_params {
+  /* mergerTreeNodeEvolverStandard (standard.F90:174-181, 135) */
+  double ode_tolerance_absolute;   /* odeToleranceAbsolute (0.01)            */
+  double ode_tolerance_relative;   /* odeToleranceRelative (0.01)            */
+  int32_t reuse_step_size;         /* reuseODEStepSize (1)                   */
+  int32_t trial_count_maximum;     /* trialCountMaximum (8)                  */
+  int32_t step_budget;             /* attempted steps per node before XCPU   */
+  uint32_t physics;                /* GAL_PHYS_* mask                        */
+  /* cosmologyParameters simple */
+  double omega_matter, omega_baryon, omega_dark_energy, hubble_constant;
+  /* hot halo: betaProfile with virialFraction core radius, virial T profile */
+  double core_radius_fraction;     /* coreRadiusOverVirialRadius (0.3)       */
+  double cooling_velocity_cutoff;  /* coolingRateWhiteFrenk1991 (1e4 km/s)   */
+  double cooling_degrees_of_freedom; /* coolingTimeSimple (3)                */
+  double reincorporation_multiplier; /* haloDynamicalTime multiplier (5)     */
+  /* galacticStructureSolverFixed: r = f lambda r_vir, v = v_vir */
+  double radius_factor_disk, radius_factor_spheroid; /* sqrt(1/2)          */
+  gal_star_formation sf_disk, sf_spheroid;
+  /* stellarPopulationPropertiesInstantaneous */
+  double recycled_fraction;        /* 0.46                                   */
+  double metal_yield;              /* 0.035                                  */
+  gal_outflow outflow_disk, outflow_spheroid;
+  /* blackHoleAccretionRateStandard + Shakura-Sunyaev thin disk */
+  double bh_enhancement_spheroid;  /* 5                                      */
+  double bh_enhancement_hot_halo;  /* 6                                      */
+  double bh_temperature_spheroid;  /* K (100)                                */
+  int32_t bh_hot_mode_only;        /* 1                                      */
+  int32_t pad;
+  double bh_efficiency_radiative;  /* 1 - E_ISCO(spin 0) = 1 - sqrt(8/9)     */
+  double bh_efficiency_jet;        /* 0                                      */
+} gal_params;
+
+/* Cooling-function and electron-density tables in the layout of the
+ * reference's CIE files (cooling_function/CIE_file.F90:535-663,
+ * chemical/state/CIE_file.F90:617-760): temperatures in K, metallicities as
+ * Z/Zsun (the first may be zero), cooling_rate in erg cm^3 s^-1 and
+ * electron_density as n_e/n_H, both row-major [iZ][iT]. */
+typedef struct gal_cie_table {
+  int32_t n_temperature;
+  int32_t n_metallicity;
+  const double* temperature;
+  const double* metallicity;
+  const double* cooling_rate;
+  const double* electron_density;
+} gal_cie_table;
+
+typedef struct gal_ctx gal_ctx;
+
+/* Fill `p` with the P-std defaults. */
+void gal_params_default(gal_params* p);
+
+/* Library version string. */
+const char* gal_version(void);
+
+/* Create a context on the current CUDA device: validate the parameters,
+ * take the log of the tables as the reference does, stage them in device
+ * memory and pick launch shapes.  Replaces the constructor
+ * mergerTreeNodeEvolverStandard (standard.F90:313-383) plus the class
+ * objects it builds from the parameter file. */
+int gal_gpu_init(const gal_params* p, const gal_cie_table* table, gal_ctx** out);
+
+/* Release a context and its device memory. */
+void gal_gpu_free(gal_ctx* ctx);
+
+/* Copy the last error message of `ctx` (or of the library, if ctx is NULL)
+ * into buf (at most len bytes, NUL terminated).  Returns the error code. */
+int gal_gpu_last_error(const gal_ctx* ctx, char* buf, int len);
+
+/* Evolve n independent nodes, node i from t_start[i] to t_end[i] (Gyr).
+ * Batched form of mergerTreeNodeEvolver%evolve (node_evolver/_class.F90:41-57,
+ * standard.F90:385-755) for nodes that are not interrupted.
+ *   state     [GAL_NY][n]  in/out  evolved properties
+ *   param     [GAL_NP][n]  in      GAL_P_* inputs
+ *   t_start, t_end [n]     in
+ *   step      [n]          in/out  node%timeStep(): the step size to try
+ *                                  first (<= 0: the whole interval); on
+ *                                  success the suggested next step
+ *   status    [n]          out     GAL_STATUS_*
+ *   counters  [3][n]       out     accepted steps, rejected steps, RHS
+ *                                  evaluations (may be NULL)
+ * Host pointers; the call copies inputs to the device, evolves and copies
+ * the outputs back before it returns. */
+int gal_gpu_evolve_batch(gal_ctx* ctx, int64_t n, double* state, const double* param,
+                         const double* t_start, const double* t_end, double* step,
+                         int32_t* status, uint32_t* counters);
+
+/* As gal_gpu_evolve_batch, on device-resident arrays, enqueued on `stream`
+ * (a cudaStream_t used as given; NULL is the legacy default stream).
+ * Asynchronous: the results are ready when the stream reaches this point. */
+int gal_gpu_evolve_batch_device(gal_ctx* ctx, int64_t n, double* state, const double* param,
+                                const double* t_start, const double* t_end, double* step,
+                                int32_t* status, uint32_t* counters, void* stream);
+
+/* Launch shape of the evolve kernel (threads per block, blocks per SM); 0
+ * keeps the current value.  Used by the autotuner. */
+int gal_gpu_set_launch(gal_ctx* ctx, int32_t threads_per_block, int32_t blocks_per_sm);
+int gal_gpu_get_launch(const gal_ctx* ctx, int32_t* threads_per_block, int32_t* blocks_per_sm);
+
+/* Number of kernel launches this context has made since creation. */
+int64_t gal_gpu_launch_count(const gal_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GALNODE_H */

@@ -1,0 +1,113 @@
+"""ctypes loader of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
+the checker and by bench.py for the timed CPU baseline.  The product never
+imports this module.
+"""
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from galacticus_gb300 import _abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+_lib = None
+
+
+def build():
+    """Compile the oracle with its Makefile (a second or two)."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        l = ctypes.CDLL(LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int32)
+        up = ctypes.POINTER(ctypes.c_uint32)
+        u64p = ctypes.POINTER(ctypes.c_uint64)
+        pp = ctypes.POINTER(_abi.Params)
+        tp = ctypes.POINTER(_abi.CieTable)
+        l.oracle_evolve_batch.argtypes = [pp, tp, ctypes.c_int64, dp, dp, dp, dp, dp, ip, up, ctypes.c_int, ctypes.c_int]
+        l.oracle_evolve_batch.restype = ctypes.c_int
+        l.oracle_cooling_function.argtypes = [tp, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        l.oracle_cooling_function.restype = ctypes.c_double
+        l.oracle_electron_density.argtypes = [tp, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        l.oracle_electron_density.restype = ctypes.c_double
+        l.oracle_cooling_radius.argtypes = [pp, tp, dp, ctypes.c_double, ctypes.c_double, ctypes.c_int]
+        l.oracle_cooling_radius.restype = ctypes.c_double
+        l.oracle_rhs.argtypes = [pp, tp, dp, dp, dp]
+        l.oracle_rhs.restype = ctypes.c_int
+        l.oracle_ode_test.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, dp, ctypes.c_double, ctypes.c_double]
+        l.oracle_ode_test.restype = ctypes.c_int
+        l.oracle_count_flops.argtypes = [pp, tp, dp, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, u64p, up]
+        l.oracle_count_flops.restype = ctypes.c_int
+        _lib = l
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def evolve_batch(params, table, state, param, t_start, t_end, step, threads=0, brent=True):
+    """Evolve copies of the given SoA arrays on the CPU.  Returns
+    (state, step, status, counters)."""
+    n = state.shape[1]
+    state = np.ascontiguousarray(state, dtype=np.float64).copy()
+    param = np.ascontiguousarray(param, dtype=np.float64)
+    t_start = np.ascontiguousarray(t_start, dtype=np.float64)
+    t_end = np.ascontiguousarray(t_end, dtype=np.float64)
+    step = np.ascontiguousarray(step, dtype=np.float64).copy()
+    status = np.zeros(n, dtype=np.int32)
+    counters = np.zeros((3, n), dtype=np.uint32)
+    rc = lib().oracle_evolve_batch(
+        ctypes.byref(params), ctypes.byref(table.struct), n, _dp(state), _dp(param), _dp(t_start), _dp(t_end),
+        _dp(step), status.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+        counters.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), int(threads), 1 if brent else 0)
+    if rc != 0:
+        raise RuntimeError(f"oracle_evolve_batch failed with code {rc}")
+    return state, step, status, counters
+
+
+def ode_test(problem, x0, x1, y, tol_abs, tol_rel):
+    y = np.ascontiguousarray(y, dtype=np.float64).copy()
+    rc = lib().oracle_ode_test(problem, x0, x1, _dp(y), tol_abs, tol_rel)
+    return rc, y
+
+
+def rhs(params, table, param_node, y):
+    param_node = np.ascontiguousarray(param_node, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    d = np.zeros(_abi.NY)
+    rc = lib().oracle_rhs(ctypes.byref(params), ctypes.byref(table.struct), _dp(param_node), _dp(y), _dp(d))
+    if rc:
+        raise RuntimeError(f"oracle_rhs failed with code {rc}")
+    return d
+
+
+def cooling_radius(params, table, param_node, mass_hot, metals_hot, brent=True):
+    param_node = np.ascontiguousarray(param_node, dtype=np.float64)
+    return lib().oracle_cooling_radius(ctypes.byref(params), ctypes.byref(table.struct), _dp(param_node),
+                                       mass_hot, metals_hot, 1 if brent else 0)
+
+
+def count_flops(params, table, param_node, y, t0, t1, step=-1.0):
+    """Operation counts (add, mul, div, sqrt, log, exp, pow, atan, cbrt) and
+    the (accepted, rejected, rhs) counters of one node evolution."""
+    param_node = np.ascontiguousarray(param_node, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64).copy()
+    ops = np.zeros(9, dtype=np.uint64)
+    counters = np.zeros(3, dtype=np.uint32)
+    lib().oracle_count_flops(ctypes.byref(params), ctypes.byref(table.struct), _dp(param_node), _dp(y), t0, t1, step,
+                             ops.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                             counters.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+    return ops, counters

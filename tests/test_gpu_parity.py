@@ -1,0 +1,140 @@
+"""GPU kernel vs CPU oracle: parity of final masses and metal masses.
+
+Each final value must lie within ten times the ODE tolerance of the oracle in
+the solver's mixed norm (oracle/compare.py).  Runs through the C ABI.
+"""
+
+import numpy as np
+import pytest
+
+from galacticus_gb300 import _abi, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def evolver(table):
+    from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
+    ev = MergerTreeNodeEvolverStandard(params=workloads.isolated_params(), table=table)
+    yield ev
+    ev.close()
+
+
+def run_both(ev, oracle_mod, batch, params=None):
+    params = params or ev.params
+    gpu = batch.copy()
+    status, counters = ev.evolve(gpu.state, gpu.param, gpu.t_start, gpu.t_end, gpu.step, return_status=True,
+                                 counters=True)
+    ref_state, ref_step, ref_status, ref_counters = oracle_mod.evolve_batch(
+        params, ev.table, batch.state, batch.param, batch.t_start, batch.t_end, batch.step)
+    return gpu, status, counters, ref_state, ref_step, ref_status, ref_counters
+
+
+def test_isolated_halos_parity(evolver, oracle_mod):
+    from oracle import compare
+    batch = workloads.isolated_halos(n=8192, seed=2)
+    gpu, status, counters, ref, ref_step, ref_status, ref_counters = run_both(evolver, oracle_mod, batch)
+    assert np.all(status == 0) and np.all(ref_status == 0)
+    ratio = compare.parity_ratio(gpu.state, ref, batch.state, batch.param, evolver.params)
+    assert ratio.max() <= 1.0, f"worst parity ratio {ratio.max():.3g}"
+    # Same step sequence in practice: accepted-step counts agree for almost every node.
+    same = (counters[0] == ref_counters[0]) & (counters[1] == ref_counters[1])
+    assert np.mean(same) > 0.99
+    # Where the step sequences agree, so does the suggested next step.  The
+    # suggestion scales as (error ratio)^(-1/6), and the embedded error is a
+    # cancellation-prone difference of stage slopes, so allow 5% on the few
+    # nodes whose error sits at rounding level.
+    rel = np.abs(gpu.step[same] / ref_step[same] - 1.0)
+    assert np.mean(rel < 1e-4) > 0.99 and rel.max() < 0.05
+
+
+@pytest.mark.parametrize("n", [1, 7, 33, 1000])
+def test_ragged_sizes(evolver, oracle_mod, n):
+    from oracle import compare
+    batch = workloads.isolated_halos(n=n, seed=11)
+    gpu, status, _, ref, _, ref_status, _ = run_both(evolver, oracle_mod, batch)
+    assert np.all(status == ref_status)
+    assert compare.parity_ratio(gpu.state, ref, batch.state, batch.param, evolver.params).max() <= 1.0
+
+
+def test_empty_batch(evolver):
+    state = np.zeros((_abi.NY, 0))
+    status = evolver.evolve(state, np.zeros((_abi.NP, 0)), np.zeros(0), np.zeros(0), np.zeros(0), return_status=True)
+    assert status.shape == (0,)
+
+
+def test_zero_interval_sets_unset_step(evolver):
+    batch = workloads.isolated_halos(n=40, seed=3)
+    batch.t_end[:] = batch.t_start
+    batch.step[:] = 0.5
+    gpu = batch.copy()
+    status = evolver.evolve(gpu.state, gpu.param, gpu.t_start, gpu.t_end, gpu.step, return_status=True)
+    assert np.all(status == 0)
+    np.testing.assert_array_equal(gpu.state, batch.state)
+    assert np.all(gpu.step == -1.0)
+
+
+def test_step_reuse_matches_oracle(evolver, oracle_mod):
+    from oracle import compare
+    batch = workloads.isolated_halos(n=2048, seed=5)
+    batch.step[:] = 0.003  # a previous node%timeStep(): first trial starts from it
+    gpu, status, counters, ref, ref_step, ref_status, ref_counters = run_both(evolver, oracle_mod, batch)
+    assert np.all(status == 0) and np.all(ref_status == 0)
+    assert compare.parity_ratio(gpu.state, ref, batch.state, batch.param, evolver.params).max() <= 1.0
+    assert np.mean(counters[0] == ref_counters[0]) > 0.99
+
+
+def test_failure_statuses_match_oracle(table, oracle_mod):
+    """Host-made failures: a tolerance no step can meet (all trials fail ->
+    errorStatusUnderflow) and a tiny step budget (-> errorStatusXCPU)."""
+    from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
+    batch = workloads.isolated_halos(n=64, seed=7)
+    p = workloads.isolated_params()
+    p.ode_tolerance_relative = 0.0
+    p.ode_tolerance_absolute = 1.0e-300  # no representable step meets this
+    ev = MergerTreeNodeEvolverStandard(params=p, table=table)
+    gpu, status, _, ref, _, ref_status, _ = run_both(ev, oracle_mod, batch, p)
+    ev.close()
+    # Acceptance at this tolerance only happens when an embedded error
+    # rounds to exactly zero, which depends on FMA contraction; nearly every
+    # node fails every trial on both sides.
+    assert np.mean(ref_status == _abi.STATUS_UNDERFLOW) > 0.9
+    assert np.mean(status == ref_status) > 0.95
+    failed = status == _abi.STATUS_UNDERFLOW
+    np.testing.assert_array_equal(gpu.state[:, failed], batch.state[:, failed])  # failed nodes keep their input state
+    p = workloads.isolated_params()
+    p.step_budget = 2
+    ev = MergerTreeNodeEvolverStandard(params=p, table=table)
+    gpu, status, _, ref, _, ref_status, _ = run_both(ev, oracle_mod, batch, p)
+    ev.close()
+    assert np.any(ref_status == _abi.STATUS_XCPU)
+    np.testing.assert_array_equal(status, ref_status)
+
+
+def test_closed_and_leaky_box_on_gpu(table):
+    """The reference's closedBox/leakyBox reproducibility answers
+    (testSuite/test-reproducibility.py:47-67) from the GPU kernel."""
+    from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
+    from cases import box_case
+    for name, (p, batch, expect, tol) in box_case().items():
+        ev = MergerTreeNodeEvolverStandard(params=p, table=table)
+        b = batch.copy()
+        ev.evolve(b.state, b.param, b.t_start, b.t_end, b.step)
+        ev.close()
+        got = [b.state[_abi.Y_DISK_GAS, 0], b.state[_abi.Y_DISK_STARS, 0], b.state[_abi.Y_DISK_GAS_METALS, 0],
+               b.state[_abi.Y_DISK_STARS_METALS, 0]]
+        np.testing.assert_allclose(got, expect, rtol=tol, err_msg=name)
+
+
+def test_launch_shapes_agree(evolver, oracle_mod):
+    """Every autotuner launch shape gives the same result bit for bit."""
+    batch = workloads.isolated_halos(n=3000, seed=9)
+    results = []
+    for threads in (64, 128, 256, 512):
+        evolver.set_launch(threads, 1)
+        b = batch.copy()
+        evolver.evolve(b.state, b.param, b.t_start, b.t_end, b.step)
+        results.append(b.state)
+    evolver.set_launch(128, 1)
+    for r in results[1:]:
+        np.testing.assert_array_equal(r, results[0])
