@@ -56,9 +56,10 @@ struct Batch {
   unsigned long long* queue;  // work-queue head (device scratch, zeroed before launch)
 };
 
-// Shared-memory layout: [nZ*nT] double2 tables, then ln T [nT], ln Z [nZ].
+// Shared-memory layout: [nZ*nT] double2 tables, then ln T [nT], ln Z [nZ]
+// and 1/(ln Z[i+1] - ln Z[i]) [nZ].
 __host__ __device__ inline size_t shared_bytes(int nT, int nZ) {
-  return (size_t)nZ * nT * sizeof(double2) + (size_t)(nT + nZ) * sizeof(double);
+  return (size_t)nZ * nT * sizeof(double2) + (size_t)(nT + 2 * nZ) * sizeof(double);
 }
 
 template <int THREADS>
@@ -70,9 +71,10 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const double2* __restr
   double2* sTab = smem;
   double* sLnT = reinterpret_cast<double*>(sTab + nZ * nT);
   double* sLnZ = sLnT + nT;
+  double* sInvDlnZ = sLnZ + nZ;
   for (int i = threadIdx.x; i < nZ * nT; i += blockDim.x) sTab[i] = gTab[i];
   for (int i = threadIdx.x; i < nT; i += blockDim.x) sLnT[i] = gLnT[i];
-  for (int i = threadIdx.x; i < nZ; i += blockDim.x) sLnZ[i] = gLnZ[i];
+  for (int i = threadIdx.x; i < 2 * nZ; i += blockDim.x) sLnZ[i] = gLnZ[i];  // ln Z, then the reciprocal spacings
   __syncthreads();
 
   const int lane = threadIdx.x & 31;
@@ -138,7 +140,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const double2* __restr
         }
         t = t0;
         count = 0;
-        rhs(G, sTab, sLnZ, c, y, k1);  // dydt_in of the first step
+        rhs(G, sTab, sLnZ, sInvDlnZ, c, y, k1);  // dydt_in of the first step
         ++nRhs;
         phase = PH_STEP;
       }
@@ -151,31 +153,37 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const double2* __restr
       const double hh = finalStep ? dt : h;
 #pragma unroll
       for (int i = 0; i < GAL_NY; ++i) tmp[i] = y[i] + ck::b21 * hh * k1[i];
-      rhs(G, sTab, sLnZ, c, tmp, k2);
+      rhs(G, sTab, sLnZ, sInvDlnZ, c, tmp, k2);
 #pragma unroll
       for (int i = 0; i < GAL_NY; ++i) tmp[i] = y[i] + hh * (ck::b31 * k1[i] + ck::b32 * k2[i]);
-      rhs(G, sTab, sLnZ, c, tmp, k3);
+      rhs(G, sTab, sLnZ, sInvDlnZ, c, tmp, k3);
 #pragma unroll
       for (int i = 0; i < GAL_NY; ++i) tmp[i] = y[i] + hh * (ck::b41 * k1[i] + ck::b42 * k2[i] + ck::b43 * k3[i]);
-      rhs(G, sTab, sLnZ, c, tmp, k4);
+      rhs(G, sTab, sLnZ, sInvDlnZ, c, tmp, k4);
 #pragma unroll
       for (int i = 0; i < GAL_NY; ++i)
         tmp[i] = y[i] + hh * (ck::b51 * k1[i] + ck::b52 * k2[i] + ck::b53 * k3[i] + ck::b54 * k4[i]);
-      rhs(G, sTab, sLnZ, c, tmp, k5);
+      rhs(G, sTab, sLnZ, sInvDlnZ, c, tmp, k5);
 #pragma unroll
       for (int i = 0; i < GAL_NY; ++i)
         tmp[i] = y[i] + hh * (ck::b61 * k1[i] + ck::b62 * k2[i] + ck::b63 * k3[i] + ck::b64 * k4[i] + ck::b65 * k5[i]);
-      rhs(G, sTab, sLnZ, c, tmp, k6);
+      rhs(G, sTab, sLnZ, sInvDlnZ, c, tmp, k6);
       nRhs += 5;
       // 5th-order solution into tmp, scaled error ratio (sc2_control_hadjust, a_y=1, a_dydt=0).
-      double rmax = 2.2250738585072014e-308;  // DBL_MIN
+      // The largest |err_i|/D_i is found by cross-multiplication and divided
+      // once (max of the quotients = quotient of the maximal pair).
+      double errMax = 0.0, dMax = 1.0;
 #pragma unroll
       for (int i = 0; i < GAL_NY; ++i) {
         tmp[i] = y[i] + hh * (ck::c1 * k1[i] + ck::c3 * k3[i] + ck::c4 * k4[i] + ck::c6 * k6[i]);
-        const double err = hh * (ck::e1 * k1[i] + ck::e3 * k3[i] + ck::e4 * k4[i] + ck::e5 * k5[i] + ck::e6 * k6[i]);
-        const double D0 = epsRel * fabs(tmp[i]) + epsAbs * s[i];
-        rmax = fmax(fabs(err) / fabs(D0), rmax);
+        const double err = fabs(hh * (ck::e1 * k1[i] + ck::e3 * k3[i] + ck::e4 * k4[i] + ck::e5 * k5[i] + ck::e6 * k6[i]));
+        const double D0 = fabs(epsRel * fabs(tmp[i]) + epsAbs * s[i]);
+        if (err * dMax > errMax * D0 || !(err == err)) {
+          errMax = err;
+          dMax = D0;
+        }
       }
+      const double rmax = fmax(errMax / dMax, 2.2250738585072014e-308);  // floor DBL_MIN as cscal2.c
       ++count;
       const double tNew = finalStep ? t1 : t + hh;
       double hNew = hh;
@@ -215,7 +223,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const double2* __restr
         ++nAcc;
         const bool reached = !(t1 - t > 0.0 || t1 - t < 0.0);
         if (!reached) {
-          rhs(G, sTab, sLnZ, c, y, k1);  // dydt_out, reused as the next dydt_in
+          rhs(G, sTab, sLnZ, sInvDlnZ, c, y, k1);  // dydt_out, reused as the next dydt_in
           ++nRhs;
         }
         post_step(y);  // clamps return GSL_Continue: dydt_out is kept
@@ -429,9 +437,11 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
   g.accretionFraction = p->omega_baryon / p->omega_matter;
 
   std::vector<double2> tab((size_t)nZ * nT);
-  std::vector<double> lnT(nT), lnZ(nZ);
+  std::vector<double> lnT(nT), lnZ(2 * nZ, 0.0);
   for (int i = 0; i < nT; ++i) lnT[i] = std::log(t->temperature[i]);
   for (int j = 0; j < nZ; ++j) lnZ[j] = t->metallicity[j] > 0.0 ? std::log(t->metallicity[j]) : -999.0;
+  for (int j = 0; j + 1 < nZ; ++j) lnZ[nZ + j] = 1.0 / (lnZ[j + 1] - lnZ[j]);
+  g.invFirstNonZero = 1.0 / g.firstNonZero;
   for (int i = 0; i < nZ * nT; ++i) tab[i] = make_double2(std::log(t->cooling_rate[i]), std::log(t->electron_density[i]));
 
   auto cleanup = [&](int code) {
@@ -441,7 +451,7 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMalloc(&ctx->dTab, tab.size() * sizeof(double2)) != cudaSuccess ||
       cudaMalloc(&ctx->dLnT, nT * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&ctx->dLnZ, nZ * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&ctx->dLnZ, 2 * nZ * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&ctx->dQueue, sizeof(unsigned long long)) != cudaSuccess) {
     cudaGetLastError();
     fail(nullptr, GAL_ERR_CUDA, "device allocation failed%s");
@@ -449,7 +459,7 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
   }
   if (cudaMemcpy(ctx->dTab, tab.data(), tab.size() * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(ctx->dLnT, lnT.data(), nT * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(ctx->dLnZ, lnZ.data(), nZ * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaMemcpy(ctx->dLnZ, lnZ.data(), 2 * nZ * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
     fail(nullptr, GAL_ERR_CUDA, "table upload failed%s");
     return cleanup(GAL_ERR_CUDA);
   }

@@ -54,6 +54,7 @@ struct Globals {
   int nT, nZ;                 // table shape
   int firstZero;              // first metallicity row is Z = 0
   double firstNonZero;        // Z/Zsun of the first non-zero row
+  double invFirstNonZero;
   double Tmin, Tmax, Zmin, Zmax;
   double soundSpeedSpheroid;  // km/s at bh_temperature_spheroid
   double jeansPrefactor;      // c_s/sqrt(G) for the spheroid gas
@@ -63,34 +64,43 @@ struct Globals {
   double accretionFraction;   // Omega_b / Omega_m
 };
 
-// Per-node constants of one evolve call.
+// Per-node constants of one evolve call.  Reciprocals of the per-node
+// lengths and times are taken here once, so that the right-hand side
+// multiplies instead of dividing (an FP64 divide is ~10 slow-pipe
+// instructions on GB300).
 struct NodeC {
   double massHalo;            // basic mass at the start (tolerance scale)
   double tdyn;                // halo dynamical time r_vir/V_vir (Gyr)
+  double invTdyn;
   double rcore;               // beta-profile core radius (Mpc)
+  double invRcore;
   double rho0PerMass;         // central beta-profile density per unit hot mass
   double rOuter;              // hot-halo outer radius = virial radius (Mpc)
+  double invRvir;
   double onePlusXOuter2;      // 1 + (r_outer/r_core)^2
   double coolingTimeCoef;     // coolingCoef * T_vir
+  double coolingRateCoef;     // 2 pi rho0PerMass r_core^2 / t_dyn
   double hT;                  // temperature interpolation weight
   int iT;                     // temperature cell of T_vir
   int coolingAllowed;         // V_vir <= velocity cut-off
   double sfrDisk, sfrSph;     // 1/tau_* of the disk and spheroid (0: none)
   double outDisk, outSph;     // outflow rate per unit SFR
-  double outDiskMax, outSph_max; // 1/(t_dyn f_min) of the rate limit (<0: no limit)
+  double outDiskMax, outSphMax; // 1/(t_dyn f_min) of the rate limit (<0: no limit)
   double aSph;                // spheroid scale radius (Mpc)
+  double invASph;
   double rhoSphPerMass;       // 1/(2 pi a^3)
   double radiusDisk;          // disk radius (Mpc)
   double bhRadiusHotCoef;     // G / c_s(T_vir)^2
   double bhHotCoef;           // enhancement * bhl * c_s(T_vir)
   double bhHotMaxCoef;        // c_s/(r_outer MpcPerKmPerSToGyr)
   double accretionRate;       // hot-gas accretion rate (Msun/Gyr)
-  double rvir;
+  double reincorporationRate; // multiplier / t_dyn
 };
 
-__device__ __forceinline__ double mass_fraction(double metals, double mass) {
-  // Abundances_Mass_To_Mass_Fraction_Packed (objects/abundances.F90:781-809)
-  return metals > mass ? 1.0 : (metals <= 0.0 ? 0.0 : metals / mass);
+// Abundances_Mass_To_Mass_Fraction_Packed (objects/abundances.F90:781-809)
+// given the reciprocal of the mass.
+__device__ __forceinline__ double mass_fraction(double metals, double mass, double invMass) {
+  return metals > mass ? 1.0 : (metals <= 0.0 ? 0.0 : metals * invMass);
 }
 
 // Largest i with g[i] <= x, kept in [0, n-2]; g in shared memory.
@@ -113,16 +123,19 @@ __device__ __forceinline__ void node_setup(const Globals& G, const double* sLnT,
   const double M = prm[GAL_P_MASS], Mdot = prm[GAL_P_MASS_RATE];
   const double rvir = prm[GAL_P_RADIUS_VIRIAL], vvir = prm[GAL_P_VELOCITY_VIRIAL], spin = prm[GAL_P_SPIN];
   c.massHalo = M;
-  c.rvir = rvir;
   // virialDensityContrastDefinition{VirialTemperature,DynamicalTimescale} (virial_density_contrast.F90:195-262)
   const double T = 0.5 * k::atomicMassUnit * k::meanAtomicMassPrimordial * (k::kilo * vvir) * (k::kilo * vvir) / k::boltzmannsConstant;
   c.tdyn = rvir / vvir * k::MpcPerKmPerSToGyr;
+  c.invTdyn = 1.0 / c.tdyn;
   c.rcore = p.core_radius_fraction * rvir;
+  c.invRcore = 1.0 / c.rcore;
   c.rOuter = rvir;  // outer radius clamp of hot_halo/standard/_class.F90:430-450
+  c.invRvir = 1.0 / rvir;
   const double x = c.rOuter / c.rcore;
   const double norm = x < 1.0e-6 ? 3.0 / (x * x * x) + 9.0 / 5.0 / x - 36.0 * x / 175.0 : 1.0 / (x - atan(x));
   c.rho0PerMass = norm / (4.0 * k::Pi) / (c.rcore * c.rcore * c.rcore);
   c.onePlusXOuter2 = 1.0 + x * x;
+  c.coolingRateCoef = 2.0 * k::Pi * c.rho0PerMass * c.rcore * c.rcore * c.invTdyn;
   // Temperature coordinate of the CIE tables ("extrapolate" in T = clamp).
   const double Tc = fmin(fmax(T, G.Tmin), G.Tmax);
   const double lnT = log(Tc);
@@ -134,6 +147,7 @@ __device__ __forceinline__ void node_setup(const Globals& G, const double* sLnT,
   const double Rd = p.radius_factor_disk * spin * rvir, Rs = p.radius_factor_spheroid * spin * rvir;
   c.radiusDisk = Rd;
   c.aSph = Rs;
+  c.invASph = Rs > 0.0 ? 1.0 / Rs : 0.0;
   c.rhoSphPerMass = Rs > 0.0 ? 1.0 / (2.0 * k::Pi) / (Rs * Rs * Rs) : 0.0;
   // Star-formation timescales (star_formation/timescales/dynamical_time.F90:121-189).
   auto timescale = [&](const gal_star_formation& sf, double R) -> double {
@@ -159,44 +173,35 @@ __device__ __forceinline__ void node_setup(const Globals& G, const double* sLnT,
   c.outDisk = loading(p.outflow_disk);
   c.outSph = loading(p.outflow_spheroid);
   c.outDiskMax = limit(p.outflow_disk, Rd);
-  c.outSph_max = limit(p.outflow_spheroid, Rs);
+  c.outSphMax = limit(p.outflow_spheroid, Rs);
   // Hot-halo Bondi accretion constants at the virial temperature.
   const double cs = sqrt(5.0 * k::boltzmannsConstant * T / 3.0 / k::meanAtomicMassPrimordial / k::atomicMassUnit) / k::kilo;
   c.bhRadiusHotCoef = T > 0.0 ? k::gravitationalConstantInternal / (cs * cs) : 0.0;
   c.bhHotCoef = p.bh_enhancement_hot_halo * k::bhlPrefactor * cs;
   c.bhHotMaxCoef = cs / (c.rOuter * k::MpcPerKmPerSToGyr);
   c.accretionRate = Mdot > 0.0 ? G.accretionFraction * Mdot : 0.0;
-}
-
-// Hydrogen mass and number fractions of gas of metal mass fraction Z
-// (objects/abundances.F90:830-883).
-__device__ __forceinline__ void hydrogen_fractions(double Z, double& xMass, double& xNumber) {
-  const double zs = Z * (1.0 / k::metallicitySolar);
-  const double xH = fmin(fmax(zs * (k::hydrogenByMassSolar - k::hydrogenByMassPrimordial) + k::hydrogenByMassPrimordial, 0.7),
-                         k::hydrogenByMassPrimordial);
-  const double yHe = fmin(zs * (k::heliumByMassSolar - k::heliumByMassPrimordial) + k::heliumByMassPrimordial, k::heliumByMassPrimordial);
-  const double nH = xH * (1.0 / k::atomicMassHydrogen), nHe = yHe * (1.0 / k::atomicMassHelium);
-  xMass = xH;
-  xNumber = nH / (nH + nHe);
+  c.reincorporationRate = p.reincorporation_multiplier * c.invTdyn;
 }
 
 // Interpolated cooling function (erg cm^3 s^-1, without the n_H^2 factor)
 // and n_e/n_H at the node temperature and metallicity Z/Zsun
 // (cooling_function/CIE_file.F90:238-317, 665-735; chemical/state/
-// CIE_file.F90:245-320).  `tab` interleaves (ln Lambda, ln n_e/n_H).
-__device__ __forceinline__ void cie_lookup(const Globals& G, const double2* tab, const double* sLnZ, const NodeC& c,
-                                          double zSolar, double& lambda, double& electrons) {
+// CIE_file.F90:245-320).  `tab` interleaves (ln Lambda, ln n_e/n_H);
+// sInvDlnZ[i] = 1/(ln Z[i+1] - ln Z[i]).
+__device__ __forceinline__ void cie_lookup(const Globals& G, const double2* tab, const double* sLnZ,
+                                          const double* sInvDlnZ, const NodeC& c, double zSolar, double& lambda,
+                                          double& electrons) {
   zSolar = fmin(fmax(zSolar, G.Zmin), G.Zmax);  // "fix" extrapolation in metallicity
   const double zUse = fmax(zSolar, 0.0);
   int iZ;
   double hZ;
   if (G.firstZero && zUse < G.firstNonZero) {
     iZ = 0;
-    hZ = zUse / G.firstNonZero;
+    hZ = zUse * G.invFirstNonZero;
   } else {
     const double lnZ = log(zUse);
     iZ = locate(sLnZ, G.nZ, lnZ);
-    hZ = (lnZ - sLnZ[iZ]) / (sLnZ[iZ + 1] - sLnZ[iZ]);
+    hZ = (lnZ - sLnZ[iZ]) * sInvDlnZ[iZ];
   }
   const int nT = G.nT;
   const double2 a = tab[iZ * nT + c.iT], b = tab[(iZ + 1) * nT + c.iT];
@@ -211,37 +216,42 @@ __device__ __forceinline__ void cie_lookup(const Globals& G, const double2* tab,
 // fixed temperature and metallicity the cooling time is proportional to
 // 1/rho (Lambda scales as n_H^2, n_e as n_H), so t_cool(r) = t_avail solves
 // as r = r_core sqrt(t_avail/t_cool(0) - 1) inside the bracket [0, r_outer]
-// that the reference's root finder searches.  t_avail = t_dyn
-// (coolingTimeAvailableWhiteFrenk1991 with ageFactor = 0).
-__device__ __forceinline__ double cooling_radius(const Globals& G, const double2* tab, const double* sLnZ, const NodeC& c,
-                                                double massHot, double metalsHot) {
-  const double Z = mass_fraction(metalsHot, massHot);
-  double xMass, xNumber;
-  hydrogen_fractions(Z, xMass, xNumber);
+// that the reference's root finder searches; t_avail = t_dyn
+// (coolingTimeAvailableWhiteFrenk1991 with ageFactor = 0).  The cooling time
+// of coolingTimeSimple (cooling_time/simple.F90:128-179) is
+//   t_cool(0) = (dof/2) k T (n_H/x_num + n_e) / ergs / (Lambda n_H^2) / Gyr
+// with n_H = rho(0) X_H and 1/x_num = 1 + (Y m_H)/(X_H m_He); the ratio
+// q = t_avail/t_cool(0) below is that expression with one division.
+__device__ __forceinline__ double cooling_radius(const Globals& G, const double2* tab, const double* sLnZ,
+                                                const double* sInvDlnZ, const NodeC& c, double massHot, double zHot) {
+  // Abundances_Hydrogen/Helium_Mass_Fraction (objects/abundances.F90:830-868).
+  const double zs = zHot * (1.0 / k::metallicitySolar);
+  const double xH = fmin(fmax(zs * (k::hydrogenByMassSolar - k::hydrogenByMassPrimordial) + k::hydrogenByMassPrimordial, 0.7),
+                         k::hydrogenByMassPrimordial);
+  const double yHe = fmin(zs * (k::heliumByMassSolar - k::heliumByMassPrimordial) + k::heliumByMassPrimordial, k::heliumByMassPrimordial);
   double lambda, electrons;
-  cie_lookup(G, tab, sLnZ, c, Z * (1.0 / k::metallicitySolar), lambda, electrons);
-  const double rho0 = massHot > 0.0 ? massHot * c.rho0PerMass : 0.0;
-  // t_cool(0) = (dof/2) k T (n_H/x_num + n_e) / ergs / (Lambda n_H^2) / Gyr, n_H = rho X_H conv.
-  const double nH0 = rho0 * xMass;  // in units of densityToHydrogenNumber
-  const double denominator = lambda * nH0;
-  const double tcool0 = denominator > 0.0 ? c.coolingTimeCoef * (1.0 / xNumber + electrons) / denominator : 1.0e10;
-  const double tAvail = c.tdyn;
-  if (tcool0 * c.onePlusXOuter2 < tAvail) return c.rOuter;
-  if (tcool0 > tAvail) return 0.0;
-  return c.rcore * sqrt(tAvail / tcool0 - 1.0);
+  cie_lookup(G, tab, sLnZ, sInvDlnZ, c, zs, lambda, electrons);
+  const double num = c.tdyn * lambda * massHot * c.rho0PerMass * xH * xH;
+  const double den = c.coolingTimeCoef * (xH * (1.0 + electrons) + yHe * (k::atomicMassHydrogen / k::atomicMassHelium));
+  const double q = massHot > 0.0 ? num / den : 0.0;
+  if (q > c.onePlusXOuter2) return c.rOuter;  // t_cool(r_outer) < t_avail
+  if (q < 1.0) return 0.0;                    // t_cool(0) > t_avail
+  return c.rcore * sqrt(q - 1.0);
 }
 
 // Right-hand side of the node ODE system: the node operators of
 // nodeOperatorMulti (nodes/operators/multi.F90:313-332) in the order of
 // parameters/quickTest.xml.  Same logic, branch by branch, as the oracle.
-__device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const double* sLnZ, const NodeC& c,
-                                   const double* y, double* dydt) {
+__device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const double* sLnZ, const double* sInvDlnZ,
+                                   const NodeC& c, const double* y, double* dydt) {
   const gal_params& p = G.p;
   const uint32_t ph = p.physics;
 #pragma unroll
   for (int i = 0; i < GAL_NY; ++i) dydt[i] = 0.0;
   const double massHot = y[GAL_Y_HOT_MASS], metalsHot = y[GAL_Y_HOT_METALS];
   const double gasDisk = y[GAL_Y_DISK_GAS], gasSph = y[GAL_Y_SPHEROID_GAS];
+  const double invHot = massHot > 0.0 ? 1.0 / massHot : 0.0;
+  const double zHot = mass_fraction(metalsHot, massHot, invHot);
   bool coolingRadiusKnown = false;
   double rCool = 0.0;
 
@@ -249,7 +259,8 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
   // (stellar_populations/properties/instantaneous.F90:133-219).
   const bool diskOk = !(c.radiusDisk < 0.0 || gasDisk < 0.0);
   const double sfrDisk = diskOk ? gasDisk * c.sfrDisk : 0.0;
-  const double zDisk = mass_fraction(y[GAL_Y_DISK_GAS_METALS], gasDisk);
+  const double zDisk = gasDisk > 0.0 ? mass_fraction(y[GAL_Y_DISK_GAS_METALS], gasDisk, 1.0 / gasDisk)
+                                     : mass_fraction(y[GAL_Y_DISK_GAS_METALS], gasDisk, 0.0);
   if ((ph & GAL_PHYS_STAR_FORMATION_DISK) && diskOk) {
     const double rateStars = (1.0 - p.recycled_fraction) * sfrDisk;
     const double rateMetals = zDisk * rateStars;
@@ -261,20 +272,18 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
   // starFormationSpheroids (star_formation/spheroids.F90:152-)
   const bool sphOk = !(c.aSph < 1.0e-12 || gasSph < 1.0e-6);
   const double sfrSph = sphOk ? gasSph * c.sfrSph : 0.0;
-  const double zSph = mass_fraction(y[GAL_Y_SPHEROID_GAS_METALS], gasSph);
+  const double invSph = gasSph > 0.0 ? 1.0 / gasSph : 0.0;
+  const double zSph = mass_fraction(y[GAL_Y_SPHEROID_GAS_METALS], gasSph, invSph);
   if ((ph & GAL_PHYS_STAR_FORMATION_SPHEROID) && sphOk) {
     const double rateStars = (1.0 - p.recycled_fraction) * sfrSph;
     dydt[GAL_Y_SPHEROID_STARS] += rateStars;
     dydt[GAL_Y_SPHEROID_GAS] += -rateStars;
     dydt[GAL_Y_SPHEROID_GAS_METALS] += -(zSph * rateStars) + p.metal_yield * sfrSph;
   }
-  // stellarFeedbackDisks (stellar_feedback/disks.F90:116-205)
+  // stellarFeedbackDisks (stellar_feedback/disks.F90:116-205); rateLimit caps at the maximum.
   if ((ph & GAL_PHYS_FEEDBACK_DISK) && diskOk) {
     double total = c.outDisk * sfrDisk;
-    if (c.outDiskMax >= 0.0) {
-      const double maximum = fmax(gasDisk * c.outDiskMax, 0.0);
-      if (total > maximum) total = total * maximum / total;
-    }
+    if (c.outDiskMax >= 0.0) total = fmin(total, fmax(gasDisk * c.outDiskMax, 0.0));
     if (total > 0.0) {
       const double metals = gasDisk > 0.0 ? zDisk * total : 0.0;
       dydt[GAL_Y_OUTFLOWED_MASS] += total;
@@ -286,10 +295,7 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
   // stellarFeedbackSpheroids (stellar_feedback/spheroids.F90:116-208)
   if ((ph & GAL_PHYS_FEEDBACK_SPHEROID) && sphOk) {
     double total = c.outSph * sfrSph;
-    if (c.outSph_max >= 0.0) {
-      const double maximum = fmax(gasSph * c.outSph_max, 0.0);
-      if (total > maximum) total = total * maximum / total;
-    }
+    if (c.outSphMax >= 0.0) total = fmin(total, fmax(gasSph * c.outSphMax, 0.0));
     if (total > 0.0) {
       const double metals = gasSph > 0.0 ? zSph * total : 0.0;
       dydt[GAL_Y_OUTFLOWED_MASS] += total;
@@ -305,19 +311,17 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
     const double eps = p.bh_efficiency_radiative;
     const double eddingtonCap = eps > 0.0 ? k::eddingtonPerMass * massBH / eps : 0.0;
     double rateSph = 0.0;
-    {
+    if (gasSph > 0.0 && c.aSph > 0.0) {
+      // Bondi-Hoyle from the spheroid gas (Hernquist density at max(r_BHL, Jeans length)).
       const double rAcc = fmax(G.bhRadiusSpheroidCoef * massBH, 0.0);
-      double rho = 0.0;
-      if (gasSph > 0.0 && c.aSph > 0.0) {
-        const double xx = rAcc / c.aSph, opx = 1.0 + xx;
-        rho = gasSph * c.rhoSphPerMass / xx / (opx * opx * opx);
-      }
+      double xx = rAcc * c.invASph, opx = 1.0 + xx;
+      double rho = gasSph * c.rhoSphPerMass / (xx * opx * opx * opx);
       if (rho > 1.0) {
-        double jeans = G.jeansPrefactor / sqrt(rho);
-        jeans = fmin(jeans, c.aSph);
+        const double jeans = fmin(G.jeansPrefactor * rsqrt(rho), c.aSph);
         if (jeans > rAcc) {
-          const double xx = jeans / c.aSph, opx = 1.0 + xx;
-          rho = gasSph * c.rhoSphPerMass / xx / (opx * opx * opx);
+          xx = jeans * c.invASph;
+          opx = 1.0 + xx;
+          rho = gasSph * c.rhoSphPerMass / (xx * opx * opx * opx);
         }
         rateSph = fmax(G.bhSpheroidCoef * massBH * massBH * rho, 0.0);
         if (eps > 0.0) rateSph = fmin(rateSph, eddingtonCap);
@@ -325,58 +329,55 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
     }
     double rateHot = 0.0;
     {
-      double rAcc = c.bhRadiusHotCoef > 0.0 ? c.bhRadiusHotCoef * massBH : HUGE_VAL;
-      rAcc = fmin(rAcc, c.rOuter);
+      const double rAcc = fmin(c.bhRadiusHotCoef > 0.0 ? c.bhRadiusHotCoef * massBH : HUGE_VAL, c.rOuter);
       double fractionHot = 1.0;
       if (p.bh_hot_mode_only) {
         // standardHotModeFraction (accretion_rates/standard.F90:442-468)
-        rCool = cooling_radius(G, tab, sLnZ, c, massHot, metalsHot);
+        rCool = cooling_radius(G, tab, sLnZ, sInvDlnZ, c, massHot, zHot);
         coolingRadiusKnown = true;
-        const double xx = rCool / c.rvir;
+        const double xx = rCool * c.invRvir;
         if (xx < 0.9) fractionHot = 1.0;
         else if (xx > 1.0) fractionHot = 0.0;
         else {
-          const double u = (xx - 0.9) / 0.1;
+          const double u = (xx - 0.9) * 10.0;
           fractionHot = u * u * (2.0 * u - 3.0) + 1.0;
         }
       }
-      double rho = 0.0;
-      if (massHot > 0.0 && !(rAcc > c.rOuter)) {
-        const double xx = rAcc / c.rcore;
-        rho = massHot * c.rho0PerMass / (1.0 + xx * xx);
-      }
-      rho *= fractionHot;
-      if (rho > 1.0) {
-        rateHot = fmax(c.bhHotCoef * rAcc * rAcc * rho, 0.0);
-        rateHot = fmin(rateHot, fmax(massHot * c.bhHotMaxCoef, 0.0));
-        if (eps > 0.0) rateHot = fmin(rateHot, eddingtonCap);
+      if (massHot > 0.0 && fractionHot > 0.0) {
+        const double xx = rAcc * c.invRcore;
+        const double rho = fractionHot * massHot * c.rho0PerMass / (1.0 + xx * xx);
+        if (rho > 1.0) {
+          rateHot = fmax(c.bhHotCoef * rAcc * rAcc * rho, 0.0);
+          rateHot = fmin(rateHot, fmax(massHot * c.bhHotMaxCoef, 0.0));
+          if (eps > 0.0) rateHot = fmin(rateHot, eddingtonCap);
+        }
       }
     }
     const double total = rateSph + rateHot;
     if (total > 0.0) {
-      const double reduced = total * (1.0 - p.bh_efficiency_radiative - p.bh_efficiency_jet);
-      dydt[GAL_Y_BLACK_HOLE] += reduced;
+      dydt[GAL_Y_BLACK_HOLE] += total * (1.0 - p.bh_efficiency_radiative - p.bh_efficiency_jet);
       // spheroid gas sink (spheroid/standard/_class.F90:638-671)
       if (rateSph != 0.0 && gasSph > 0.0 && gasSph + y[GAL_Y_SPHEROID_STARS] > 0.0) {
         dydt[GAL_Y_SPHEROID_GAS] += -rateSph;
-        dydt[GAL_Y_SPHEROID_GAS_METALS] += (-rateSph / gasSph) * y[GAL_Y_SPHEROID_GAS_METALS];
+        dydt[GAL_Y_SPHEROID_GAS_METALS] += (-rateSph * invSph) * y[GAL_Y_SPHEROID_GAS_METALS];
       }
       // hot-halo mass sink (hot_halo/standard/_class.F90:771-799)
       if (rateHot != 0.0 && massHot > 0.0) {
         dydt[GAL_Y_HOT_MASS] += -rateHot;
-        dydt[GAL_Y_HOT_METALS] += metalsHot * (-rateHot / massHot);
+        dydt[GAL_Y_HOT_METALS] += metalsHot * (-rateHot * invHot);
       }
     }
   }
   // CGMAccretion (circumgalactic_medium/accretion.F90:517-593; accretion/halo/simple.F90:281-319)
   if (ph & GAL_PHYS_CGM_ACCRETION) dydt[GAL_Y_HOT_MASS] += c.accretionRate;
   // CGMOutflowReincorporation (circumgalactic_medium/outflow_reincorporation.F90:272-349;
-  // hot_halo/outflow_reincorporation/halo_dynamical_time.F90:113-128)
+  // hot_halo/outflow_reincorporation/halo_dynamical_time.F90:113-128):
+  // rate = M_out k, metals = rate MZ_out/M_out = MZ_out k.
   if (ph & GAL_PHYS_REINCORPORATION) {
     const double massOut = y[GAL_Y_OUTFLOWED_MASS];
     if (massOut > 0.0) {
-      const double rate = massOut * p.reincorporation_multiplier / c.tdyn;
-      const double metals = rate * y[GAL_Y_OUTFLOWED_METALS] / massOut;
+      const double rate = massOut * c.reincorporationRate;
+      const double metals = y[GAL_Y_OUTFLOWED_METALS] * c.reincorporationRate;
       dydt[GAL_Y_OUTFLOWED_MASS] += -rate;
       dydt[GAL_Y_OUTFLOWED_METALS] += -metals;
       dydt[GAL_Y_HOT_MASS] += rate;
@@ -388,20 +389,18 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
   if ((ph & GAL_PHYS_COOLING) && massHot > 0.0 && c.rOuter > 0.0) {
     double rate = 0.0;
     if (c.coolingAllowed) {
-      if (!coolingRadiusKnown) rCool = cooling_radius(G, tab, sLnZ, c, massHot, metalsHot);
+      if (!coolingRadiusKnown) rCool = cooling_radius(G, tab, sLnZ, sInvDlnZ, c, massHot, zHot);
       if (rCool >= c.rOuter) {
-        rate = massHot / c.tdyn;
+        rate = massHot * c.invTdyn;
       } else if (rCool > 0.0) {
         // 4 pi r^2 rho(r) dr_cool/dt with dr/dt = r/t_avail/(2x^2/(1+x^2))
-        // (cooling_radius/simple.F90:229-311, isothermal gas).
-        const double xx = rCool / c.rcore;
-        const double slope = 2.0 * xx * xx / (xx * xx + 1.0);
-        const double growth = rCool / c.tdyn / slope;
-        rate = 4.0 * k::Pi * rCool * rCool * (massHot * c.rho0PerMass / (1.0 + xx * xx)) * growth;
+        // (cooling_radius/simple.F90:229-311, isothermal gas)
+        //   = 2 pi rho(0) r_core^2 r_cool / t_dyn.
+        rate = massHot * c.coolingRateCoef * rCool;
       }
     }
     if (rate > 0.0) {
-      const double metals = rate * metalsHot / massHot;
+      const double metals = rate * metalsHot * invHot;
       dydt[GAL_Y_HOT_MASS] += -rate;
       dydt[GAL_Y_HOT_METALS] += -metals;
       dydt[GAL_Y_DISK_GAS] += rate;
