@@ -172,6 +172,9 @@ def load_library(path=LIB_PATH):
     lib.gal_gpu_get_launch.restype = ctypes.c_int
     lib.gal_gpu_launch_count.argtypes = [vp]
     lib.gal_gpu_launch_count.restype = ctypes.c_int64
+    lib.gal_gpu_evolve_batch_noalloc.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(CieTable), ctypes.c_int64,
+                                                 vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.gal_gpu_evolve_batch_noalloc.restype = ctypes.c_int
     lib.gal_calibrate_fp64.argtypes = [dp, dp]
     lib.gal_calibrate_fp64.restype = ctypes.c_int
     _lib = lib

@@ -563,3 +563,154 @@ int gal_gpu_evolve_batch(gal_ctx* ctx, int64_t n, double* state, const double* p
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Evolution without any allocation.
+//
+// Some callers cannot let a library allocate device memory: a host code that
+// hands all device memory to its own pool allocator up front (so a library
+// cudaMalloc fails or fragments the pool), or a scheduler that must not take
+// the device-wide synchronisation that cudaMalloc/cudaFree can impose while
+// its other work is in flight.  gal_gpu_evolve_batch_noalloc serves them: the
+// caller passes every input and output in device memory it already owns, and
+// the one piece of scratch the kernel needs besides them -- the work-queue
+// head plus the log-converted CIE tables staged for the shared-memory copy --
+// lives in the file-scope array below, which every GPU that loads this
+// library holds until the process exits.
+// ===========================================================================
+#include <mutex>
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 128 * 1024;  // queue head + tables; see the size check below
+constexpr int kNoAllocThreads = 128;                  // launch shape of this entry point (one block per SM)
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
+
+std::mutex g_noallocMutex;
+void* g_noallocScratchPtr[kNoAllocMaxDevices] = {nullptr};
+
+// Scratch layout: [0,256) queue head; then the double2 table [nZ*nT];
+// then ln T [nT]; then ln Z [nZ] and 1/(ln Z[i+1]-ln Z[i]) [nZ].
+size_t noalloc_bytes(int nT, int nZ) { return 256 + shared_bytes(nT, nZ); }
+
+// In-place conversion of the staged raw table to the layout the kernel
+// reads (the logarithms of cieFileReadFile, CIE_file.F90:535-663).
+__global__ void noalloc_prepare_tables(double2* tab, double* lnT, double* lnZ, int nT, int nZ) {
+  const int stride = blockDim.x * gridDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nZ * nT; i += stride) {
+    double2 v = tab[i];
+    tab[i] = make_double2(log(v.x), log(v.y));
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nT; i += stride) lnT[i] = log(lnT[i]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    for (int j = 0; j < nZ; ++j) lnZ[j] = lnZ[j] > 0.0 ? log(lnZ[j]) : -999.0;
+    for (int j = 0; j + 1 < nZ; ++j) lnZ[nZ + j] = 1.0 / (lnZ[j + 1] - lnZ[j]);
+    lnZ[2 * nZ - 1] = 0.0;
+  }
+}
+
+}  // namespace
+
+extern "C" int gal_gpu_evolve_batch_noalloc(const gal_params* p, const gal_cie_table* t, int64_t n, double* state,
+                                            const double* param, const double* tStart, const double* tEnd, double* step,
+                                            int32_t* status, uint32_t* counters, void* stream) {
+  if (!p || !t) return fail(nullptr, GAL_ERR_ARGUMENT, "gal_gpu_evolve_batch_noalloc: params and table are required%s");
+  if (n < 0) return fail(nullptr, GAL_ERR_ARGUMENT, "gal_gpu_evolve_batch_noalloc: negative node count%s");
+  if (n == 0) return GAL_OK;
+  if (!state || !param || !tStart || !tEnd || !step || !status)
+    return fail(nullptr, GAL_ERR_ARGUMENT, "gal_gpu_evolve_batch_noalloc: NULL array%s");
+  if (!(p->ode_tolerance_absolute > 0.0 || p->ode_tolerance_relative > 0.0) || p->ode_tolerance_absolute < 0.0 ||
+      p->ode_tolerance_relative < 0.0 || p->trial_count_maximum < 1 || p->trial_count_maximum > 30)
+    return fail(nullptr, GAL_ERR_ARGUMENT, "gal_gpu_evolve_batch_noalloc: invalid tolerances or trial count%s");
+  const int nT = t->n_temperature, nZ = t->n_metallicity;
+  if (nT < 2 || nZ < 2 || !t->temperature || !t->metallicity || !t->cooling_rate || !t->electron_density)
+    return fail(nullptr, GAL_ERR_TABLE, "gal_gpu_evolve_batch_noalloc: CIE table needs at least 2x2 entries%s");
+  if (noalloc_bytes(nT, nZ) > kNoAllocScratchBytes)
+    return fail(nullptr, GAL_ERR_TOO_LARGE,
+                "gal_gpu_evolve_batch_noalloc: CIE table too large for the fixed 128 KiB scratch "
+                "(16 (n_metallicity*n_temperature) + 8 (n_temperature + 2 n_metallicity) + 256 bytes must not exceed 131072)%s");
+  for (int i = 0; i < nT * nZ; ++i)
+    if (!(t->cooling_rate[i] > 0.0) || !(t->electron_density[i] > 0.0))
+      return fail(nullptr, GAL_ERR_TABLE, "gal_gpu_evolve_batch_noalloc: table values must be positive%s");
+  for (int i = 1; i < nT; ++i)
+    if (!(t->temperature[i] > t->temperature[i - 1])) return fail(nullptr, GAL_ERR_TABLE, "CIE table: temperatures must increase%s");
+  for (int i = 1; i < nZ; ++i)
+    if (!(t->metallicity[i] > t->metallicity[i - 1])) return fail(nullptr, GAL_ERR_TABLE, "CIE table: metallicities must increase%s");
+  if (!(t->temperature[0] > 0.0) || t->metallicity[0] < 0.0) return fail(nullptr, GAL_ERR_TABLE, "CIE table: bad grid origin%s");
+
+  // Once per device, with that device current: the device address of the
+  // scratch array (its name is only a host-side stand-in in host code).
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kNoAllocMaxDevices)
+    return fail(nullptr, GAL_ERR_NO_DEVICE, "gal_gpu_evolve_batch_noalloc: no usable current device%s");
+  unsigned char* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    if (!g_noallocScratchPtr[device]) {
+      void* ptr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&ptr, g_noallocScratch);
+      if (e != cudaSuccess || !ptr)
+        return fail(nullptr, GAL_ERR_CUDA, "gal_gpu_evolve_batch_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      g_noallocScratchPtr[device] = ptr;
+    }
+    scratch = (unsigned char*)g_noallocScratchPtr[device];
+  }
+  unsigned long long* queue = (unsigned long long*)scratch;
+  double2* tab = (double2*)(scratch + 256);
+  double* lnT = (double*)(tab + (size_t)nZ * nT);
+  double* lnZ = lnT + nT;
+
+  Globals g;
+  std::memset(&g, 0, sizeof g);
+  g.p = *p;
+  g.nT = nT;
+  g.nZ = nZ;
+  g.Tmin = t->temperature[0];
+  g.Tmax = t->temperature[nT - 1];
+  g.Zmin = t->metallicity[0];
+  g.Zmax = t->metallicity[nZ - 1];
+  g.firstZero = t->metallicity[0] == 0.0;
+  g.firstNonZero = t->metallicity[1];
+  g.invFirstNonZero = 1.0 / g.firstNonZero;
+  const double cs = sound_speed_host(p->bh_temperature_spheroid);
+  g.soundSpeedSpheroid = cs;
+  g.jeansPrefactor = cs / std::sqrt(k::gravitationalConstantInternal);
+  g.bhSpheroidCoef = p->bh_enhancement_spheroid * k::bhlPrefactor * k::gravitationalConstantInternal *
+                     k::gravitationalConstantInternal / (cs * cs * cs);
+  g.bhRadiusSpheroidCoef = k::gravitationalConstantInternal / (cs * cs);
+  g.coolingCoef = p->cooling_degrees_of_freedom / 2.0 * k::boltzmannsConstant / k::ergs / k::gigaYear / k::densityToHydrogenNumber;
+  g.accretionFraction = p->omega_baryon / p->omega_matter;
+
+  cudaStream_t st = (cudaStream_t)stream;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1)
+    return fail(nullptr, GAL_ERR_CUDA, "gal_gpu_evolve_batch_noalloc: cannot query the SM count%s");
+  cudaError_t e = cudaSuccess;
+  // Stage the raw table: cooling rates into .x, electron densities into .y.
+  const size_t cells = (size_t)nZ * nT;
+  if (e == cudaSuccess) e = cudaMemcpy2DAsync(&tab[0].x, sizeof(double2), t->cooling_rate, sizeof(double), sizeof(double), cells,
+                                              cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpy2DAsync(&tab[0].y, sizeof(double2), t->electron_density, sizeof(double), sizeof(double),
+                                              cells, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(lnT, t->temperature, nT * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(lnZ, t->metallicity, nZ * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    noalloc_prepare_tables<<<32, 256, 0, st>>>(tab, lnT, lnZ, nT, nZ);
+    e = cudaGetLastError();
+  }
+  // The queue head must start at zero: the array keeps the last call's contents.
+  if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), st);
+  const size_t shm = shared_bytes(nT, nZ);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(evolve_kernel<kNoAllocThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  if (e == cudaSuccess) {
+    Batch b{n, state, param, tStart, tEnd, step, status, counters, queue};
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(sms, (n + kNoAllocThreads - 1) / kNoAllocThreads));
+    evolve_kernel<kNoAllocThreads><<<(unsigned)blocks, kNoAllocThreads, shm, st>>>(g, b, tab, lnT, lnZ);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) return fail(nullptr, GAL_ERR_CUDA, "gal_gpu_evolve_batch_noalloc: CUDA error: %s", cudaGetErrorString(e));
+  return GAL_OK;
+}

@@ -228,6 +228,27 @@ int gal_gpu_evolve_batch_device(gal_ctx* ctx, int64_t n, double* state, const do
                                 const double* t_start, const double* t_end, double* step,
                                 int32_t* status, uint32_t* counters, void* stream);
 
+/* Evolution for callers that cannot let a library allocate device memory,
+ * e.g. a host code whose pool allocator owns all device memory, or one that
+ * must not take the device-wide synchronisation cudaMalloc/cudaFree can
+ * cause.  No counterpart in the reference: it exists for such integrations.
+ * Same node arrays and semantics as gal_gpu_evolve_batch_device (device
+ * pointers, enqueued on `stream`, NULL = legacy default stream); `p` and
+ * `table` are host structures as for gal_gpu_init.  No context is used and
+ * nothing is allocated, on the device or the host: the kernel's scratch (the
+ * work-queue head plus the log-converted CIE tables) is one fixed 128 KiB
+ * static device array in this library, held by every GPU that loads it until
+ * the process exits.  Tables needing more than that (16 B per table cell +
+ * 8 B per grid point + 256 B) are rejected with GAL_ERR_TOO_LARGE.  The
+ * first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  Every call restages the table and
+ * resets the queue head in the shared array, so calls that overlap on the
+ * GPU (on different streams or from different threads) race: serialise
+ * them.  Launch shape is fixed at 128 threads, one block per SM. */
+int gal_gpu_evolve_batch_noalloc(const gal_params* p, const gal_cie_table* table, int64_t n, double* state,
+                                 const double* param, const double* t_start, const double* t_end, double* step,
+                                 int32_t* status, uint32_t* counters, void* stream);
+
 /* Launch shape of the evolve kernel (threads per block, blocks per SM); 0
  * keeps the current value.  Used by the autotuner. */
 int gal_gpu_set_launch(gal_ctx* ctx, int32_t threads_per_block, int32_t blocks_per_sm);
