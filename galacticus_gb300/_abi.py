@@ -30,6 +30,8 @@ STATUS_SUCCESS = 0
 STATUS_UNDERFLOW = 15
 STATUS_XCPU = 1025
 STATUS_NOT_FINITE = 2001
+RATES_FP64 = 0
+RATES_FP32 = 1
 
 OK, ERR_ARGUMENT, ERR_CUDA, ERR_TABLE, ERR_NO_DEVICE, ERR_TOO_LARGE = range(6)
 
@@ -172,10 +174,16 @@ def load_library(path=LIB_PATH):
     lib.gal_gpu_get_launch.restype = ctypes.c_int
     lib.gal_gpu_launch_count.argtypes = [vp]
     lib.gal_gpu_launch_count.restype = ctypes.c_int64
+    lib.gal_gpu_set_rate_precision.argtypes = [vp, ctypes.c_int32]
+    lib.gal_gpu_set_rate_precision.restype = ctypes.c_int
+    lib.gal_gpu_get_rate_precision.argtypes = [vp]
+    lib.gal_gpu_get_rate_precision.restype = ctypes.c_int
     lib.gal_gpu_evolve_batch_noalloc.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(CieTable), ctypes.c_int64,
                                                  vp, vp, vp, vp, vp, vp, vp, vp]
     lib.gal_gpu_evolve_batch_noalloc.restype = ctypes.c_int
     lib.gal_calibrate_fp64.argtypes = [dp, dp]
     lib.gal_calibrate_fp64.restype = ctypes.c_int
+    lib.gal_selftest_fastmath.argtypes = [dp]
+    lib.gal_selftest_fastmath.restype = ctypes.c_int
     _lib = lib
     return lib

@@ -16,7 +16,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgalnode.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177"]
-SOURCES = ["galnode.cu", "calibrate.cu"]
+SOURCES = ["galnode.cu", "evolve_plain.cu", "evolve_surrogate.cu", "evolve_fast.cu", "evolve_fast_surrogate.cu",
+           "calibrate.cu", "surrogate_train.cu"]
 
 
 def nvcc():

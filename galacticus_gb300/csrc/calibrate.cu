@@ -52,3 +52,78 @@ extern "C" int gal_calibrate_fp64(double* flops, double* ms) {
   if (ms) *ms = best;
   return 0;
 }
+
+// ---------------------------------------------------------------------------
+// Self-test of the short-latency FP64 helpers against the library functions.
+// ---------------------------------------------------------------------------
+#include "galnode_fastmath.cuh"
+
+namespace {
+constexpr int kTests = 8;
+
+__global__ void fastmath_errors(double* blockMax, int samples, const double2* logT, const double* expT) {
+  __shared__ double sMax[kTests][256];
+  const gal::FastTables F{logT, expT};
+  double m[kTests] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < samples; i += gridDim.x * blockDim.x) {
+    // Log-spaced arguments over 1e-29 .. 1e29 with a non-smooth mantissa.
+    const double u = (double)i / samples;
+    const double x = exp(-66.8 + 133.6 * u) * (1.0 + 0.4 * sin(1.0e3 * u));
+    const double a = 1.0 + 0.3 * cos(7.0e2 * u);
+    m[0] = fmax(m[0], fabs(gal::fast_rcp(x) * x - 1.0));
+    m[1] = fmax(m[1], fabs(gal::fast_div(a, x) / (a / x) - 1.0));
+    m[2] = fmax(m[2], fabs(gal::fast_rsqrt(x) * sqrt(x) - 1.0));
+    m[3] = fmax(m[3], fabs(gal::fast_sqrt(x) / sqrt(x) - 1.0));
+    // log: error relative to max(1, |ln x|) (absolute near x = 1, where the
+    // table coordinates need it), arguments 1e-29..1e29.
+    const double lx = log(x);
+    m[4] = fmax(m[4], fabs(gal::fast_log(F, x) - lx) / fmax(1.0, fabs(lx)));
+    // exp: relative error over the table's range of ln Lambda and ln n_e/n_H (-120..+5).
+    const double y = -120.0 + 125.0 * u + 1.0e-3 * sin(3.0e3 * u);
+    m[5] = fmax(m[5], fabs(gal::fast_exp(F, y) / exp(y) - 1.0));
+    // The controller's range of error ratios, log-spaced.
+    const double r = exp(log(3.0e-5) + (log(1900.0) - log(3.0e-5)) * u);
+    m[6] = fmax(m[6], fabs(gal::inv_root<5>(r) / pow(r, -0.2) - 1.0));
+    m[7] = fmax(m[7], fabs(gal::inv_root<6>(r) / pow(r, -1.0 / 6.0) - 1.0));
+  }
+  for (int t = 0; t < kTests; ++t) sMax[t][threadIdx.x] = m[t];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int t = 0; t < kTests; ++t) {
+      double v = 0.0;
+      for (int j = 0; j < blockDim.x; ++j) v = fmax(v, sMax[t][j]);
+      blockMax[blockIdx.x * kTests + t] = v;
+    }
+  }
+}
+}  // namespace
+
+extern "C" int gal_selftest_fastmath(double* maxRelErr) {
+  const int blocks = 256, threads = 256, samples = 1 << 22;
+  double2 hLog[gal::kLogTableSize];
+  double hExp[gal::kExpTableSize];
+  gal::fast_tables_host(hLog, hExp);
+  double* d = nullptr;
+  double2* dLog = nullptr;
+  double* dExp = nullptr;
+  if (cudaMalloc(&d, blocks * kTests * sizeof(double)) != cudaSuccess) return 2;
+  if (cudaMalloc(&dLog, sizeof hLog) != cudaSuccess || cudaMalloc(&dExp, sizeof hExp) != cudaSuccess) {
+    cudaFree(d); cudaFree(dLog);
+    return 2;
+  }
+  cudaMemcpy(dLog, hLog, sizeof hLog, cudaMemcpyHostToDevice);
+  cudaMemcpy(dExp, hExp, sizeof hExp, cudaMemcpyHostToDevice);
+  fastmath_errors<<<blocks, threads>>>(d, samples, dLog, dExp);
+  double h[blocks * kTests];
+  cudaError_t e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  cudaFree(dLog);
+  cudaFree(dExp);
+  if (e != cudaSuccess) return 2;
+  for (int t = 0; t < kTests; ++t) {
+    double v = 0.0;
+    for (int b = 0; b < blocks; ++b) v = h[b * kTests + t] > v ? h[b * kTests + t] : v;
+    maxRelErr[t] = v;
+  }
+  return 0;
+}

@@ -1,0 +1,540 @@
+// evolve_kernel.cuh -- the persistent node-evolution kernel and its launch.
+//
+// One thread owns one node at a time and integrates it with the Cash-Karp
+// 4(5) stepper and the reference's scaled error controller, trial loop and
+// post-step clamps (merger_trees/node_evolver/standard.F90:385-755,
+// numerical/ODE_solver/solver.F90:492-691, external/gslODEInitVal2/
+// driver2.c:148-250, cscal2.c:93-169).  The kernel is persistent: each warp
+// loops over RK attempts, and a lane whose node has finished takes the next
+// node from a device work queue (one atomic per warp), so lanes stay busy
+// however uneven the per-node step counts are.
+//
+// Four forms share the stepper (EvolveMode):
+//   PLAIN          FP64 rates, CIE table (parity form: the reference's arithmetic)
+//   SURROGATE      FP64 rates, cooling function from the MLP surrogate
+//   FAST           FP32 rates (galnode_physics_fast.cuh), FP32 CIE table
+//   FAST_SURROGATE FP32 rates, cooling function from the MLP surrogate
+// In every form the state, the accepted-step update, the error norm and the
+// step-size control are FP64.  The instantiations live in evolve_*.cu, one
+// translation unit per form, so that they compile in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+
+#include "../../include/galnode.h"
+#include "galnode_physics.cuh"
+#include "galnode_physics_fast.cuh"
+#include "surrogate.cuh"
+
+namespace gal {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// Cash-Karp 4(5) tableau (Cash & Karp 1990, ACM TOMS 16, 201).  The node
+// right-hand side has no explicit time dependence (halo mass growth enters
+// through the constant accretion rate), so the stage abscissae are unused.
+namespace ck {
+constexpr double b21 = 1.0 / 5.0;
+constexpr double b31 = 3.0 / 40.0, b32 = 9.0 / 40.0;
+constexpr double b41 = 3.0 / 10.0, b42 = -9.0 / 10.0, b43 = 6.0 / 5.0;
+constexpr double b51 = -11.0 / 54.0, b52 = 5.0 / 2.0, b53 = -70.0 / 27.0, b54 = 35.0 / 27.0;
+constexpr double b61 = 1631.0 / 55296.0, b62 = 175.0 / 512.0, b63 = 575.0 / 13824.0, b64 = 44275.0 / 110592.0,
+                 b65 = 253.0 / 4096.0;
+constexpr double c1 = 37.0 / 378.0, c3 = 250.0 / 621.0, c4 = 125.0 / 594.0, c6 = 512.0 / 1771.0;
+constexpr double e1 = 37.0 / 378.0 - 2825.0 / 27648.0, e3 = 250.0 / 621.0 - 18575.0 / 48384.0,
+                 e4 = 125.0 / 594.0 - 13525.0 / 55296.0, e5 = -277.0 / 14336.0, e6 = 512.0 / 1771.0 - 0.25;
+constexpr double order = 5.0;  // order GSL's rkck reports to the step controller
+}  // namespace ck
+
+enum EvolveMode : int { MODE_PLAIN = 0, MODE_SURROGATE = 1, MODE_FAST = 2, MODE_FAST_SURROGATE = 3 };
+
+enum Phase : int { PH_NEED = 0, PH_TRIAL = 1, PH_STEP = 2, PH_DONE = 3 };
+
+struct Batch {
+  int64_t n;
+  double* state;
+  const double* param;
+  const double* tStart;
+  const double* tEnd;
+  double* step;
+  int32_t* status;
+  uint32_t* counters;
+  unsigned long long* queue;  // work-queue head (device scratch, zeroed before launch)
+};
+
+// Device tables: the FP64 forms read gTab/gLnT/gLnZ/gFastLog/gFastExp, the
+// FP32 forms gTabF/gLnZF (and gLnT for the temperature cell of each node).
+struct DeviceTables {
+  const double2* tab;     // (ln Lambda, ln n_e/n_H) [nZ][nT]
+  const double* lnT;      // [nT]
+  const double* lnZ;      // ln Z [nZ], then 1/(ln Z[i+1] - ln Z[i]) [nZ]
+  const double2* fastLog; // short-log table [kLogTableSize]
+  const double* fastExp;  // 2^(j/64) [kExpTableSize]
+  const float2* tabF;     // FP32 copy of tab
+  const float* lnZF;      // FP32 copy of lnZ (both halves)
+};
+
+// Device copy of an installed cooling-function surrogate.
+struct SurrogateDev {
+  const float* small;          // kSurrSmall FP32 values
+  const __nv_bfloat16* planes; // W2 hi, W2 lo, W3 hi, W3 lo, each [64][kMlpStride]
+  const uint8_t* map;          // [mapT][mapZ] use-table flags
+  SurrogateInfo info;
+  unsigned long long* stats;   // [2]: network and table evaluations
+};
+
+// Shared-memory layout.  FP64 forms: [nZ*nT] double2 tables, the short-log
+// table [128 double2], ln T [nT], ln Z [nZ], 1/(ln Z[i+1] - ln Z[i]) [nZ],
+// the 2^(j/64) table [64].  FP32 forms: [nZ*nT] float2 tables, ln Z and the
+// reciprocal spacings [2 nZ, rounded up to even].  The surrogate forms
+// append the network (kSurrSmall floats rounded up to a multiple of 4, then
+// the four BF16 planes) and the error map.
+__host__ __device__ inline size_t shared_bytes(int nT, int nZ) {
+  return (size_t)(nZ * nT + kLogTableSize) * sizeof(double2) + (size_t)(nT + 2 * nZ + kExpTableSize) * sizeof(double);
+}
+__host__ __device__ inline size_t shared_bytes_fast(int nT, int nZ) {
+  return (size_t)nZ * nT * sizeof(float2) + (size_t)((2 * nZ + 1) & ~1) * sizeof(float);
+}
+__host__ __device__ inline size_t surrogate_shared_bytes(int mapCells) {
+  return (size_t)((kSurrSmall + 3) & ~3) * sizeof(float) + 4 * (size_t)kSurrPlane * sizeof(__nv_bfloat16) +
+         (size_t)((mapCells + 15) & ~15);
+}
+__host__ __device__ inline size_t evolve_shared_bytes(int mode, int nT, int nZ, int mapCells) {
+  const size_t base = (mode & MODE_FAST) ? shared_bytes_fast(nT, nZ) : shared_bytes(nT, nZ);
+  return base + ((mode & MODE_SURROGATE) ? surrogate_shared_bytes(mapCells) : 0);
+}
+
+// Cooling function (without the n_H^2 factor) and n_e/n_H of one
+// right-hand-side evaluation from the surrogate, for the node of this lane:
+// the network gives log10 Lambda at the central hot-gas density and n_e/n_H
+// is interpolated from the table in FP32.  use = false (the caller
+// interpolates the table) outside the training domain, in error-map cells
+// marked for the table, and when there is no hot gas.  Warp-collective.
+template <class NodeT, class Real, class Tab2, class TabR>
+__device__ __forceinline__ CoolingValuesF surrogate_cooling(const Globals& G, const Tab2* tab, const TabR* lnZTab,
+                                                           const TabR* invDlnZTab, const SurrogateSmem& N,
+                                                           const SurrogateInfo& I, const uint8_t* map, const NodeT& c,
+                                                           const Real* y, bool active, int lane, uint32_t& nNet,
+                                                           uint32_t& nTab) {
+  const float massHot = (float)y[GAL_Y_HOT_MASS];
+  const float metals = (float)y[GAL_Y_HOT_METALS];
+  bool ok = active && massHot > 0.0f && c.coolingAllowed;
+  const float zf = ok ? (metals > massHot ? 1.0f : (metals <= 0.0f ? 0.0f : __fdividef(metals, massHot))) : 0.0f;
+  const float zs = zf * (float)(1.0 / k::metallicitySolar);
+  const float xH = fminf(fmaxf(zs * (float)(k::hydrogenByMassSolar - k::hydrogenByMassPrimordial) +
+                               (float)k::hydrogenByMassPrimordial, 0.7f), (float)k::hydrogenByMassPrimordial);
+  const float nH = massHot * (float)c.rho0PerMass * xH * (float)k::densityToHydrogenNumber;
+  const float lt = c.log10T;
+  const float lz = zs > 0.0f ? __log10f(zs) : -1.0e30f;
+  const float ln = nH > 0.0f ? __log10f(nH) : -1.0e30f;
+  ok = ok && lt >= I.lo[0] && lt <= I.hi[0] && lz >= I.lo[1] && lz <= I.hi[1] && ln >= I.lo[2] && ln <= I.hi[2];
+  if (ok) {
+    const int it = min(max((int)((lt - I.mapLoT) * I.mapInvDT), 0), I.mapT - 1);
+    const int iz = min(max((int)((lz - I.mapLoZ) * I.mapInvDZ), 0), I.mapZ - 1);
+    ok = map[it * I.mapZ + iz] == 0;
+  }
+  CoolingValuesF cv{false, 0.0f, 0.0f};
+  // The network runs only when some lane of the warp can use it.
+  const unsigned need = __ballot_sync(FULL, ok);
+  if (!need) {
+    if (active) ++nTab;
+    return cv;
+  }
+  const float x0 = ok ? (lt - I.inMean[0]) / I.inScale[0] : 0.0f;
+  const float x1 = ok ? (lz - I.inMean[1]) / I.inScale[1] : 0.0f;
+  const float x2 = ok ? (ln - I.inMean[2]) / I.inScale[2] : 0.0f;
+  const float yn = surrogate_eval(N, x0, x1, x2, lane, need);
+  if (ok) {
+    // Lambda without its n_H^2 factor, as the table stores it: the network
+    // output is log10 Lambda - 2 log10 n_H.
+    cv.lambda = exp10f(fmaf(yn, I.yScale, I.yMean));
+    // n_e/n_H: bilinear interpolation of the log table in FP32.
+    int iZ;
+    float hZ;
+    if (G.firstZero && zs < (float)G.firstNonZero) {
+      iZ = 0;
+      hZ = zs * (float)G.invFirstNonZero;
+    } else {
+      const float lnZ = lz * 2.302585093f;
+      const int last = G.nZ - 2;
+      int j = G.zFirstLog + (int)floorf((lnZ - (float)G.lnZFirst) * (float)G.invDlnZ);
+      j = min(max(j, G.zFirstLog), last);
+      iZ = j;
+      hZ = fminf(fmaxf((lnZ - (float)lnZTab[j]) * (float)invDlnZTab[j], 0.0f), 1.0f);
+    }
+    const int nT = G.nT;
+    const float hT = (float)c.hT;
+    const float a = (float)tab[iZ * nT + c.iT].y, b = (float)tab[(iZ + 1) * nT + c.iT].y;
+    const float d = (float)tab[iZ * nT + c.iT + 1].y, e = (float)tab[(iZ + 1) * nT + c.iT + 1].y;
+    cv.electrons = __expf((1.0f - hT) * ((1.0f - hZ) * a + hZ * b) + hT * ((1.0f - hZ) * d + hZ * e));
+    cv.use = true;
+    ++nNet;
+  } else if (active) {
+    ++nTab;
+  }
+  return cv;
+}
+
+template <int THREADS, int MODE>
+__global__ void __launch_bounds__(THREADS, 1)
+evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant__ DeviceTables T,
+              const __grid_constant__ SurrogateDev sd) {
+  constexpr bool SURR = (MODE & MODE_SURROGATE) != 0;
+  constexpr bool FAST = (MODE & MODE_FAST) != 0;
+  using RateT = typename std::conditional<FAST, float, double>::type;
+  extern __shared__ double2 smem[];
+  const int nT = G.nT, nZ = G.nZ;
+  const int lane = threadIdx.x & 31;
+
+  // ---- stage the tables (and the network) into shared memory
+  Smem S{};
+  SmemF SF{};
+  const double* sLnT = T.lnT;  // FAST: node_setup reads ln T from global memory
+  unsigned char* tail;
+  if constexpr (FAST) {
+    float2* sTab = reinterpret_cast<float2*>(smem);
+    float* sLnZ = reinterpret_cast<float*>(sTab + nZ * nT);
+    for (int i = threadIdx.x; i < nZ * nT; i += blockDim.x) sTab[i] = T.tabF[i];
+    for (int i = threadIdx.x; i < 2 * nZ; i += blockDim.x) sLnZ[i] = T.lnZF[i];
+    SF = SmemF{sTab, sLnZ, sLnZ + nZ};
+    tail = reinterpret_cast<unsigned char*>(smem) + shared_bytes_fast(nT, nZ);
+  } else {
+    double2* sTab = smem;
+    double2* sFastLog = sTab + nZ * nT;
+    double* lnT = reinterpret_cast<double*>(sFastLog + kLogTableSize);
+    double* sLnZ = lnT + nT;
+    double* sInvDlnZ = sLnZ + nZ;
+    double* sFastExp = sInvDlnZ + nZ;
+    for (int i = threadIdx.x; i < nZ * nT; i += blockDim.x) sTab[i] = T.tab[i];
+    for (int i = threadIdx.x; i < nT; i += blockDim.x) lnT[i] = T.lnT[i];
+    for (int i = threadIdx.x; i < 2 * nZ; i += blockDim.x) sLnZ[i] = T.lnZ[i];  // ln Z, then the reciprocal spacings
+    for (int i = threadIdx.x; i < kLogTableSize; i += blockDim.x) sFastLog[i] = T.fastLog[i];
+    for (int i = threadIdx.x; i < kExpTableSize; i += blockDim.x) sFastExp[i] = T.fastExp[i];
+    S = Smem{sTab, sLnZ, sInvDlnZ, FastTables{sFastLog, sFastExp}};
+    sLnT = lnT;
+    tail = reinterpret_cast<unsigned char*>(smem) + shared_bytes(nT, nZ);
+  }
+  const float* sSmall = nullptr;
+  const __nv_bfloat16* sPlanes = nullptr;
+  const uint8_t* sMap = nullptr;
+  if constexpr (SURR) {
+    float* small = reinterpret_cast<float*>(tail);
+    __nv_bfloat16* planes = reinterpret_cast<__nv_bfloat16*>(small + ((kSurrSmall + 3) & ~3));
+    uint8_t* map = reinterpret_cast<uint8_t*>(planes + 4 * kSurrPlane);
+    for (int i = threadIdx.x; i < kSurrSmall; i += blockDim.x) small[i] = sd.small[i];
+    for (int i = threadIdx.x; i < 4 * kSurrPlane / 2; i += blockDim.x)
+      reinterpret_cast<uint32_t*>(planes)[i] = reinterpret_cast<const uint32_t*>(sd.planes)[i];
+    for (int i = threadIdx.x; i < sd.info.mapT * sd.info.mapZ; i += blockDim.x) map[i] = sd.map[i];
+    sSmall = small;
+    sPlanes = planes;
+    sMap = map;
+  }
+  __syncthreads();
+  SurrogateSmem N{};
+  if constexpr (SURR) N = surrogate_view(sSmall, sPlanes);
+
+  const int64_t n = b.n;
+  const double epsAbs = G.p.ode_tolerance_absolute, epsRel = G.p.ode_tolerance_relative;
+  const uint32_t budget = (uint32_t)max(G.p.step_budget, 0);
+
+  int phase = PH_NEED;
+  int64_t node = 0;
+  NodeC c;
+  NodeF cf;
+  // y, s and the accepted solution are FP64 in every form; the stages k and
+  // the stage arguments x are FP64 or FP32 with the rates.
+  // In the FP64 forms yr is y itself and ynew shares the stage argument
+  // array x, so those forms keep the register footprint of a plain stepper.
+  double y[GAL_NY], s[GAL_NY];
+  RateT k1[GAL_NY], k2[GAL_NY], k3[GAL_NY], k4[GAL_NY], k5[GAL_NY], k6[GAL_NY], x[GAL_NY];
+  float yf[GAL_NY];
+  double ynewF[GAL_NY];
+  RateT* yr;
+  double* ynew;
+  if constexpr (FAST) {
+    yr = yf;
+    ynew = ynewF;
+  } else {
+    yr = y;
+    ynew = x;
+  }
+  double t = 0.0, t0 = 0.0, t1 = 0.0, h = 0.0, stepIn = -1.0;
+  int trial = 0;
+  uint32_t count = 0, nAcc = 0, nRej = 0, nRhs = 0, nNet = 0, nTab = 0;
+  c.log10T = 0.0f;
+  cf.log10T = 0.0f;
+
+  // One right-hand-side evaluation at xx for the lanes with `active`; with
+  // the surrogate, every lane of the warp takes part in the network evaluation.
+  auto eval = [&](const RateT* xx, RateT* d, bool active) {
+    if constexpr (FAST) {
+      if constexpr (SURR) {
+        const CoolingValuesF cv =
+            surrogate_cooling(G, SF.tab, SF.lnZ, SF.invDlnZ, N, sd.info, sMap, cf, xx, active, lane, nNet, nTab);
+        if (active) rhs_fast(G, SF, cf, xx, d, cv);
+      } else {
+        rhs_fast(G, SF, cf, xx, d);
+      }
+    } else {
+      if constexpr (SURR) {
+        const CoolingValuesF cv =
+            surrogate_cooling(G, S.tab, S.lnZ, S.invDlnZ, N, sd.info, sMap, c, xx, active, lane, nNet, nTab);
+        if (active) rhs(G, S, c, xx, d, CoolingValues{cv.use, (double)cv.lambda, (double)cv.electrons});
+      } else {
+        rhs(G, S, c, xx, d);
+      }
+    }
+  };
+  // Whether the warp must enter a right-hand-side evaluation.
+  auto any = [&](bool p) { return SURR ? __any_sync(FULL, p) : p; };
+  // The FP32 copy of y in the FAST forms.
+  auto sync_yr = [&]() {
+    if constexpr (FAST) {
+#pragma unroll
+      for (int v = 0; v < GAL_NY; ++v) yf[v] = (float)y[v];
+    }
+  };
+
+  for (;;) {
+    // ---- refill lanes whose node has finished (warp-aggregated queue pop)
+    const unsigned need = __ballot_sync(FULL, phase == PH_NEED);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(b.queue, (unsigned long long)__popc(need));
+      base = __shfl_sync(FULL, base, leader);
+      if (phase == PH_NEED) {
+        node = (int64_t)(base + __popc(need & ((1u << lane) - 1u)));
+        if (node >= n) {
+          phase = PH_DONE;
+        } else {
+          double prm[GAL_NP];
+#pragma unroll
+          for (int v = 0; v < GAL_NP; ++v) prm[v] = b.param[v * n + node];
+          node_setup(G, sLnT, prm, c);
+          if constexpr (FAST) cf = node_fast(c);
+#pragma unroll
+          for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
+          scales(y, c.massHalo, s);
+          t0 = b.tStart[node];
+          t1 = b.tEnd[node];
+          stepIn = b.step[node];
+          trial = 0;
+          nAcc = nRej = nRhs = 0;
+          phase = PH_TRIAL;
+        }
+      }
+    }
+    if (__all_sync(FULL, phase == PH_DONE)) break;
+
+    // ---- start (or restart) an ODE trial: odeSolverSolve + driver reset
+    if (phase == PH_TRIAL && t0 == t1) {
+      b.step[node] = -1.0;  // node%timeStepSet(-1) when there is nothing to do
+      b.status[node] = GAL_STATUS_SUCCESS;
+      if (b.counters) {
+        b.counters[node] = 0; b.counters[n + node] = 0; b.counters[2 * n + node] = 0;
+      }
+      phase = PH_NEED;
+    }
+    const bool starting = phase == PH_TRIAL;
+    if (starting) {
+      const double stepSize = G.p.reuse_step_size ? stepIn / (double)(1u << trial) : -1.0;
+      h = t1 - t0;
+      if (stepSize > 0.0) h = fmin(stepSize, h);
+      if (trial > 0) {
+#pragma unroll
+        for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
+      }
+      sync_yr();
+      t = t0;
+      count = 0;
+    }
+    if (any(starting)) eval(yr, k1, starting);  // dydt_in of the first step
+    if (starting) {
+      ++nRhs;
+      phase = PH_STEP;
+    }
+
+    // ---- one attempted step (one pass of gsl_odeiv2_evolve_apply's try_step)
+    const bool stepping = phase == PH_STEP;
+    bool needOut = false;
+    bool finished = false;
+    int finalStatus = GAL_STATUS_SUCCESS;
+    if (any(stepping)) {
+      const double dt = t1 - t;
+      const bool finalStep = (dt >= 0.0 && h > dt) || (dt < 0.0 && h < dt);
+      const double hh = finalStep ? dt : h;
+      const RateT hr = (RateT)hh;
+      // Stage arguments: y + h sum_j b_ij k_j (in the rate precision).
+#pragma unroll
+      for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + (RateT)ck::b21 * hr * k1[i];
+      eval(x, k2, stepping);
+#pragma unroll
+      for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + hr * ((RateT)ck::b31 * k1[i] + (RateT)ck::b32 * k2[i]);
+      eval(x, k3, stepping);
+#pragma unroll
+      for (int i = 0; i < GAL_NY; ++i)
+        x[i] = yr[i] + hr * ((RateT)ck::b41 * k1[i] + (RateT)ck::b42 * k2[i] + (RateT)ck::b43 * k3[i]);
+      eval(x, k4, stepping);
+#pragma unroll
+      for (int i = 0; i < GAL_NY; ++i)
+        x[i] = yr[i] + hr * ((RateT)ck::b51 * k1[i] + (RateT)ck::b52 * k2[i] + (RateT)ck::b53 * k3[i] +
+                             (RateT)ck::b54 * k4[i]);
+      eval(x, k5, stepping);
+#pragma unroll
+      for (int i = 0; i < GAL_NY; ++i)
+        x[i] = yr[i] + hr * ((RateT)ck::b61 * k1[i] + (RateT)ck::b62 * k2[i] + (RateT)ck::b63 * k3[i] +
+                             (RateT)ck::b64 * k4[i] + (RateT)ck::b65 * k5[i]);
+      eval(x, k6, stepping);
+      if (stepping) {
+        nRhs += 5;
+        // 5th-order solution, scaled error ratio (sc2_control_hadjust, a_y=1, a_dydt=0), FP64.
+        // The largest |err_i|/D_i is found by cross-multiplication and divided
+        // once (max of the quotients = quotient of the maximal pair).
+        double errMax = 0.0, dMax = 1.0;
+#pragma unroll
+        for (int i = 0; i < GAL_NY; ++i) {
+          const RateT inc = (RateT)ck::c1 * k1[i] + (RateT)ck::c3 * k3[i] + (RateT)ck::c4 * k4[i] + (RateT)ck::c6 * k6[i];
+          const RateT est = (RateT)ck::e1 * k1[i] + (RateT)ck::e3 * k3[i] + (RateT)ck::e4 * k4[i] + (RateT)ck::e5 * k5[i] +
+                            (RateT)ck::e6 * k6[i];
+          ynew[i] = y[i] + hh * (double)inc;
+          const double err = fabs(hh * (double)est);
+          const double D0 = fabs(epsRel * fabs(ynew[i]) + epsAbs * s[i]);
+          if (err * dMax > errMax * D0 || !(err == err)) {
+            errMax = err;
+            dMax = D0;
+          }
+        }
+        const double rmax = dmax(fast_div(errMax, dMax), 2.2250738585072014e-308);  // floor DBL_MIN as cscal2.c
+        ++count;
+        const double tNew = finalStep ? t1 : t + hh;
+        double hNew = hh;
+        bool decrease = false;
+        // 0.9 rmax^(-1/5), floored at 0.2 (reached for rmax >= 4.5^5 exactly),
+        // and 0.9 rmax^(-1/6) capped at 4.9 (reached below (0.9/4.9)^6).
+        if (rmax > 1.1) {
+          double r = rmax > 1845.28125 ? 0.2 : 0.9 * inv_root<5>(rmax);
+          if (r < 0.2) r = 0.2;
+          hNew = r * hh;
+          decrease = true;
+        } else if (rmax < 0.5) {
+          double r = rmax < 3.8394e-5 ? 4.9 : 0.9 * inv_root<6>(rmax);
+          if (r > 4.9) r = 4.9;
+          if (r < 1.0) r = 1.0;
+          hNew = r * hh;
+        }
+        if (decrease) {
+          const double tNext = tNew + hNew;
+          if (fabs(hNew) < fabs(hh) && tNext != tNew) {
+            h = hNew;  // reject: retry from the same (t, y) with the smaller step
+            ++nRej;
+            if (budget && count >= budget) { finished = true; finalStatus = GAL_STATUS_XCPU; }
+          } else {
+            // The step cannot shrink any further: this trial fails
+            // (GSL_FAILURE); the node evolver restarts with half the step.
+            ++trial;
+            if (trial >= G.p.trial_count_maximum) { finished = true; finalStatus = GAL_STATUS_UNDERFLOW; }
+            else phase = PH_TRIAL;
+          }
+        } else {
+          // Accept.
+#pragma unroll
+          for (int i = 0; i < GAL_NY; ++i) y[i] = ynew[i];
+          sync_yr();
+          t = tNew;
+          h = hNew;
+          ++nAcc;
+          const bool reached = !(t1 - t > 0.0 || t1 - t < 0.0);
+          if (reached) {
+            post_step(y);
+            finished = true;
+            bool finite = true;
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) finite = finite && isfinite(y[i]);
+            finalStatus = finite ? GAL_STATUS_SUCCESS : GAL_STATUS_NOT_FINITE;
+          } else {
+            needOut = true;
+          }
+        }
+      }
+    }
+    // dydt_out at the accepted point, reused as the next dydt_in; then the
+    // post-step clamps (they return GSL_Continue: dydt_out is kept).
+    if (any(needOut)) eval(yr, k1, needOut);
+    if (needOut) {
+      ++nRhs;
+      post_step(y);
+      sync_yr();
+      if (budget && count >= budget) {
+        finished = true;
+        finalStatus = GAL_STATUS_XCPU;
+      }
+    }
+    if (finished) {
+      if (finalStatus == GAL_STATUS_SUCCESS) {
+#pragma unroll
+        for (int v = 0; v < GAL_NY; ++v) b.state[v * n + node] = y[v];
+        b.step[node] = h;
+      }
+      b.status[node] = finalStatus;
+      if (b.counters) {
+        b.counters[node] = nAcc;
+        b.counters[n + node] = nRej;
+        b.counters[2 * n + node] = nRhs;
+      }
+      phase = PH_NEED;
+    }
+  }
+  if (SURR && sd.stats) {
+    // One atomic pair per warp for the network/table evaluation counts.
+    for (int o = 16; o > 0; o >>= 1) {
+      nNet += __shfl_down_sync(FULL, nNet, o);
+      nTab += __shfl_down_sync(FULL, nTab, o);
+    }
+    if (lane == 0) {
+      atomicAdd(&sd.stats[0], (unsigned long long)nNet);
+      atomicAdd(&sd.stats[1], (unsigned long long)nTab);
+    }
+  }
+}
+
+// Everything one launch needs.
+struct LaunchArgs {
+  Globals G;
+  Batch b;
+  DeviceTables tables;
+  SurrogateDev sd;
+  size_t shm;
+  int64_t blocks;
+  cudaStream_t stream;
+};
+
+template <int THREADS, int MODE>
+cudaError_t launch_evolve(const LaunchArgs& a) {
+  cudaError_t e = cudaFuncSetAttribute(evolve_kernel<THREADS, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a.shm);
+  if (e != cudaSuccess) return e;
+  evolve_kernel<THREADS, MODE><<<(unsigned)a.blocks, THREADS, a.shm, a.stream>>>(a.G, a.b, a.tables, a.sd);
+  return cudaGetLastError();
+}
+
+// Per-form launchers (evolve_plain.cu, evolve_surrogate.cu, evolve_fast.cu,
+// evolve_fast_surrogate.cu); cudaErrorInvalidConfiguration for a block size
+// the form is not built for.
+cudaError_t evolve_launch_plain(int threads, const LaunchArgs& a);
+cudaError_t evolve_launch_surrogate(int threads, const LaunchArgs& a);
+cudaError_t evolve_launch_fast(int threads, const LaunchArgs& a);
+cudaError_t evolve_launch_fast_surrogate(int threads, const LaunchArgs& a);
+
+inline cudaError_t evolve_launch(int mode, int threads, const LaunchArgs& a) {
+  switch (mode) {
+    case MODE_PLAIN: return evolve_launch_plain(threads, a);
+    case MODE_SURROGATE: return evolve_launch_surrogate(threads, a);
+    case MODE_FAST: return evolve_launch_fast(threads, a);
+    case MODE_FAST_SURROGATE: return evolve_launch_fast_surrogate(threads, a);
+    default: return cudaErrorInvalidConfiguration;
+  }
+}
+
+}  // namespace gal

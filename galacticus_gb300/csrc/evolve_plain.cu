@@ -1,0 +1,17 @@
+// evolve_plain.cu -- instantiations of evolve_kernel for the plain form
+// (FP64 rates, CIE table: the parity form).
+#include "evolve_kernel.cuh"
+
+namespace gal {
+
+cudaError_t evolve_launch_plain(int threads, const LaunchArgs& a) {
+  switch (threads) {
+    case 64: return launch_evolve<64, MODE_PLAIN>(a);
+    case 128: return launch_evolve<128, MODE_PLAIN>(a);
+    case 256: return launch_evolve<256, MODE_PLAIN>(a);
+    case 512: return launch_evolve<512, MODE_PLAIN>(a);
+    default: return cudaErrorInvalidConfiguration;
+  }
+}
+
+}  // namespace gal

@@ -1,15 +1,10 @@
-// galnode.cu -- batched node evolution on GB300 (sm_103a) and its C ABI.
+// galnode.cu -- batched node evolution on GB300 (sm_103a): context, C ABI.
 //
-// Hot path: gal_gpu_evolve_batch[_device] -> evolve_kernel.  One thread owns
-// one node at a time and integrates it with the Cash-Karp 4(5) stepper and
-// the reference's scaled error controller, trial loop and post-step clamps
-// (merger_trees/node_evolver/standard.F90:385-755, numerical/ODE_solver/
-// solver.F90:492-691, external/gslODEInitVal2/driver2.c:148-250,
-// cscal2.c:93-169).  The kernel is persistent: each warp loops over RK
-// attempts, and a lane whose node has finished takes the next node from a
-// device work queue (one atomic per warp), so lanes stay busy however uneven
-// the per-node step counts are.  State, stages and step control are FP64 in
-// registers; the CIE tables are staged in shared memory once per block.
+// Hot path: gal_gpu_evolve_batch[_device] -> evolve_kernel (evolve_kernel.cuh,
+// instantiated per form in evolve_*.cu).  This file owns the context: the
+// tables uploaded once per context, the launch shape, the optional
+// cooling-function surrogate and the rate precision, and the entry points of
+// include/galnode.h and include/galnode_surrogate.h.
 
 #include <cuda_runtime.h>
 #include <cstdio>
@@ -20,241 +15,23 @@
 #include <algorithm>
 
 #include "../../include/galnode.h"
-#include "galnode_physics.cuh"
+#include "../../include/galnode_surrogate.h"
+#include "evolve_kernel.cuh"
 
 namespace gal {
 
-constexpr unsigned FULL = 0xffffffffu;
-
-// Cash-Karp 4(5) tableau (Cash & Karp 1990, ACM TOMS 16, 201).  The node
-// right-hand side has no explicit time dependence (halo mass growth enters
-// through the constant accretion rate), so the stage abscissae are unused.
-namespace ck {
-constexpr double b21 = 1.0 / 5.0;
-constexpr double b31 = 3.0 / 40.0, b32 = 9.0 / 40.0;
-constexpr double b41 = 3.0 / 10.0, b42 = -9.0 / 10.0, b43 = 6.0 / 5.0;
-constexpr double b51 = -11.0 / 54.0, b52 = 5.0 / 2.0, b53 = -70.0 / 27.0, b54 = 35.0 / 27.0;
-constexpr double b61 = 1631.0 / 55296.0, b62 = 175.0 / 512.0, b63 = 575.0 / 13824.0, b64 = 44275.0 / 110592.0,
-                 b65 = 253.0 / 4096.0;
-constexpr double c1 = 37.0 / 378.0, c3 = 250.0 / 621.0, c4 = 125.0 / 594.0, c6 = 512.0 / 1771.0;
-constexpr double e1 = 37.0 / 378.0 - 2825.0 / 27648.0, e3 = 250.0 / 621.0 - 18575.0 / 48384.0,
-                 e4 = 125.0 / 594.0 - 13525.0 / 55296.0, e5 = -277.0 / 14336.0, e6 = 512.0 / 1771.0 - 0.25;
-constexpr double order = 5.0;  // order GSL's rkck reports to the step controller
-}  // namespace ck
-
-enum Phase : int { PH_NEED = 0, PH_TRIAL = 1, PH_STEP = 2, PH_DONE = 3 };
-
-struct Batch {
-  int64_t n;
-  double* state;
-  const double* param;
-  const double* tStart;
-  const double* tEnd;
-  double* step;
-  int32_t* status;
-  uint32_t* counters;
-  unsigned long long* queue;  // work-queue head (device scratch, zeroed before launch)
+// The short-log/exp tables, computed once on the host from the C library.
+struct HostFastTables {
+  double2 log[kLogTableSize];
+  double exp2[kExpTableSize];
+  HostFastTables() { fast_tables_host(log, exp2); }
 };
-
-// Shared-memory layout: [nZ*nT] double2 tables, then ln T [nT], ln Z [nZ]
-// and 1/(ln Z[i+1] - ln Z[i]) [nZ].
-__host__ __device__ inline size_t shared_bytes(int nT, int nZ) {
-  return (size_t)nZ * nT * sizeof(double2) + (size_t)(nT + 2 * nZ) * sizeof(double);
+const HostFastTables& host_fast_tables() {
+  static const HostFastTables tables;  // thread-safe one-time initialisation
+  return tables;
 }
-
-template <int THREADS>
-__global__ void __launch_bounds__(THREADS, 1)
-evolve_kernel(const __grid_constant__ Globals G, Batch b, const double2* __restrict__ gTab, const double* __restrict__ gLnT,
-              const double* __restrict__ gLnZ) {
-  extern __shared__ double2 smem[];
-  const int nT = G.nT, nZ = G.nZ;
-  double2* sTab = smem;
-  double* sLnT = reinterpret_cast<double*>(sTab + nZ * nT);
-  double* sLnZ = sLnT + nT;
-  double* sInvDlnZ = sLnZ + nZ;
-  for (int i = threadIdx.x; i < nZ * nT; i += blockDim.x) sTab[i] = gTab[i];
-  for (int i = threadIdx.x; i < nT; i += blockDim.x) sLnT[i] = gLnT[i];
-  for (int i = threadIdx.x; i < 2 * nZ; i += blockDim.x) sLnZ[i] = gLnZ[i];  // ln Z, then the reciprocal spacings
-  __syncthreads();
-
-  const int lane = threadIdx.x & 31;
-  const int64_t n = b.n;
-  const double epsAbs = G.p.ode_tolerance_absolute, epsRel = G.p.ode_tolerance_relative;
-  const uint32_t budget = (uint32_t)max(G.p.step_budget, 0);
-
-  int phase = PH_NEED;
-  int64_t node = 0;
-  NodeC c;
-  double y[GAL_NY], s[GAL_NY], k1[GAL_NY], k2[GAL_NY], k3[GAL_NY], k4[GAL_NY], k5[GAL_NY], k6[GAL_NY], tmp[GAL_NY];
-  double t = 0.0, t0 = 0.0, t1 = 0.0, h = 0.0, stepIn = -1.0;
-  int trial = 0;
-  uint32_t count = 0, nAcc = 0, nRej = 0, nRhs = 0;
-
-  for (;;) {
-    // ---- refill lanes whose node has finished (warp-aggregated queue pop)
-    const unsigned need = __ballot_sync(FULL, phase == PH_NEED);
-    if (need) {
-      const int leader = __ffs(need) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(b.queue, (unsigned long long)__popc(need));
-      base = __shfl_sync(FULL, base, leader);
-      if (phase == PH_NEED) {
-        node = (int64_t)(base + __popc(need & ((1u << lane) - 1u)));
-        if (node >= n) {
-          phase = PH_DONE;
-        } else {
-          double prm[GAL_NP];
-#pragma unroll
-          for (int v = 0; v < GAL_NP; ++v) prm[v] = b.param[v * n + node];
-          node_setup(G, sLnT, prm, c);
-#pragma unroll
-          for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
-          scales(y, c.massHalo, s);
-          t0 = b.tStart[node];
-          t1 = b.tEnd[node];
-          stepIn = b.step[node];
-          trial = 0;
-          nAcc = nRej = nRhs = 0;
-          phase = PH_TRIAL;
-        }
-      }
-    }
-    if (__all_sync(FULL, phase == PH_DONE)) break;
-
-    // ---- start (or restart) an ODE trial: odeSolverSolve + driver reset
-    if (phase == PH_TRIAL) {
-      if (t0 == t1) {
-        b.step[node] = -1.0;  // node%timeStepSet(-1) when there is nothing to do
-        b.status[node] = GAL_STATUS_SUCCESS;
-        if (b.counters) {
-          b.counters[node] = 0; b.counters[n + node] = 0; b.counters[2 * n + node] = 0;
-        }
-        phase = PH_NEED;
-      } else {
-        const double stepSize = G.p.reuse_step_size ? stepIn / (double)(1u << trial) : -1.0;
-        h = t1 - t0;
-        if (stepSize > 0.0) h = fmin(stepSize, h);
-        if (trial > 0) {
-#pragma unroll
-          for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
-        }
-        t = t0;
-        count = 0;
-        rhs(G, sTab, sLnZ, sInvDlnZ, c, y, k1);  // dydt_in of the first step
-        ++nRhs;
-        phase = PH_STEP;
-      }
-    }
-
-    // ---- one attempted step (one pass of gsl_odeiv2_evolve_apply's try_step)
-    if (phase == PH_STEP) {
-      const double dt = t1 - t;
-      const bool finalStep = (dt >= 0.0 && h > dt) || (dt < 0.0 && h < dt);
-      const double hh = finalStep ? dt : h;
-#pragma unroll
-      for (int i = 0; i < GAL_NY; ++i) tmp[i] = y[i] + ck::b21 * hh * k1[i];
-      rhs(G, sTab, sLnZ, sInvDlnZ, c, tmp, k2);
-#pragma unroll
-      for (int i = 0; i < GAL_NY; ++i) tmp[i] = y[i] + hh * (ck::b31 * k1[i] + ck::b32 * k2[i]);
-      rhs(G, sTab, sLnZ, sInvDlnZ, c, tmp, k3);
-#pragma unroll
-      for (int i = 0; i < GAL_NY; ++i) tmp[i] = y[i] + hh * (ck::b41 * k1[i] + ck::b42 * k2[i] + ck::b43 * k3[i]);
-      rhs(G, sTab, sLnZ, sInvDlnZ, c, tmp, k4);
-#pragma unroll
-      for (int i = 0; i < GAL_NY; ++i)
-        tmp[i] = y[i] + hh * (ck::b51 * k1[i] + ck::b52 * k2[i] + ck::b53 * k3[i] + ck::b54 * k4[i]);
-      rhs(G, sTab, sLnZ, sInvDlnZ, c, tmp, k5);
-#pragma unroll
-      for (int i = 0; i < GAL_NY; ++i)
-        tmp[i] = y[i] + hh * (ck::b61 * k1[i] + ck::b62 * k2[i] + ck::b63 * k3[i] + ck::b64 * k4[i] + ck::b65 * k5[i]);
-      rhs(G, sTab, sLnZ, sInvDlnZ, c, tmp, k6);
-      nRhs += 5;
-      // 5th-order solution into tmp, scaled error ratio (sc2_control_hadjust, a_y=1, a_dydt=0).
-      // The largest |err_i|/D_i is found by cross-multiplication and divided
-      // once (max of the quotients = quotient of the maximal pair).
-      double errMax = 0.0, dMax = 1.0;
-#pragma unroll
-      for (int i = 0; i < GAL_NY; ++i) {
-        tmp[i] = y[i] + hh * (ck::c1 * k1[i] + ck::c3 * k3[i] + ck::c4 * k4[i] + ck::c6 * k6[i]);
-        const double err = fabs(hh * (ck::e1 * k1[i] + ck::e3 * k3[i] + ck::e4 * k4[i] + ck::e5 * k5[i] + ck::e6 * k6[i]));
-        const double D0 = fabs(epsRel * fabs(tmp[i]) + epsAbs * s[i]);
-        if (err * dMax > errMax * D0 || !(err == err)) {
-          errMax = err;
-          dMax = D0;
-        }
-      }
-      const double rmax = fmax(errMax / dMax, 2.2250738585072014e-308);  // floor DBL_MIN as cscal2.c
-      ++count;
-      const double tNew = finalStep ? t1 : t + hh;
-      double hNew = hh;
-      bool decrease = false;
-      if (rmax > 1.1) {
-        double r = 0.9 / pow(rmax, 1.0 / ck::order);
-        if (r < 0.2) r = 0.2;
-        hNew = r * hh;
-        decrease = true;
-      } else if (rmax < 0.5) {
-        double r = 0.9 / pow(rmax, 1.0 / (ck::order + 1.0));
-        if (r > 4.9) r = 4.9;
-        if (r < 1.0) r = 1.0;
-        hNew = r * hh;
-      }
-      bool finished = false;
-      int finalStatus = GAL_STATUS_SUCCESS;
-      if (decrease) {
-        const double tNext = tNew + hNew;
-        if (fabs(hNew) < fabs(hh) && tNext != tNew) {
-          h = hNew;  // reject: retry from the same (t, y) with the smaller step
-          ++nRej;
-          if (budget && count >= budget) { finished = true; finalStatus = GAL_STATUS_XCPU; }
-        } else {
-          // The step cannot shrink any further: this trial fails
-          // (GSL_FAILURE); the node evolver restarts with half the step.
-          ++trial;
-          if (trial >= G.p.trial_count_maximum) { finished = true; finalStatus = GAL_STATUS_UNDERFLOW; }
-          else phase = PH_TRIAL;
-        }
-      } else {
-        // Accept.
-#pragma unroll
-        for (int i = 0; i < GAL_NY; ++i) y[i] = tmp[i];
-        t = tNew;
-        h = hNew;
-        ++nAcc;
-        const bool reached = !(t1 - t > 0.0 || t1 - t < 0.0);
-        if (!reached) {
-          rhs(G, sTab, sLnZ, sInvDlnZ, c, y, k1);  // dydt_out, reused as the next dydt_in
-          ++nRhs;
-        }
-        post_step(y);  // clamps return GSL_Continue: dydt_out is kept
-        if (reached) {
-          finished = true;
-          bool finite = true;
-#pragma unroll
-          for (int i = 0; i < GAL_NY; ++i) finite = finite && isfinite(y[i]);
-          finalStatus = finite ? GAL_STATUS_SUCCESS : GAL_STATUS_NOT_FINITE;
-        } else if (budget && count >= budget) {
-          finished = true;
-          finalStatus = GAL_STATUS_XCPU;
-        }
-      }
-      if (finished) {
-        if (finalStatus == GAL_STATUS_SUCCESS) {
-#pragma unroll
-          for (int v = 0; v < GAL_NY; ++v) b.state[v * n + node] = y[v];
-          b.step[node] = h;
-        }
-        b.status[node] = finalStatus;
-        if (b.counters) {
-          b.counters[node] = nAcc;
-          b.counters[n + node] = nRej;
-          b.counters[2 * n + node] = nRhs;
-        }
-        phase = PH_NEED;
-      }
-    }
-  }
-}
+const double2* host_fast_log_table() { return host_fast_tables().log; }
+const double* host_fast_exp_table() { return host_fast_tables().exp2; }
 
 }  // namespace gal
 
@@ -272,11 +49,22 @@ struct gal_ctx {
   double2* dTab = nullptr;
   double* dLnT = nullptr;
   double* dLnZ = nullptr;
+  double2* dFastLog = nullptr;           // tables of the short FP64 log/exp
+  double* dFastExp = nullptr;
+  float2* dTabF = nullptr;               // FP32 copies of the tables (FP32-rate forms)
+  float* dLnZF = nullptr;
   unsigned long long* dQueue = nullptr;  // work-queue head
   void* dBuf = nullptr;                  // staging for the host-pointer API
+  // Installed cooling-function surrogate (dSurrSmall == nullptr: none).
+  float* dSurrSmall = nullptr;
+  __nv_bfloat16* dSurrPlanes = nullptr;
+  uint8_t* dSurrMap = nullptr;
+  unsigned long long* dSurrStats = nullptr;
+  SurrogateInfo surrInfo{};
   size_t bufBytes = 0;
   int threads = 128;
   int blocksPerSm = 1;
+  int ratePrecision = GAL_RATES_FP64;
   int64_t launches = 0;
   int lastError = 0;
   char message[512] = {0};
@@ -309,26 +97,73 @@ double sound_speed_host(double T) {
   return std::sqrt(5.0 * k::boltzmannsConstant * T / 3.0 / k::meanAtomicMassPrimordial / k::atomicMassUnit) / k::kilo;
 }
 
-template <int THREADS>
-cudaError_t launch_evolve(gal_ctx* ctx, const Batch& b, cudaStream_t st) {
-  const size_t shm = shared_bytes(ctx->globals.nT, ctx->globals.nZ);
-  cudaError_t e = cudaFuncSetAttribute(evolve_kernel<THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-  if (e != cudaSuccess) return e;
-  int64_t warps = (b.n + 31) / 32;
-  int64_t blocks = (int64_t)ctx->smCount * ctx->blocksPerSm;
-  blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (warps * 32 + THREADS - 1) / THREADS));
-  evolve_kernel<THREADS><<<(unsigned)blocks, THREADS, shm, st>>>(ctx->globals, b, ctx->dTab, ctx->dLnT, ctx->dLnZ);
-  return cudaGetLastError();
+// Record whether the non-zero metallicity rows are evenly spaced in ln Z
+// (the Cloudy grid is), so the kernel can find the cell arithmetically.
+void set_uniform_metallicity_grid(Globals& g, const double* lnZ, int nZ) {
+  const int first = g.firstZero ? 1 : 0;
+  g.zFirstLog = first;
+  g.lnZFirst = lnZ[first];
+  g.zUniform = 0;
+  if (nZ - first < 2) return;
+  const double d = (lnZ[nZ - 1] - lnZ[first]) / (nZ - 1 - first);
+  for (int j = first; j + 1 < nZ; ++j)
+    if (std::fabs(lnZ[j + 1] - lnZ[j] - d) > 1.0e-9 * std::fabs(d)) return;
+  g.invDlnZ = 1.0 / d;
+  g.zUniform = 1;
+}
+
+int ctx_mode(const gal_ctx* ctx) {
+  return (ctx->ratePrecision == GAL_RATES_FP32 ? MODE_FAST : 0) | (ctx->dSurrSmall ? MODE_SURROGATE : 0);
+}
+
+size_t ctx_shared_bytes(const gal_ctx* ctx, int mode) {
+  return evolve_shared_bytes(mode, ctx->globals.nT, ctx->globals.nZ, ctx->surrInfo.mapT * ctx->surrInfo.mapZ);
+}
+
+// Block sizes each form is built for (evolve_*.cu).
+bool mode_has_threads(int mode, int threads) {
+  switch (mode) {
+    case MODE_PLAIN: return threads == 64 || threads == 128 || threads == 256 || threads == 512;
+    case MODE_FAST: return threads == 128 || threads == 256 || threads == 512;
+    default: return threads == 128 || threads == 256;
+  }
+}
+
+// The launch shape in use for a form: the requested one, moved to the
+// nearest size the form is built for and to the blocks per SM that fit.
+void effective_shape(const gal_ctx* ctx, int mode, int& threads, int& blocksPerSm) {
+  threads = ctx->threads;
+  if (!mode_has_threads(mode, threads)) threads = threads < 128 ? 128 : 256;
+  const size_t shm = ctx_shared_bytes(ctx, mode);
+  blocksPerSm = ctx->blocksPerSm;
+  while (blocksPerSm > 1 && (size_t)blocksPerSm * shm > 228 * 1024) --blocksPerSm;
 }
 
 cudaError_t dispatch(gal_ctx* ctx, const Batch& b, cudaStream_t st) {
-  switch (ctx->threads) {
-    case 64: return launch_evolve<64>(ctx, b, st);
-    case 128: return launch_evolve<128>(ctx, b, st);
-    case 256: return launch_evolve<256>(ctx, b, st);
-    case 512: return launch_evolve<512>(ctx, b, st);
-    default: return cudaErrorInvalidConfiguration;
-  }
+  const int mode = ctx_mode(ctx);
+  int threads, blocksPerSm;
+  effective_shape(ctx, mode, threads, blocksPerSm);
+  LaunchArgs a{};
+  a.G = ctx->globals;
+  a.b = b;
+  a.tables = DeviceTables{ctx->dTab, ctx->dLnT, ctx->dLnZ, ctx->dFastLog, ctx->dFastExp, ctx->dTabF, ctx->dLnZF};
+  if (mode & MODE_SURROGATE) a.sd = SurrogateDev{ctx->dSurrSmall, ctx->dSurrPlanes, ctx->dSurrMap, ctx->surrInfo, ctx->dSurrStats};
+  a.shm = ctx_shared_bytes(ctx, mode);
+  const int64_t warps = (b.n + 31) / 32;
+  a.blocks = std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->smCount * blocksPerSm, (warps * 32 + threads - 1) / threads));
+  a.stream = st;
+  return evolve_launch(mode, threads, a);
+}
+
+void free_surrogate(gal_ctx* ctx) {
+  cudaFree(ctx->dSurrSmall);
+  cudaFree(ctx->dSurrPlanes);
+  cudaFree(ctx->dSurrMap);
+  cudaFree(ctx->dSurrStats);
+  ctx->dSurrSmall = nullptr;
+  ctx->dSurrPlanes = nullptr;
+  ctx->dSurrMap = nullptr;
+  ctx->dSurrStats = nullptr;
 }
 }  // namespace
 
@@ -442,7 +277,12 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
   for (int j = 0; j < nZ; ++j) lnZ[j] = t->metallicity[j] > 0.0 ? std::log(t->metallicity[j]) : -999.0;
   for (int j = 0; j + 1 < nZ; ++j) lnZ[nZ + j] = 1.0 / (lnZ[j + 1] - lnZ[j]);
   g.invFirstNonZero = 1.0 / g.firstNonZero;
+  set_uniform_metallicity_grid(g, lnZ.data(), nZ);
   for (int i = 0; i < nZ * nT; ++i) tab[i] = make_double2(std::log(t->cooling_rate[i]), std::log(t->electron_density[i]));
+  std::vector<float2> tabF(tab.size());
+  std::vector<float> lnZF(2 * nZ);
+  for (size_t i = 0; i < tab.size(); ++i) tabF[i] = make_float2((float)tab[i].x, (float)tab[i].y);
+  for (int j = 0; j < 2 * nZ; ++j) lnZF[j] = (float)lnZ[j];
 
   auto cleanup = [&](int code) {
     gal_gpu_free(ctx);
@@ -452,6 +292,10 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
       cudaMalloc(&ctx->dTab, tab.size() * sizeof(double2)) != cudaSuccess ||
       cudaMalloc(&ctx->dLnT, nT * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&ctx->dLnZ, 2 * nZ * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&ctx->dFastLog, kLogTableSize * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&ctx->dFastExp, kExpTableSize * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&ctx->dTabF, tab.size() * sizeof(float2)) != cudaSuccess ||
+      cudaMalloc(&ctx->dLnZF, 2 * nZ * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&ctx->dQueue, sizeof(unsigned long long)) != cudaSuccess) {
     cudaGetLastError();
     fail(nullptr, GAL_ERR_CUDA, "device allocation failed%s");
@@ -459,7 +303,11 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
   }
   if (cudaMemcpy(ctx->dTab, tab.data(), tab.size() * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(ctx->dLnT, lnT.data(), nT * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(ctx->dLnZ, lnZ.data(), 2 * nZ * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaMemcpy(ctx->dLnZ, lnZ.data(), 2 * nZ * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->dFastLog, host_fast_log_table(), kLogTableSize * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->dFastExp, host_fast_exp_table(), kExpTableSize * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->dTabF, tabF.data(), tabF.size() * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->dLnZF, lnZF.data(), 2 * nZ * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
     fail(nullptr, GAL_ERR_CUDA, "table upload failed%s");
     return cleanup(GAL_ERR_CUDA);
   }
@@ -473,22 +321,29 @@ void gal_gpu_free(gal_ctx* ctx) {
   cudaFree(ctx->dTab);
   cudaFree(ctx->dLnT);
   cudaFree(ctx->dLnZ);
+  cudaFree(ctx->dFastLog);
+  cudaFree(ctx->dFastExp);
+  cudaFree(ctx->dTabF);
+  cudaFree(ctx->dLnZF);
   cudaFree(ctx->dQueue);
   cudaFree(ctx->dBuf);
+  free_surrogate(ctx);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
 
 int gal_gpu_set_launch(gal_ctx* ctx, int32_t threads, int32_t blocksPerSm) {
   if (!ctx) return fail(nullptr, GAL_ERR_ARGUMENT, "gal_gpu_set_launch: NULL context%s");
+  const int mode = ctx_mode(ctx);
   if (threads) {
     if (threads != 64 && threads != 128 && threads != 256 && threads != 512)
       return fail(ctx, GAL_ERR_ARGUMENT, "threads per block must be 64, 128, 256 or 512%s");
+    if (!mode_has_threads(mode, threads))
+      return fail(ctx, GAL_ERR_ARGUMENT, "this block size is not built for the current form (rate precision / surrogate)%s");
     ctx->threads = threads;
   }
   if (blocksPerSm) {
-    const size_t shm = shared_bytes(ctx->globals.nT, ctx->globals.nZ);
-    if (blocksPerSm < 1 || (size_t)blocksPerSm * shm > 228 * 1024)
+    if (blocksPerSm < 1 || (size_t)blocksPerSm * ctx_shared_bytes(ctx, mode) > 228 * 1024)
       return fail(ctx, GAL_ERR_ARGUMENT, "blocks per SM out of range for the shared-memory footprint%s");
     ctx->blocksPerSm = blocksPerSm;
   }
@@ -497,10 +352,22 @@ int gal_gpu_set_launch(gal_ctx* ctx, int32_t threads, int32_t blocksPerSm) {
 
 int gal_gpu_get_launch(const gal_ctx* ctx, int32_t* threads, int32_t* blocksPerSm) {
   if (!ctx) return GAL_ERR_ARGUMENT;
-  if (threads) *threads = ctx->threads;
-  if (blocksPerSm) *blocksPerSm = ctx->blocksPerSm;
+  int t, bps;
+  effective_shape(ctx, ctx_mode(ctx), t, bps);
+  if (threads) *threads = t;
+  if (blocksPerSm) *blocksPerSm = bps;
   return GAL_OK;
 }
+
+int gal_gpu_set_rate_precision(gal_ctx* ctx, int32_t precision) {
+  if (!ctx) return fail(nullptr, GAL_ERR_ARGUMENT, "gal_gpu_set_rate_precision: NULL context%s");
+  if (precision != GAL_RATES_FP64 && precision != GAL_RATES_FP32)
+    return fail(ctx, GAL_ERR_ARGUMENT, "rate precision must be GAL_RATES_FP64 or GAL_RATES_FP32%s");
+  ctx->ratePrecision = precision;
+  return GAL_OK;
+}
+
+int gal_gpu_get_rate_precision(const gal_ctx* ctx) { return ctx ? ctx->ratePrecision : -1; }
 
 int64_t gal_gpu_launch_count(const gal_ctx* ctx) { return ctx ? ctx->launches : -1; }
 
@@ -562,6 +429,69 @@ int gal_gpu_evolve_batch(gal_ctx* ctx, int64_t n, double* state, const double* p
   return GAL_OK;
 }
 
+int gal_gpu_set_surrogate(gal_ctx* ctx, const gal_surrogate* sg) {
+  if (!ctx) return fail(nullptr, GAL_ERR_ARGUMENT, "gal_gpu_set_surrogate: NULL context%s");
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  free_surrogate(ctx);
+  if (!sg) return GAL_OK;
+  if (!sg->params || !sg->use_table || sg->map_t < 1 || sg->map_z < 1 || sg->map_t * sg->map_z > 4096 ||
+      !(sg->map_dt > 0.0f) || !(sg->map_dz > 0.0f) || !(sg->y_scale > 0.0f))
+    return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_set_surrogate: incomplete surrogate description%s");
+  for (int i = 0; i < 3; ++i)
+    if (!(sg->in_scale[i] > 0.0f) || !(sg->hi[i] > sg->lo[i]))
+      return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_set_surrogate: bad normalisation or domain%s");
+  std::vector<float> small(kSurrSmall);
+  std::vector<__nv_bfloat16> planes(4 * kSurrPlane);
+  surrogate_pack(sg->params, small.data(), planes.data());
+  const int cells = sg->map_t * sg->map_z;
+  SurrogateInfo& I = ctx->surrInfo;
+  for (int i = 0; i < 3; ++i) {
+    I.inMean[i] = sg->in_mean[i];
+    I.inScale[i] = sg->in_scale[i];
+    I.lo[i] = sg->lo[i];
+    I.hi[i] = sg->hi[i];
+  }
+  I.yMean = sg->y_mean;
+  I.yScale = sg->y_scale;
+  I.mapT = sg->map_t;
+  I.mapZ = sg->map_z;
+  I.mapLoT = sg->map_lo_t;
+  I.mapLoZ = sg->map_lo_z;
+  I.mapInvDT = 1.0f / sg->map_dt;
+  I.mapInvDZ = 1.0f / sg->map_dz;
+  if (shared_bytes(ctx->globals.nT, ctx->globals.nZ) + surrogate_shared_bytes(cells) > 227 * 1024)
+    return fail(ctx, GAL_ERR_TOO_LARGE, "gal_gpu_set_surrogate: shared memory footprint too large%s");
+  if (cudaMalloc(&ctx->dSurrSmall, small.size() * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&ctx->dSurrPlanes, planes.size() * sizeof(__nv_bfloat16)) != cudaSuccess ||
+      cudaMalloc(&ctx->dSurrMap, cells) != cudaSuccess ||
+      cudaMalloc(&ctx->dSurrStats, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+    cudaGetLastError();
+    free_surrogate(ctx);
+    return fail(ctx, GAL_ERR_CUDA, "gal_gpu_set_surrogate: device allocation failed%s");
+  }
+  if (cudaMemcpy(ctx->dSurrSmall, small.data(), small.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->dSurrPlanes, planes.data(), planes.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->dSurrMap, sg->use_table, cells, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(ctx->dSurrStats, 0, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+    free_surrogate(ctx);
+    return fail(ctx, GAL_ERR_CUDA, "gal_gpu_set_surrogate: upload failed%s");
+  }
+  return GAL_OK;
+}
+
+int gal_gpu_surrogate_stats(const gal_ctx* ctx, uint64_t* network, uint64_t* table) {
+  if (!ctx) return GAL_ERR_ARGUMENT;
+  unsigned long long h[2] = {0, 0};
+  if (ctx->dSurrStats) {
+    cudaStreamSynchronize(ctx->stream);
+    if (cudaMemcpy(h, ctx->dSurrStats, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess) return GAL_ERR_CUDA;
+  }
+  if (network) *network = h[0];
+  if (table) *table = h[1];
+  return GAL_OK;
+}
+
 }  // extern "C"
 
 // ===========================================================================
@@ -591,8 +521,9 @@ static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchB
 std::mutex g_noallocMutex;
 void* g_noallocScratchPtr[kNoAllocMaxDevices] = {nullptr};
 
-// Scratch layout: [0,256) queue head; then the double2 table [nZ*nT];
-// then ln T [nT]; then ln Z [nZ] and 1/(ln Z[i+1]-ln Z[i]) [nZ].
+// Scratch layout: [0,256) queue head; then the double2 table [nZ*nT]; the
+// short-log table [128 double2]; ln T [nT]; ln Z [nZ] and
+// 1/(ln Z[i+1]-ln Z[i]) [nZ]; the 2^(j/64) table [64] (the shared layout).
 size_t noalloc_bytes(int nT, int nZ) { return 256 + shared_bytes(nT, nZ); }
 
 // In-place conversion of the staged raw table to the layout the kernel
@@ -630,7 +561,7 @@ extern "C" int gal_gpu_evolve_batch_noalloc(const gal_params* p, const gal_cie_t
   if (noalloc_bytes(nT, nZ) > kNoAllocScratchBytes)
     return fail(nullptr, GAL_ERR_TOO_LARGE,
                 "gal_gpu_evolve_batch_noalloc: CIE table too large for the fixed 128 KiB scratch "
-                "(16 (n_metallicity*n_temperature) + 8 (n_temperature + 2 n_metallicity) + 256 bytes must not exceed 131072)%s");
+                "(16 (n_metallicity*n_temperature + 128) + 8 (n_temperature + 2 n_metallicity + 64) + 256 bytes must not exceed 131072)%s");
   for (int i = 0; i < nT * nZ; ++i)
     if (!(t->cooling_rate[i] > 0.0) || !(t->electron_density[i] > 0.0))
       return fail(nullptr, GAL_ERR_TABLE, "gal_gpu_evolve_batch_noalloc: table values must be positive%s");
@@ -659,8 +590,10 @@ extern "C" int gal_gpu_evolve_batch_noalloc(const gal_params* p, const gal_cie_t
   }
   unsigned long long* queue = (unsigned long long*)scratch;
   double2* tab = (double2*)(scratch + 256);
-  double* lnT = (double*)(tab + (size_t)nZ * nT);
+  double2* fastLog = tab + (size_t)nZ * nT;
+  double* lnT = (double*)(fastLog + kLogTableSize);
   double* lnZ = lnT + nT;
+  double* fastExp = lnZ + 2 * nZ;
 
   Globals g;
   std::memset(&g, 0, sizeof g);
@@ -696,20 +629,25 @@ extern "C" int gal_gpu_evolve_batch_noalloc(const gal_params* p, const gal_cie_t
                                               cells, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(lnT, t->temperature, nT * sizeof(double), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(lnZ, t->metallicity, nZ * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(fastLog, host_fast_log_table(), kLogTableSize * sizeof(double2), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(fastExp, host_fast_exp_table(), kExpTableSize * sizeof(double), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     noalloc_prepare_tables<<<32, 256, 0, st>>>(tab, lnT, lnZ, nT, nZ);
     e = cudaGetLastError();
   }
   // The queue head must start at zero: the array keeps the last call's contents.
   if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), st);
-  const size_t shm = shared_bytes(nT, nZ);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(evolve_kernel<kNoAllocThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   if (e == cudaSuccess) {
-    Batch b{n, state, param, tStart, tEnd, step, status, counters, queue};
-    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(sms, (n + kNoAllocThreads - 1) / kNoAllocThreads));
-    evolve_kernel<kNoAllocThreads><<<(unsigned)blocks, kNoAllocThreads, shm, st>>>(g, b, tab, lnT, lnZ);
-    e = cudaGetLastError();
+    LaunchArgs a{};
+    a.G = g;
+    a.b = Batch{n, state, param, tStart, tEnd, step, status, counters, queue};
+    a.tables = DeviceTables{tab, lnT, lnZ, fastLog, fastExp, nullptr, nullptr};
+    a.shm = shared_bytes(nT, nZ);
+    a.blocks = std::max<int64_t>(1, std::min<int64_t>(sms, (n + kNoAllocThreads - 1) / kNoAllocThreads));
+    a.stream = st;
+    e = evolve_launch_plain(kNoAllocThreads, a);
   }
   if (e != cudaSuccess) return fail(nullptr, GAL_ERR_CUDA, "gal_gpu_evolve_batch_noalloc: CUDA error: %s", cudaGetErrorString(e));
   return GAL_OK;

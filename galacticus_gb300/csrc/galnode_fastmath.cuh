@@ -1,0 +1,146 @@
+// galnode_fastmath.cuh -- FP64 elementary functions with few FP64-pipe
+// instructions, for the integrator's critical path.
+//
+// On GB300 the FP64 pipe accepts about one warp instruction every 64-76
+// cycles per SM sub-partition, whatever the number of active lanes.  A node
+// that needs a thousand right-hand-side evaluations runs alone in its warp at
+// the end of a batch, so its time is the number of FP64 instructions on its
+// path times that interval.  The library log, exp, divide, sqrt and pow
+// expand to 12-90 FP64 instructions each; the versions below use integer and
+// single-precision instructions (other pipes) wherever they do not limit
+// accuracy, and FP64 for the refinement:
+//
+//  * rcp/div/rsqrt/sqrt: the single-precision hardware approximation
+//    (relative error ~1e-7) refined by two Newton-Raphson steps in FP64,
+//    which square the error twice (~1e-28) before the final rounding.
+//  * log: the classical table-driven reduction.  x = 2^e m, m in [1,2);
+//    c = 1 + (j + 1/2)/128 from the top seven mantissa bits; then
+//    ln x = e ln 2 + ln c + ln(1 + r), r = m/c - 1, |r| < 2^-8, with
+//    ln(1 + r) from its Taylor series to r^6 (truncation < 2^-58).
+//  * exp: x = (64 k + j) ln2/64 + r, |r| <= ln2/128, so
+//    e^x = 2^k 2^(j/64) e^r with e^r from its Taylor series to r^6
+//    (truncation < 2^-65) and 2^(j/64) from a table.
+//  * inv_root: x^(-1/Q) from the single-precision seed and Newton steps
+//    g <- g + g (1 - x g^Q)/Q (replaces pow in the step-size controller).
+//
+// The tables (ln c_j, 1/c_j and 2^(j/64)) are computed on the host in FP64
+// from the C library and staged in shared memory.  Arguments outside the
+// ranges the reductions cover fall back to the CUDA functions.  Every
+// function is checked against the CUDA library by gal_selftest_fastmath.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+namespace gal {
+
+struct FastTables {
+  const double2* log;  // [128]: (ln c_j, 1/c_j)
+  const double* exp2;  // [64]: 2^(j/64)
+};
+
+constexpr int kLogTableSize = 128;
+constexpr int kExpTableSize = 64;
+constexpr double kLn2Hi = 6.93147180369123816490e-01;  // ln 2 split into a head with trailing zero bits
+constexpr double kLn2Lo = 1.90821492927058770002e-10;  // and the remainder
+
+// Integer tests on the high word: x is positive with a binary exponent in
+// [lo, hi]; |x| has a binary exponent in [lo, hi].
+__device__ __forceinline__ bool positive_exponent_in(double x, int lo, int hi) {
+  const int h = __double2hiint(x);
+  return h >= ((lo + 1023) << 20) && h < ((hi + 1024) << 20);
+}
+__device__ __forceinline__ bool abs_exponent_in(double x, int lo, int hi) {
+  const int h = __double2hiint(x) & 0x7fffffff;
+  return h >= ((lo + 1023) << 20) && h < ((hi + 1024) << 20);
+}
+
+__device__ __forceinline__ double fast_rcp(double y) {
+  if (!abs_exponent_in(y, -120, 120)) return 1.0 / y;
+  double r = (double)__frcp_rn((float)y);
+  double e = fma(-y, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-y, r, 1.0);
+  return fma(r, e, r);
+}
+
+__device__ __forceinline__ double fast_div(double x, double y) { return x * fast_rcp(y); }
+
+__device__ __forceinline__ double fast_rsqrt(double x) {
+  if (!positive_exponent_in(x, -120, 120)) return 1.0 / sqrt(x);
+  double r = (double)rsqrtf((float)x);
+  const double hx = 0.5 * x;
+  r = r * fma(-hx * r, r, 1.5);
+  return r * fma(-hx * r, r, 1.5);
+}
+
+__device__ __forceinline__ double fast_sqrt(double x) {
+  if (!positive_exponent_in(x, -120, 120)) return sqrt(x);
+  const double r = fast_rsqrt(x);
+  const double s = x * r;
+  return fma(0.5 * r, fma(-s, s, x), s);
+}
+
+__device__ __forceinline__ double fast_log(const FastTables& T, double x) {
+  if (!positive_exponent_in(x, -1000, 1000)) return log(x);
+  const long long bits = __double_as_longlong(x);
+  const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+  const int j = (int)((bits >> 45) & 127);
+  const double m = __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  const double2 t = T.log[j];
+  const double r = fma(m, t.y, -1.0);
+  // ln(1+r) = r + r^2 (-1/2 + r/3 - r^2/4 + r^3/5 - r^4/6)
+  double p = fma(r, -1.0 / 6.0, 1.0 / 5.0);
+  p = fma(r, p, -0.25);
+  p = fma(r, p, 1.0 / 3.0);
+  p = fma(r, p, -0.5);
+  p = fma(r * r, p, r);
+  const double de = (double)e;
+  return fma(de, kLn2Hi, t.x + fma(de, kLn2Lo, p));
+}
+
+__device__ __forceinline__ double fast_exp(const FastTables& T, double x) {
+  if (!(x > -700.0 && x < 700.0)) return exp(x);
+  const double shifter = 6755399441055744.0;  // 1.5 * 2^52: adding it rounds to an integer in the low bits
+  const double kd = fma(x, 64.0 / 0.69314718055994530942, shifter);
+  const int k = __double2loint(kd);
+  const double n = kd - shifter;
+  const double r = fma(-n, kLn2Lo / 64.0, fma(-n, kLn2Hi / 64.0, x));
+  // e^r - 1 = r + r^2 (1/2 + r/6 + r^2/24 + r^3/120 + r^4/720)
+  double p = fma(r, 1.0 / 720.0, 1.0 / 120.0);
+  p = fma(r, p, 1.0 / 24.0);
+  p = fma(r, p, 1.0 / 6.0);
+  p = fma(r, p, 0.5);
+  p = fma(r * r, p, r);
+  const double s = T.exp2[k & 63];
+  const double v = fma(s, p, s);
+  // Multiply by 2^(k >> 6) through the exponent field (|k >> 6| < 1011 here).
+  return __longlong_as_double(__double_as_longlong(v) + ((long long)(k >> 6) << 52));
+}
+
+template <int Q>
+__device__ __forceinline__ double inv_root(double x) {
+  double g = (double)exp2f(-(1.0f / Q) * __log2f((float)x));
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const double g2 = g * g;
+    const double gq = Q == 5 ? g2 * g2 * g : g2 * g2 * g2;
+    g = fma(g * (1.0 / Q), fma(-x, gq, 1.0), g);
+  }
+  return g;
+}
+
+// FP64 min/max as compare-and-select (shorter than the min/max instruction).
+__device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
+__device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
+
+// Host-side construction of the tables.
+inline void fast_tables_host(double2* logTable, double* exp2Table) {
+  for (int j = 0; j < kLogTableSize; ++j) {
+    const double c = 1.0 + (j + 0.5) / kLogTableSize;
+    logTable[j] = make_double2(std::log(c), 1.0 / c);
+  }
+  for (int j = 0; j < kExpTableSize; ++j) exp2Table[j] = std::exp2((double)j / kExpTableSize);
+}
+
+}  // namespace gal

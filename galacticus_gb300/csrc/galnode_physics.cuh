@@ -11,6 +11,7 @@
 
 #include <cstdint>
 #include "../../include/galnode.h"
+#include "galnode_fastmath.cuh"
 
 namespace gal {
 
@@ -55,6 +56,9 @@ struct Globals {
   int firstZero;              // first metallicity row is Z = 0
   double firstNonZero;        // Z/Zsun of the first non-zero row
   double invFirstNonZero;
+  int zUniform;               // non-zero rows evenly spaced in ln Z: cell by arithmetic
+  int zFirstLog;              // index of the first non-zero row
+  double lnZFirst, invDlnZ;   // its ln Z and the reciprocal spacing
   double Tmin, Tmax, Zmin, Zmax;
   double soundSpeedSpheroid;  // km/s at bh_temperature_spheroid
   double jeansPrefactor;      // c_s/sqrt(G) for the spheroid gas
@@ -83,6 +87,7 @@ struct NodeC {
   double hT;                  // temperature interpolation weight
   int iT;                     // temperature cell of T_vir
   int coolingAllowed;         // V_vir <= velocity cut-off
+  float log10T;               // log10 T_vir (input of the cooling surrogate)
   double sfrDisk, sfrSph;     // 1/tau_* of the disk and spheroid (0: none)
   double outDisk, outSph;     // outflow rate per unit SFR
   double outDiskMax, outSphMax; // 1/(t_dyn f_min) of the rate limit (<0: no limit)
@@ -95,6 +100,14 @@ struct NodeC {
   double bhHotMaxCoef;        // c_s/(r_outer MpcPerKmPerSToGyr)
   double accretionRate;       // hot-gas accretion rate (Msun/Gyr)
   double reincorporationRate; // multiplier / t_dyn
+};
+
+// Shared-memory tables used by the right-hand side.
+struct Smem {
+  const double2* tab;      // (ln Lambda, ln n_e/n_H) [nZ][nT]
+  const double* lnZ;       // ln Z/Zsun of the rows
+  const double* invDlnZ;   // 1/(ln Z[i+1] - ln Z[i])
+  FastTables fast;         // tables of the short FP64 log/exp
 };
 
 // Abundances_Mass_To_Mass_Fraction_Packed (objects/abundances.F90:781-809)
@@ -142,6 +155,7 @@ __device__ __forceinline__ void node_setup(const Globals& G, const double* sLnT,
   c.iT = locate(sLnT, G.nT, lnT);
   c.hT = (lnT - sLnT[c.iT]) / (sLnT[c.iT + 1] - sLnT[c.iT]);
   c.coolingTimeCoef = G.coolingCoef * T;
+  c.log10T = T > 0.0 ? (float)log10(T) : -1.0e30f;
   c.coolingAllowed = !(vvir > p.cooling_velocity_cutoff);
   // galacticStructureSolverFixed: r = f lambda r_vir, V = V_vir.
   const double Rd = p.radius_factor_disk * spin * rvir, Rs = p.radius_factor_spheroid * spin * rvir;
@@ -188,28 +202,41 @@ __device__ __forceinline__ void node_setup(const Globals& G, const double* sLnT,
 // (cooling_function/CIE_file.F90:238-317, 665-735; chemical/state/
 // CIE_file.F90:245-320).  `tab` interleaves (ln Lambda, ln n_e/n_H);
 // sInvDlnZ[i] = 1/(ln Z[i+1] - ln Z[i]).
-__device__ __forceinline__ void cie_lookup(const Globals& G, const double2* tab, const double* sLnZ,
-                                          const double* sInvDlnZ, const NodeC& c, double zSolar, double& lambda,
+__device__ __forceinline__ void cie_lookup(const Globals& G, const Smem& S, const NodeC& c, double zSolar, double& lambda,
                                           double& electrons) {
-  zSolar = fmin(fmax(zSolar, G.Zmin), G.Zmax);  // "fix" extrapolation in metallicity
-  const double zUse = fmax(zSolar, 0.0);
+  const double* sLnZ = S.lnZ;
+  zSolar = dmin(dmax(zSolar, G.Zmin), G.Zmax);  // "fix" extrapolation in metallicity
+  const double zUse = dmax(zSolar, 0.0);
   int iZ;
   double hZ;
   if (G.firstZero && zUse < G.firstNonZero) {
     iZ = 0;
     hZ = zUse * G.invFirstNonZero;
   } else {
-    const double lnZ = log(zUse);
-    iZ = locate(sLnZ, G.nZ, lnZ);
-    hZ = (lnZ - sLnZ[iZ]) * sInvDlnZ[iZ];
+    const double lnZ = fast_log(S.fast, zUse);
+    if (G.zUniform) {
+      // Evenly spaced rows: estimate the cell, then settle it against the
+      // grid values so that it is exactly locate()'s answer.
+      const int last = G.nZ - 2;
+      int j = G.zFirstLog + (int)floor((lnZ - G.lnZFirst) * G.invDlnZ);
+      j = j < G.zFirstLog ? G.zFirstLog : (j > last ? last : j);
+      if (j > G.zFirstLog && lnZ < sLnZ[j]) --j;
+      if (j < last && lnZ >= sLnZ[j + 1]) ++j;
+      if (lnZ < sLnZ[j]) j = 0 > j - 1 ? 0 : j - 1;  // below the first non-zero row
+      iZ = j;
+    } else {
+      iZ = locate(sLnZ, G.nZ, lnZ);
+    }
+    hZ = (lnZ - sLnZ[iZ]) * S.invDlnZ[iZ];
   }
+  const double2* tab = S.tab;
   const int nT = G.nT;
   const double2 a = tab[iZ * nT + c.iT], b = tab[(iZ + 1) * nT + c.iT];
   const double2 d = tab[iZ * nT + c.iT + 1], e = tab[(iZ + 1) * nT + c.iT + 1];
   const double hT = c.hT;
   const double w00 = (1.0 - hT) * (1.0 - hZ), w01 = (1.0 - hT) * hZ, w10 = hT * (1.0 - hZ), w11 = hT * hZ;
-  lambda = exp(a.x * w00 + b.x * w01 + d.x * w10 + e.x * w11);
-  electrons = exp(a.y * w00 + b.y * w01 + d.y * w10 + e.y * w11);
+  lambda = fast_exp(S.fast, a.x * w00 + b.x * w01 + d.x * w10 + e.x * w11);
+  electrons = fast_exp(S.fast, a.y * w00 + b.y * w01 + d.y * w10 + e.y * w11);
 }
 
 // Cooling radius (cooling_radius/simple.F90:313-427) in closed form.  At
@@ -222,35 +249,47 @@ __device__ __forceinline__ void cie_lookup(const Globals& G, const double2* tab,
 //   t_cool(0) = (dof/2) k T (n_H/x_num + n_e) / ergs / (Lambda n_H^2) / Gyr
 // with n_H = rho(0) X_H and 1/x_num = 1 + (Y m_H)/(X_H m_He); the ratio
 // q = t_avail/t_cool(0) below is that expression with one division.
-__device__ __forceinline__ double cooling_radius(const Globals& G, const double2* tab, const double* sLnZ,
-                                                const double* sInvDlnZ, const NodeC& c, double massHot, double zHot) {
+// Cooling function and electron fraction supplied by the surrogate for this
+// evaluation (use = false: interpolate the table).
+struct CoolingValues {
+  bool use;
+  double lambda, electrons;
+};
+
+__device__ __forceinline__ double cooling_radius(const Globals& G, const Smem& S, const NodeC& c, double massHot, double zHot,
+                                                const CoolingValues& cv) {
   // Abundances_Hydrogen/Helium_Mass_Fraction (objects/abundances.F90:830-868).
   const double zs = zHot * (1.0 / k::metallicitySolar);
-  const double xH = fmin(fmax(zs * (k::hydrogenByMassSolar - k::hydrogenByMassPrimordial) + k::hydrogenByMassPrimordial, 0.7),
+  const double xH = dmin(dmax(zs * (k::hydrogenByMassSolar - k::hydrogenByMassPrimordial) + k::hydrogenByMassPrimordial, 0.7),
                          k::hydrogenByMassPrimordial);
-  const double yHe = fmin(zs * (k::heliumByMassSolar - k::heliumByMassPrimordial) + k::heliumByMassPrimordial, k::heliumByMassPrimordial);
+  const double yHe = dmin(zs * (k::heliumByMassSolar - k::heliumByMassPrimordial) + k::heliumByMassPrimordial, k::heliumByMassPrimordial);
   double lambda, electrons;
-  cie_lookup(G, tab, sLnZ, sInvDlnZ, c, zs, lambda, electrons);
+  if (cv.use) {
+    lambda = cv.lambda;
+    electrons = cv.electrons;
+  } else {
+    cie_lookup(G, S, c, zs, lambda, electrons);
+  }
   const double num = c.tdyn * lambda * massHot * c.rho0PerMass * xH * xH;
   const double den = c.coolingTimeCoef * (xH * (1.0 + electrons) + yHe * (k::atomicMassHydrogen / k::atomicMassHelium));
-  const double q = massHot > 0.0 ? num / den : 0.0;
+  const double q = massHot > 0.0 ? fast_div(num, den) : 0.0;
   if (q > c.onePlusXOuter2) return c.rOuter;  // t_cool(r_outer) < t_avail
   if (q < 1.0) return 0.0;                    // t_cool(0) > t_avail
-  return c.rcore * sqrt(q - 1.0);
+  return c.rcore * fast_sqrt(q - 1.0);
 }
 
 // Right-hand side of the node ODE system: the node operators of
 // nodeOperatorMulti (nodes/operators/multi.F90:313-332) in the order of
 // parameters/quickTest.xml.  Same logic, branch by branch, as the oracle.
-__device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const double* sLnZ, const double* sInvDlnZ,
-                                   const NodeC& c, const double* y, double* dydt) {
+__device__ __forceinline__ void rhs(const Globals& G, const Smem& S, const NodeC& c, const double* y, double* dydt,
+                                   const CoolingValues& cv = CoolingValues{false, 0.0, 0.0}) {
   const gal_params& p = G.p;
   const uint32_t ph = p.physics;
 #pragma unroll
   for (int i = 0; i < GAL_NY; ++i) dydt[i] = 0.0;
   const double massHot = y[GAL_Y_HOT_MASS], metalsHot = y[GAL_Y_HOT_METALS];
   const double gasDisk = y[GAL_Y_DISK_GAS], gasSph = y[GAL_Y_SPHEROID_GAS];
-  const double invHot = massHot > 0.0 ? 1.0 / massHot : 0.0;
+  const double invHot = massHot > 0.0 ? fast_rcp(massHot) : 0.0;
   const double zHot = mass_fraction(metalsHot, massHot, invHot);
   bool coolingRadiusKnown = false;
   double rCool = 0.0;
@@ -259,8 +298,7 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
   // (stellar_populations/properties/instantaneous.F90:133-219).
   const bool diskOk = !(c.radiusDisk < 0.0 || gasDisk < 0.0);
   const double sfrDisk = diskOk ? gasDisk * c.sfrDisk : 0.0;
-  const double zDisk = gasDisk > 0.0 ? mass_fraction(y[GAL_Y_DISK_GAS_METALS], gasDisk, 1.0 / gasDisk)
-                                     : mass_fraction(y[GAL_Y_DISK_GAS_METALS], gasDisk, 0.0);
+  const double zDisk = mass_fraction(y[GAL_Y_DISK_GAS_METALS], gasDisk, gasDisk > 0.0 ? fast_rcp(gasDisk) : 0.0);
   if ((ph & GAL_PHYS_STAR_FORMATION_DISK) && diskOk) {
     const double rateStars = (1.0 - p.recycled_fraction) * sfrDisk;
     const double rateMetals = zDisk * rateStars;
@@ -272,7 +310,7 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
   // starFormationSpheroids (star_formation/spheroids.F90:152-)
   const bool sphOk = !(c.aSph < 1.0e-12 || gasSph < 1.0e-6);
   const double sfrSph = sphOk ? gasSph * c.sfrSph : 0.0;
-  const double invSph = gasSph > 0.0 ? 1.0 / gasSph : 0.0;
+  const double invSph = gasSph > 0.0 ? fast_rcp(gasSph) : 0.0;
   const double zSph = mass_fraction(y[GAL_Y_SPHEROID_GAS_METALS], gasSph, invSph);
   if ((ph & GAL_PHYS_STAR_FORMATION_SPHEROID) && sphOk) {
     const double rateStars = (1.0 - p.recycled_fraction) * sfrSph;
@@ -283,7 +321,7 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
   // stellarFeedbackDisks (stellar_feedback/disks.F90:116-205); rateLimit caps at the maximum.
   if ((ph & GAL_PHYS_FEEDBACK_DISK) && diskOk) {
     double total = c.outDisk * sfrDisk;
-    if (c.outDiskMax >= 0.0) total = fmin(total, fmax(gasDisk * c.outDiskMax, 0.0));
+    if (c.outDiskMax >= 0.0) total = dmin(total, dmax(gasDisk * c.outDiskMax, 0.0));
     if (total > 0.0) {
       const double metals = gasDisk > 0.0 ? zDisk * total : 0.0;
       dydt[GAL_Y_OUTFLOWED_MASS] += total;
@@ -295,7 +333,7 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
   // stellarFeedbackSpheroids (stellar_feedback/spheroids.F90:116-208)
   if ((ph & GAL_PHYS_FEEDBACK_SPHEROID) && sphOk) {
     double total = c.outSph * sfrSph;
-    if (c.outSphMax >= 0.0) total = fmin(total, fmax(gasSph * c.outSphMax, 0.0));
+    if (c.outSphMax >= 0.0) total = dmin(total, dmax(gasSph * c.outSphMax, 0.0));
     if (total > 0.0) {
       const double metals = gasSph > 0.0 ? zSph * total : 0.0;
       dydt[GAL_Y_OUTFLOWED_MASS] += total;
@@ -313,27 +351,27 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
     double rateSph = 0.0;
     if (gasSph > 0.0 && c.aSph > 0.0) {
       // Bondi-Hoyle from the spheroid gas (Hernquist density at max(r_BHL, Jeans length)).
-      const double rAcc = fmax(G.bhRadiusSpheroidCoef * massBH, 0.0);
+      const double rAcc = dmax(G.bhRadiusSpheroidCoef * massBH, 0.0);
       double xx = rAcc * c.invASph, opx = 1.0 + xx;
-      double rho = gasSph * c.rhoSphPerMass / (xx * opx * opx * opx);
+      double rho = fast_div(gasSph * c.rhoSphPerMass, xx * opx * opx * opx);
       if (rho > 1.0) {
-        const double jeans = fmin(G.jeansPrefactor * rsqrt(rho), c.aSph);
+        const double jeans = dmin(G.jeansPrefactor * fast_rsqrt(rho), c.aSph);
         if (jeans > rAcc) {
           xx = jeans * c.invASph;
           opx = 1.0 + xx;
-          rho = gasSph * c.rhoSphPerMass / (xx * opx * opx * opx);
+          rho = fast_div(gasSph * c.rhoSphPerMass, xx * opx * opx * opx);
         }
-        rateSph = fmax(G.bhSpheroidCoef * massBH * massBH * rho, 0.0);
-        if (eps > 0.0) rateSph = fmin(rateSph, eddingtonCap);
+        rateSph = dmax(G.bhSpheroidCoef * massBH * massBH * rho, 0.0);
+        if (eps > 0.0) rateSph = dmin(rateSph, eddingtonCap);
       }
     }
     double rateHot = 0.0;
     {
-      const double rAcc = fmin(c.bhRadiusHotCoef > 0.0 ? c.bhRadiusHotCoef * massBH : HUGE_VAL, c.rOuter);
+      const double rAcc = dmin(c.bhRadiusHotCoef > 0.0 ? c.bhRadiusHotCoef * massBH : HUGE_VAL, c.rOuter);
       double fractionHot = 1.0;
       if (p.bh_hot_mode_only) {
         // standardHotModeFraction (accretion_rates/standard.F90:442-468)
-        rCool = cooling_radius(G, tab, sLnZ, sInvDlnZ, c, massHot, zHot);
+        rCool = cooling_radius(G, S, c, massHot, zHot, cv);
         coolingRadiusKnown = true;
         const double xx = rCool * c.invRvir;
         if (xx < 0.9) fractionHot = 1.0;
@@ -345,11 +383,11 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
       }
       if (massHot > 0.0 && fractionHot > 0.0) {
         const double xx = rAcc * c.invRcore;
-        const double rho = fractionHot * massHot * c.rho0PerMass / (1.0 + xx * xx);
+        const double rho = fast_div(fractionHot * massHot * c.rho0PerMass, 1.0 + xx * xx);
         if (rho > 1.0) {
-          rateHot = fmax(c.bhHotCoef * rAcc * rAcc * rho, 0.0);
-          rateHot = fmin(rateHot, fmax(massHot * c.bhHotMaxCoef, 0.0));
-          if (eps > 0.0) rateHot = fmin(rateHot, eddingtonCap);
+          rateHot = dmax(c.bhHotCoef * rAcc * rAcc * rho, 0.0);
+          rateHot = dmin(rateHot, dmax(massHot * c.bhHotMaxCoef, 0.0));
+          if (eps > 0.0) rateHot = dmin(rateHot, eddingtonCap);
         }
       }
     }
@@ -389,7 +427,7 @@ __device__ __forceinline__ void rhs(const Globals& G, const double2* tab, const 
   if ((ph & GAL_PHYS_COOLING) && massHot > 0.0 && c.rOuter > 0.0) {
     double rate = 0.0;
     if (c.coolingAllowed) {
-      if (!coolingRadiusKnown) rCool = cooling_radius(G, tab, sLnZ, sInvDlnZ, c, massHot, zHot);
+      if (!coolingRadiusKnown) rCool = cooling_radius(G, S, c, massHot, zHot, cv);
       if (rCool >= c.rOuter) {
         rate = massHot * c.invTdyn;
       } else if (rCool > 0.0) {

@@ -1,0 +1,219 @@
+// surrogate.cuh -- the cooling-function surrogate: a 3-64-64-64-1 SiLU MLP
+// from (log10 T, log10 Z/Zsun, log10 n_H) to log10 Lambda, evaluated by one
+// warp for the 32 nodes of its lanes.  The CIE cooling function scales
+// exactly as n_H^2 (cieFileCoolingFunctionDensityLogSlope = 2,
+// CIE_file.F90:514-533), so that dependence enters as a fixed term:
+// log10 Lambda = (network output) y_scale + y_mean + 2 log10 n_H, and the
+// network learns the temperature and metallicity dependence.
+//
+// Layers 2 and 3 (64 -> 64) run on the tensor cores (mma.sync m16n8k16,
+// BF16 x BF16 with FP32 accumulation; the warp's 32 nodes are two 16-row
+// tiles).  Each FP32 operand is split into a BF16 high part and a BF16
+// remainder, v = hi + lo, and a product is taken as hi*hi + hi*lo + lo*hi
+// (three MMAs), which keeps about 16 significant bits -- plain BF16 operands
+// (8 bits) put up to 0.03 dex of rounding error on the output, three times
+// the fallback tolerance.  The activations never leave registers: layer 1
+// (3 -> 64, FP32) is computed directly in the A-fragment layout of layer 2,
+// the accumulator fragments of layer 2 are the A fragments of layer 3 (the
+// column pairs of an m16n8 accumulator are the column pairs of an m16k16 A
+// fragment), and the output layer (64 -> 1, FP32) reduces layer 3's
+// accumulators across the four lanes of a row group.  Only the weights live
+// in shared memory.
+//
+// Every lane of the warp must call surrogate_eval together (mma.sync is a
+// warp-collective instruction); lanes without a node feed any finite input
+// and ignore the result.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cstdint>
+
+namespace gal {
+
+constexpr int kMlpWidth = 64;
+constexpr int kMlpStride = 72;  // padded row length (BF16 elements) of the weight rows: conflict-free fragment loads
+
+// Parameter layout of the trained network (FP32, the order the trainer writes):
+// W1[64][3], b1[64], W2[64][64], b2[64], W3[64][64], b3[64], W4[64], b4.
+constexpr int kW1 = 0, kB1 = kW1 + 64 * 3, kW2 = kB1 + 64, kB2 = kW2 + 64 * 64, kW3 = kB2 + 64,
+              kB3 = kW3 + 64 * 64, kW4 = kB3 + 64, kB4 = kW4 + 64, kMlpParams = kB4 + 1;
+
+// The FP32 parameters kept in shared memory: w1[192], b1, b2, b3, w4 [64
+// each], b4 (449 values), and the BF16 weight planes W2 hi, W2 lo, W3 hi,
+// W3 lo, each [64][kMlpStride] with row n holding W[n][k].
+constexpr int kSurrSmall = 64 * 3 + 4 * 64 + 1;
+constexpr int kSurrPlane = 64 * kMlpStride;
+
+// Input normalisation and output scaling (x_n = (x - mean)/scale, log10
+// Lambda = y_n * yScale + yMean + 2 log10 n_H), the training domain, and
+// the cells of the (log10 T, log10 Z) plane where the deployed network
+// misses the table by more than the tolerance (the table is used there).
+struct SurrogateInfo {
+  float inMean[3], inScale[3];
+  float yMean, yScale;
+  float lo[3], hi[3];          // training domain of the three inputs
+  int mapT, mapZ;              // error-map cells in log10 T and log10 Z
+  float mapLoT, mapLoZ, mapInvDT, mapInvDZ;
+};
+
+// Shared-memory view of the network.
+struct SurrogateSmem {
+  const float* w1;              // [64][3]
+  const float* b1;              // [64]
+  const float* b2;
+  const float* b3;
+  const float* w4;              // [64]
+  float b4;
+  const __nv_bfloat16* w2hi;    // [64][kMlpStride]
+  const __nv_bfloat16* w2lo;
+  const __nv_bfloat16* w3hi;
+  const __nv_bfloat16* w3lo;
+};
+
+// View of the packed parameter block [small FP32 | 4 BF16 planes].
+__device__ __forceinline__ SurrogateSmem surrogate_view(const float* small, const __nv_bfloat16* planes) {
+  return SurrogateSmem{small, small + 192, small + 256, small + 320, small + 384, small[448],
+                       planes, planes + kSurrPlane, planes + 2 * kSurrPlane, planes + 3 * kSurrPlane};
+}
+
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
+
+__device__ __forceinline__ uint32_t bf16_bits(__nv_bfloat162 v) { return *reinterpret_cast<const uint32_t*>(&v); }
+
+// (a, b) -> BF16 pairs hi and lo with a = hi.x + lo.x, b = hi.y + lo.y to ~2^-16.
+__device__ __forceinline__ void split_bf16(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const float2 hf = __bfloat1622float2(h);
+  hi = bf16_bits(h);
+  lo = bf16_bits(__floats2bfloat162_rn(a - hf.x, b - hf.y));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// One 64 -> 64 layer for one 16-row tile: acc[nt] (columns nt*8 + 2t, +1 of
+// rows g and g+8) = bias + A W^T with the split products.
+__device__ __forceinline__ void mlp_layer_tile(const uint32_t (&ahi)[4][4], const uint32_t (&alo)[4][4],
+                                               const __nv_bfloat16* whi, const __nv_bfloat16* wlo, const float* bias,
+                                               float (&acc)[8][4], int g, int t) {
+#pragma unroll
+  for (int nt = 0; nt < 8; ++nt) {
+    const int col = nt * 8 + 2 * t;
+    acc[nt][0] = bias[col];
+    acc[nt][1] = bias[col + 1];
+    acc[nt][2] = bias[col];
+    acc[nt][3] = bias[col + 1];
+    const int wrow = (nt * 8 + g) * kMlpStride + 2 * t;
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+      const uint32_t bh0 = *reinterpret_cast<const uint32_t*>(whi + wrow + ks * 16);
+      const uint32_t bh1 = *reinterpret_cast<const uint32_t*>(whi + wrow + ks * 16 + 8);
+      const uint32_t bl0 = *reinterpret_cast<const uint32_t*>(wlo + wrow + ks * 16);
+      const uint32_t bl1 = *reinterpret_cast<const uint32_t*>(wlo + wrow + ks * 16 + 8);
+      mma_bf16(acc[nt], alo[ks], bh0, bh1);
+      mma_bf16(acc[nt], ahi[ks], bl0, bl1);
+      mma_bf16(acc[nt], ahi[ks], bh0, bh1);
+    }
+  }
+}
+
+// Normalised output of the network for this lane's input (x0, x1, x2):
+// returns y_n.  `need` is the warp's ballot of lanes that use the result;
+// a 16-row tile (lanes 0-15 or 16-31) that no such lane falls in is skipped
+// (warp-uniform), which halves the cost when a warp integrates its last few
+// nodes.  Warp-collective.
+__device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0, float x1, float x2, int lane,
+                                               unsigned need = 0xffffffffu) {
+  const unsigned FULLMASK = 0xffffffffu;
+  const int g = lane >> 2, t = lane & 3;
+  float part[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};  // [m-tile][row g, row g+8]: this lane's share of the output
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt) {
+    if (((need >> (16 * mt)) & 0xffffu) == 0u) continue;
+    const int r0 = mt * 16 + g, r1 = r0 + 8;
+    const float u0 = __shfl_sync(FULLMASK, x0, r0), u1 = __shfl_sync(FULLMASK, x1, r0), u2 = __shfl_sync(FULLMASK, x2, r0);
+    const float v0 = __shfl_sync(FULLMASK, x0, r1), v1 = __shfl_sync(FULLMASK, x1, r1), v2 = __shfl_sync(FULLMASK, x2, r1);
+    // Layer 1 (FP32) straight into layer 2's A fragments: for k-step ks the
+    // lane holds columns ks*16 + 2t, +1 (regs 0, 1) and ks*16 + 8 + 2t, +1
+    // (regs 2, 3) of rows r0 (regs 0, 2) and r1 (regs 1, 3).
+    uint32_t ahi[4][4], alo[4][4];
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int c = ks * 16 + half * 8 + 2 * t;
+        const float* wa = N.w1 + 3 * c;
+        const float h00 = silu(fmaf(wa[2], u2, fmaf(wa[1], u1, fmaf(wa[0], u0, N.b1[c]))));
+        const float h01 = silu(fmaf(wa[5], u2, fmaf(wa[4], u1, fmaf(wa[3], u0, N.b1[c + 1]))));
+        const float h10 = silu(fmaf(wa[2], v2, fmaf(wa[1], v1, fmaf(wa[0], v0, N.b1[c]))));
+        const float h11 = silu(fmaf(wa[5], v2, fmaf(wa[4], v1, fmaf(wa[3], v0, N.b1[c + 1]))));
+        split_bf16(h00, h01, ahi[ks][2 * half], alo[ks][2 * half]);
+        split_bf16(h10, h11, ahi[ks][2 * half + 1], alo[ks][2 * half + 1]);
+      }
+    }
+    float acc[8][4];
+    mlp_layer_tile(ahi, alo, N.w2hi, N.w2lo, N.b2, acc, g, t);
+    // Layer 2's accumulators (n-tiles 2ks and 2ks+1) are layer 3's A fragments for k-step ks.
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+      split_bf16(silu(acc[2 * ks][0]), silu(acc[2 * ks][1]), ahi[ks][0], alo[ks][0]);
+      split_bf16(silu(acc[2 * ks][2]), silu(acc[2 * ks][3]), ahi[ks][1], alo[ks][1]);
+      split_bf16(silu(acc[2 * ks + 1][0]), silu(acc[2 * ks + 1][1]), ahi[ks][2], alo[ks][2]);
+      split_bf16(silu(acc[2 * ks + 1][2]), silu(acc[2 * ks + 1][3]), ahi[ks][3], alo[ks][3]);
+    }
+    mlp_layer_tile(ahi, alo, N.w3hi, N.w3lo, N.b3, acc, g, t);
+    // Output layer (FP32): this lane's 16 columns of rows r0 and r1, then the
+    // sum over the four lanes of the row group.
+    float p0 = 0.0f, p1 = 0.0f;
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+      const int col = nt * 8 + 2 * t;
+      p0 = fmaf(N.w4[col], silu(acc[nt][0]), fmaf(N.w4[col + 1], silu(acc[nt][1]), p0));
+      p1 = fmaf(N.w4[col], silu(acc[nt][2]), fmaf(N.w4[col + 1], silu(acc[nt][3]), p1));
+    }
+    p0 += __shfl_xor_sync(FULLMASK, p0, 1);
+    p0 += __shfl_xor_sync(FULLMASK, p0, 2);
+    p1 += __shfl_xor_sync(FULLMASK, p1, 1);
+    p1 += __shfl_xor_sync(FULLMASK, p1, 2);
+    part[mt][0] = p0;
+    part[mt][1] = p1;
+  }
+  // Row `lane` is row g' = lane & 7 of half (lane >> 3) of the two tiles: its
+  // sum sits in lane 4 (lane & 7).
+  const int src = 4 * (lane & 7);
+  const float a = __shfl_sync(FULLMASK, part[0][0], src), b = __shfl_sync(FULLMASK, part[0][1], src);
+  const float c = __shfl_sync(FULLMASK, part[1][0], src), d = __shfl_sync(FULLMASK, part[1][1], src);
+  const int q = lane >> 3;
+  return N.b4 + (q == 0 ? a : (q == 1 ? b : (q == 2 ? c : d)));
+}
+
+// Host-side packing of the FP32 parameters into the block the kernels
+// stage: small[kSurrSmall] then the four BF16 planes (hi/lo of W2, W3).
+inline void surrogate_pack(const float* P, float* small, __nv_bfloat16* planes) {
+  for (int i = 0; i < 192; ++i) small[i] = P[kW1 + i];
+  for (int i = 0; i < 64; ++i) {
+    small[192 + i] = P[kB1 + i];
+    small[256 + i] = P[kB2 + i];
+    small[320 + i] = P[kB3 + i];
+    small[384 + i] = P[kW4 + i];
+  }
+  small[448] = P[kB4];
+  for (int i = 0; i < 4 * kSurrPlane; ++i) planes[i] = __float2bfloat16_rn(0.0f);
+  for (int layer = 0; layer < 2; ++layer) {
+    const float* W = P + (layer == 0 ? kW2 : kW3);
+    __nv_bfloat16* hi = planes + (2 * layer) * kSurrPlane;
+    __nv_bfloat16* lo = planes + (2 * layer + 1) * kSurrPlane;
+    for (int r = 0; r < 64; ++r)
+      for (int k = 0; k < 64; ++k) {
+        const float w = W[r * 64 + k];
+        const __nv_bfloat16 h = __float2bfloat16_rn(w);
+        hi[r * kMlpStride + k] = h;
+        lo[r * kMlpStride + k] = __float2bfloat16_rn(w - __bfloat162float(h));
+      }
+  }
+}
+
+}  // namespace gal

@@ -43,7 +43,7 @@ class MergerTreeNodeEvolverStandard:
     """GB300 evolver of node property vectors (batched)."""
 
     def __init__(self, odeToleranceAbsolute=0.01, odeToleranceRelative=0.01, reuseODEStepSize=True,
-                 params=None, table=None, stepBudget=None):
+                 params=None, table=None, stepBudget=None, ratePrecision="fp64"):
         self.lib = _abi.load_library()
         self.params = params if params is not None else _abi.default_params()
         if params is None:
@@ -58,6 +58,7 @@ class MergerTreeNodeEvolverStandard:
         rc = self.lib.gal_gpu_init(ctypes.byref(self.params), ctypes.byref(self.table.struct), ctypes.byref(ctx))
         _check(self.lib, None, rc)
         self.ctx = ctx
+        self.set_rate_precision(ratePrecision)
 
     def close(self):
         if getattr(self, "ctx", None):
@@ -72,6 +73,12 @@ class MergerTreeNodeEvolverStandard:
 
     def set_launch(self, threads_per_block=0, blocks_per_sm=0):
         _check(self.lib, self.ctx, self.lib.gal_gpu_set_launch(self.ctx, threads_per_block, blocks_per_sm))
+
+    def set_rate_precision(self, precision):
+        """"fp64" (the reference's arithmetic) or "fp32" (FP32 rates; FP64
+        state, error norm and step control)."""
+        code = {"fp64": _abi.RATES_FP64, "fp32": _abi.RATES_FP32}[precision]
+        _check(self.lib, self.ctx, self.lib.gal_gpu_set_rate_precision(self.ctx, code))
 
     def get_launch(self):
         t, b = ctypes.c_int32(), ctypes.c_int32()

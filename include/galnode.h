@@ -107,6 +107,13 @@ enum {
   GAL_OUTFLOW_FIXED = 1      /* stellarFeedbackOutflowsFixed    */
 };
 
+/* Arithmetic of the rate functions (gal_gpu_set_rate_precision).  The state,
+ * the error norm and the step-size control are FP64 in both. */
+enum {
+  GAL_RATES_FP64 = 0, /* the reference's arithmetic (default)          */
+  GAL_RATES_FP32 = 1  /* FP32 rates and table: the fast form           */
+};
+
 /* Star formation in one component (disk or spheroid).
  * Reference: source/star_formation/timescales/dynamical_time.F90:121-189,
  * source/star_formation/rates/disks/timescale.F90:109-130. */
@@ -250,9 +257,19 @@ int gal_gpu_evolve_batch_noalloc(const gal_params* p, const gal_cie_table* table
                                  int32_t* status, uint32_t* counters, void* stream);
 
 /* Launch shape of the evolve kernel (threads per block, blocks per SM); 0
- * keeps the current value.  Used by the autotuner. */
+ * keeps the current value.  Used by the autotuner.  Block sizes per form:
+ * FP64 rates 64-512, FP32 rates 128-512, with the surrogate 128 or 256;
+ * get_launch reports the shape the current form will use. */
 int gal_gpu_set_launch(gal_ctx* ctx, int32_t threads_per_block, int32_t blocks_per_sm);
 int gal_gpu_get_launch(const gal_ctx* ctx, int32_t* threads_per_block, int32_t* blocks_per_sm);
+
+/* Arithmetic of the rate functions: GAL_RATES_FP64 (default; the
+ * reference's FP64 arithmetic throughout) or GAL_RATES_FP32 (rates, cooling
+ * table and stage arguments in FP32; the state, the accepted-step update,
+ * the error norm and the step control stay FP64).  No counterpart in the
+ * reference, which evaluates every rate in FP64. */
+int gal_gpu_set_rate_precision(gal_ctx* ctx, int32_t precision);
+int gal_gpu_get_rate_precision(const gal_ctx* ctx);
 
 /* Number of kernel launches this context has made since creation. */
 int64_t gal_gpu_launch_count(const gal_ctx* ctx);

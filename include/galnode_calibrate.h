@@ -19,6 +19,14 @@ extern "C" {
  * DFMA) to *flops and the kernel time in ms to *ms.  Returns 0 on success. */
 int gal_calibrate_fp64(double* flops, double* ms);
 
+/* Self-test of the integrator's short FP64 functions against the CUDA library
+ * over 4M arguments: reciprocal, quotient, reciprocal square root and square
+ * root on 1e-29..1e29 (relative error), log on 1e-29..1e29 (error relative
+ * to max(1, |ln x|)), exp on -120..5 (relative error) and the controller's inverse fifth
+ * and sixth roots on 3e-5..1900 (relative error).  Writes the eight worst
+ * errors to maxRelErr[0..7].  Returns 0 on success. */
+int gal_selftest_fastmath(double* maxRelErr);
+
 #ifdef __cplusplus
 }
 #endif

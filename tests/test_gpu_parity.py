@@ -138,3 +138,15 @@ def test_launch_shapes_agree(evolver, oracle_mod):
     evolver.set_launch(128, 1)
     for r in results[1:]:
         np.testing.assert_array_equal(r, results[0])
+
+
+def test_fastmath_helpers_are_full_precision():
+    """The short FP64 functions of the integrator's critical path stay within
+    a few ulp of the CUDA library functions."""
+    import ctypes
+    lib = _abi.load_library()
+    err = (ctypes.c_double * 8)()
+    assert lib.gal_selftest_fastmath(err) == 0
+    names = ["rcp", "div", "rsqrt", "sqrt", "log", "exp", "inv_root5", "inv_root6"]
+    for name, e in zip(names, err):
+        assert e < 2e-15, f"{name}: max error {e:.3g}"
