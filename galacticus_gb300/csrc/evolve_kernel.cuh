@@ -297,194 +297,432 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
     }
   };
 
-  for (;;) {
-    // ---- refill lanes whose node has finished (warp-aggregated queue pop)
-    const unsigned need = __ballot_sync(FULL, phase == PH_NEED);
-    if (need) {
-      const int leader = __ffs(need) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(b.queue, (unsigned long long)__popc(need));
-      base = __shfl_sync(FULL, base, leader);
-      if (phase == PH_NEED) {
-        node = (int64_t)(base + __popc(need & ((1u << lane) - 1u)));
-        if (node >= n) {
-          phase = PH_DONE;
-        } else {
-          double prm[GAL_NP];
+  if constexpr (MODE == MODE_PLAIN) {
+    // The FP64 parity form: every right-hand side inlined at its stage, the
+    // stage arguments computed by the whole warp at once.
+    for (;;) {
+      // ---- refill lanes whose node has finished (warp-aggregated queue pop)
+      const unsigned need = __ballot_sync(FULL, phase == PH_NEED);
+      if (need) {
+        const int leader = __ffs(need) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(b.queue, (unsigned long long)__popc(need));
+        base = __shfl_sync(FULL, base, leader);
+        if (phase == PH_NEED) {
+          node = (int64_t)(base + __popc(need & ((1u << lane) - 1u)));
+          if (node >= n) {
+            phase = PH_DONE;
+          } else {
+            double prm[GAL_NP];
 #pragma unroll
-          for (int v = 0; v < GAL_NP; ++v) prm[v] = b.param[v * n + node];
-          node_setup(G, sLnT, prm, c);
-          if constexpr (FAST) cf = node_fast(c);
+            for (int v = 0; v < GAL_NP; ++v) prm[v] = b.param[v * n + node];
+            node_setup(G, sLnT, prm, c);
+            if constexpr (FAST) cf = node_fast(c);
+#pragma unroll
+            for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
+            scales(y, c.massHalo, s);
+            t0 = b.tStart[node];
+            t1 = b.tEnd[node];
+            stepIn = b.step[node];
+            trial = 0;
+            nAcc = nRej = nRhs = 0;
+            phase = PH_TRIAL;
+          }
+        }
+      }
+      if (__all_sync(FULL, phase == PH_DONE)) break;
+
+      // ---- start (or restart) an ODE trial: odeSolverSolve + driver reset
+      if (phase == PH_TRIAL && t0 == t1) {
+        b.step[node] = -1.0;  // node%timeStepSet(-1) when there is nothing to do
+        b.status[node] = GAL_STATUS_SUCCESS;
+        if (b.counters) {
+          b.counters[node] = 0; b.counters[n + node] = 0; b.counters[2 * n + node] = 0;
+        }
+        phase = PH_NEED;
+      }
+      const bool starting = phase == PH_TRIAL;
+      if (starting) {
+        const double stepSize = G.p.reuse_step_size ? stepIn / (double)(1u << trial) : -1.0;
+        h = t1 - t0;
+        if (stepSize > 0.0) h = fmin(stepSize, h);
+        if (trial > 0) {
 #pragma unroll
           for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
-          scales(y, c.massHalo, s);
-          t0 = b.tStart[node];
-          t1 = b.tEnd[node];
-          stepIn = b.step[node];
-          trial = 0;
-          nAcc = nRej = nRhs = 0;
-          phase = PH_TRIAL;
+        }
+        sync_yr();
+        t = t0;
+        count = 0;
+      }
+      if (any(starting)) eval(yr, k1, starting);  // dydt_in of the first step
+      if (starting) {
+        ++nRhs;
+        phase = PH_STEP;
+      }
+
+      // ---- one attempted step (one pass of gsl_odeiv2_evolve_apply's try_step)
+      const bool stepping = phase == PH_STEP;
+      bool needOut = false;
+      bool finished = false;
+      int finalStatus = GAL_STATUS_SUCCESS;
+      if (any(stepping)) {
+        const double dt = t1 - t;
+        const bool finalStep = (dt >= 0.0 && h > dt) || (dt < 0.0 && h < dt);
+        const double hh = finalStep ? dt : h;
+        const RateT hr = (RateT)hh;
+        // Stage arguments: y + h sum_j b_ij k_j (in the rate precision).
+#pragma unroll
+        for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + (RateT)ck::b21 * hr * k1[i];
+        eval(x, k2, stepping);
+#pragma unroll
+        for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + hr * ((RateT)ck::b31 * k1[i] + (RateT)ck::b32 * k2[i]);
+        eval(x, k3, stepping);
+#pragma unroll
+        for (int i = 0; i < GAL_NY; ++i)
+          x[i] = yr[i] + hr * ((RateT)ck::b41 * k1[i] + (RateT)ck::b42 * k2[i] + (RateT)ck::b43 * k3[i]);
+        eval(x, k4, stepping);
+#pragma unroll
+        for (int i = 0; i < GAL_NY; ++i)
+          x[i] = yr[i] + hr * ((RateT)ck::b51 * k1[i] + (RateT)ck::b52 * k2[i] + (RateT)ck::b53 * k3[i] +
+                               (RateT)ck::b54 * k4[i]);
+        eval(x, k5, stepping);
+#pragma unroll
+        for (int i = 0; i < GAL_NY; ++i)
+          x[i] = yr[i] + hr * ((RateT)ck::b61 * k1[i] + (RateT)ck::b62 * k2[i] + (RateT)ck::b63 * k3[i] +
+                               (RateT)ck::b64 * k4[i] + (RateT)ck::b65 * k5[i]);
+        eval(x, k6, stepping);
+        if (stepping) {
+          nRhs += 5;
+          // 5th-order solution, scaled error ratio (sc2_control_hadjust, a_y=1, a_dydt=0), FP64.
+          // The largest |err_i|/D_i is found by cross-multiplication and divided
+          // once (max of the quotients = quotient of the maximal pair).
+          double errMax = 0.0, dMax = 1.0;
+#pragma unroll
+          for (int i = 0; i < GAL_NY; ++i) {
+            const RateT inc = (RateT)ck::c1 * k1[i] + (RateT)ck::c3 * k3[i] + (RateT)ck::c4 * k4[i] + (RateT)ck::c6 * k6[i];
+            const RateT est = (RateT)ck::e1 * k1[i] + (RateT)ck::e3 * k3[i] + (RateT)ck::e4 * k4[i] + (RateT)ck::e5 * k5[i] +
+                              (RateT)ck::e6 * k6[i];
+            ynew[i] = y[i] + hh * (double)inc;
+            const double err = fabs(hh * (double)est);
+            const double D0 = fabs(epsRel * fabs(ynew[i]) + epsAbs * s[i]);
+            if (err * dMax > errMax * D0 || !(err == err)) {
+              errMax = err;
+              dMax = D0;
+            }
+          }
+          const double rmax = dmax(fast_div(errMax, dMax), 2.2250738585072014e-308);  // floor DBL_MIN as cscal2.c
+          ++count;
+          const double tNew = finalStep ? t1 : t + hh;
+          double hNew = hh;
+          bool decrease = false;
+          // 0.9 rmax^(-1/5), floored at 0.2 (reached for rmax >= 4.5^5 exactly),
+          // and 0.9 rmax^(-1/6) capped at 4.9 (reached below (0.9/4.9)^6).
+          if (rmax > 1.1) {
+            double r = rmax > 1845.28125 ? 0.2 : 0.9 * inv_root<5>(rmax);
+            if (r < 0.2) r = 0.2;
+            hNew = r * hh;
+            decrease = true;
+          } else if (rmax < 0.5) {
+            double r = rmax < 3.8394e-5 ? 4.9 : 0.9 * inv_root<6>(rmax);
+            if (r > 4.9) r = 4.9;
+            if (r < 1.0) r = 1.0;
+            hNew = r * hh;
+          }
+          if (decrease) {
+            const double tNext = tNew + hNew;
+            if (fabs(hNew) < fabs(hh) && tNext != tNew) {
+              h = hNew;  // reject: retry from the same (t, y) with the smaller step
+              ++nRej;
+              if (budget && count >= budget) { finished = true; finalStatus = GAL_STATUS_XCPU; }
+            } else {
+              // The step cannot shrink any further: this trial fails
+              // (GSL_FAILURE); the node evolver restarts with half the step.
+              ++trial;
+              if (trial >= G.p.trial_count_maximum) { finished = true; finalStatus = GAL_STATUS_UNDERFLOW; }
+              else phase = PH_TRIAL;
+            }
+          } else {
+            // Accept.
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) y[i] = ynew[i];
+            sync_yr();
+            t = tNew;
+            h = hNew;
+            ++nAcc;
+            const bool reached = !(t1 - t > 0.0 || t1 - t < 0.0);
+            if (reached) {
+              post_step(y);
+              finished = true;
+              bool finite = true;
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i) finite = finite && isfinite(y[i]);
+              finalStatus = finite ? GAL_STATUS_SUCCESS : GAL_STATUS_NOT_FINITE;
+            } else {
+              needOut = true;
+            }
+          }
         }
       }
-    }
-    if (__all_sync(FULL, phase == PH_DONE)) break;
-
-    // ---- start (or restart) an ODE trial: odeSolverSolve + driver reset
-    if (phase == PH_TRIAL && t0 == t1) {
-      b.step[node] = -1.0;  // node%timeStepSet(-1) when there is nothing to do
-      b.status[node] = GAL_STATUS_SUCCESS;
-      if (b.counters) {
-        b.counters[node] = 0; b.counters[n + node] = 0; b.counters[2 * n + node] = 0;
+      // dydt_out at the accepted point, reused as the next dydt_in; then the
+      // post-step clamps (they return GSL_Continue: dydt_out is kept).
+      if (any(needOut)) eval(yr, k1, needOut);
+      if (needOut) {
+        ++nRhs;
+        post_step(y);
+        sync_yr();
+        if (budget && count >= budget) {
+          finished = true;
+          finalStatus = GAL_STATUS_XCPU;
+        }
       }
-      phase = PH_NEED;
-    }
-    const bool starting = phase == PH_TRIAL;
-    if (starting) {
-      const double stepSize = G.p.reuse_step_size ? stepIn / (double)(1u << trial) : -1.0;
-      h = t1 - t0;
-      if (stepSize > 0.0) h = fmin(stepSize, h);
-      if (trial > 0) {
+      if (finished) {
+        if (finalStatus == GAL_STATUS_SUCCESS) {
 #pragma unroll
-        for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
+          for (int v = 0; v < GAL_NY; ++v) b.state[v * n + node] = y[v];
+          b.step[node] = h;
+        }
+        b.status[node] = finalStatus;
+        if (b.counters) {
+          b.counters[node] = nAcc;
+          b.counters[n + node] = nRej;
+          b.counters[2 * n + node] = nRhs;
+        }
+        phase = PH_NEED;
       }
-      sync_yr();
-      t = t0;
-      count = 0;
     }
-    if (any(starting)) eval(yr, k1, starting);  // dydt_in of the first step
-    if (starting) {
-      ++nRhs;
-      phase = PH_STEP;
-    }
-
-    // ---- one attempted step (one pass of gsl_odeiv2_evolve_apply's try_step)
-    const bool stepping = phase == PH_STEP;
+  } else {
+    // The main loop makes two kinds of right-hand-side evaluation, each from
+    // one call site, so that the right-hand side (and the network) is
+    // compiled twice rather than once per stage: f(y) for lanes that start a
+    // trial (dydt_in) or accepted a step in the previous pass (dydt_out), and
+    // the five stage slopes of an attempt, in a loop whose stage index is the
+    // same for every lane of the warp (lanes attempt steps together, so the
+    // FP64 error norm and step control run once per attempt for the warp).
     bool needOut = false;
-    bool finished = false;
-    int finalStatus = GAL_STATUS_SUCCESS;
-    if (any(stepping)) {
-      const double dt = t1 - t;
-      const bool finalStep = (dt >= 0.0 && h > dt) || (dt < 0.0 && h < dt);
-      const double hh = finalStep ? dt : h;
-      const RateT hr = (RateT)hh;
-      // Stage arguments: y + h sum_j b_ij k_j (in the rate precision).
-#pragma unroll
-      for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + (RateT)ck::b21 * hr * k1[i];
-      eval(x, k2, stepping);
-#pragma unroll
-      for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + hr * ((RateT)ck::b31 * k1[i] + (RateT)ck::b32 * k2[i]);
-      eval(x, k3, stepping);
-#pragma unroll
-      for (int i = 0; i < GAL_NY; ++i)
-        x[i] = yr[i] + hr * ((RateT)ck::b41 * k1[i] + (RateT)ck::b42 * k2[i] + (RateT)ck::b43 * k3[i]);
-      eval(x, k4, stepping);
-#pragma unroll
-      for (int i = 0; i < GAL_NY; ++i)
-        x[i] = yr[i] + hr * ((RateT)ck::b51 * k1[i] + (RateT)ck::b52 * k2[i] + (RateT)ck::b53 * k3[i] +
-                             (RateT)ck::b54 * k4[i]);
-      eval(x, k5, stepping);
-#pragma unroll
-      for (int i = 0; i < GAL_NY; ++i)
-        x[i] = yr[i] + hr * ((RateT)ck::b61 * k1[i] + (RateT)ck::b62 * k2[i] + (RateT)ck::b63 * k3[i] +
-                             (RateT)ck::b64 * k4[i] + (RateT)ck::b65 * k5[i]);
-      eval(x, k6, stepping);
-      if (stepping) {
-        nRhs += 5;
-        // 5th-order solution, scaled error ratio (sc2_control_hadjust, a_y=1, a_dydt=0), FP64.
-        // The largest |err_i|/D_i is found by cross-multiplication and divided
-        // once (max of the quotients = quotient of the maximal pair).
-        double errMax = 0.0, dMax = 1.0;
-#pragma unroll
-        for (int i = 0; i < GAL_NY; ++i) {
-          const RateT inc = (RateT)ck::c1 * k1[i] + (RateT)ck::c3 * k3[i] + (RateT)ck::c4 * k4[i] + (RateT)ck::c6 * k6[i];
-          const RateT est = (RateT)ck::e1 * k1[i] + (RateT)ck::e3 * k3[i] + (RateT)ck::e4 * k4[i] + (RateT)ck::e5 * k5[i] +
-                            (RateT)ck::e6 * k6[i];
-          ynew[i] = y[i] + hh * (double)inc;
-          const double err = fabs(hh * (double)est);
-          const double D0 = fabs(epsRel * fabs(ynew[i]) + epsAbs * s[i]);
-          if (err * dMax > errMax * D0 || !(err == err)) {
-            errMax = err;
-            dMax = D0;
-          }
-        }
-        const double rmax = dmax(fast_div(errMax, dMax), 2.2250738585072014e-308);  // floor DBL_MIN as cscal2.c
-        ++count;
-        const double tNew = finalStep ? t1 : t + hh;
-        double hNew = hh;
-        bool decrease = false;
-        // 0.9 rmax^(-1/5), floored at 0.2 (reached for rmax >= 4.5^5 exactly),
-        // and 0.9 rmax^(-1/6) capped at 4.9 (reached below (0.9/4.9)^6).
-        if (rmax > 1.1) {
-          double r = rmax > 1845.28125 ? 0.2 : 0.9 * inv_root<5>(rmax);
-          if (r < 0.2) r = 0.2;
-          hNew = r * hh;
-          decrease = true;
-        } else if (rmax < 0.5) {
-          double r = rmax < 3.8394e-5 ? 4.9 : 0.9 * inv_root<6>(rmax);
-          if (r > 4.9) r = 4.9;
-          if (r < 1.0) r = 1.0;
-          hNew = r * hh;
-        }
-        if (decrease) {
-          const double tNext = tNew + hNew;
-          if (fabs(hNew) < fabs(hh) && tNext != tNew) {
-            h = hNew;  // reject: retry from the same (t, y) with the smaller step
-            ++nRej;
-            if (budget && count >= budget) { finished = true; finalStatus = GAL_STATUS_XCPU; }
+    for (;;) {
+      // ---- refill lanes whose node has finished (warp-aggregated queue pop)
+      const unsigned need = __ballot_sync(FULL, phase == PH_NEED);
+      if (need) {
+        const int leader = __ffs(need) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(b.queue, (unsigned long long)__popc(need));
+        base = __shfl_sync(FULL, base, leader);
+        if (phase == PH_NEED) {
+          node = (int64_t)(base + __popc(need & ((1u << lane) - 1u)));
+          if (node >= n) {
+            phase = PH_DONE;
           } else {
-            // The step cannot shrink any further: this trial fails
-            // (GSL_FAILURE); the node evolver restarts with half the step.
-            ++trial;
-            if (trial >= G.p.trial_count_maximum) { finished = true; finalStatus = GAL_STATUS_UNDERFLOW; }
-            else phase = PH_TRIAL;
-          }
-        } else {
-          // Accept.
+            double prm[GAL_NP];
 #pragma unroll
-          for (int i = 0; i < GAL_NY; ++i) y[i] = ynew[i];
-          sync_yr();
-          t = tNew;
-          h = hNew;
-          ++nAcc;
-          const bool reached = !(t1 - t > 0.0 || t1 - t < 0.0);
-          if (reached) {
-            post_step(y);
-            finished = true;
-            bool finite = true;
+            for (int v = 0; v < GAL_NP; ++v) prm[v] = b.param[v * n + node];
+            node_setup(G, sLnT, prm, c);
+            if constexpr (FAST) cf = node_fast(c);
 #pragma unroll
-            for (int i = 0; i < GAL_NY; ++i) finite = finite && isfinite(y[i]);
-            finalStatus = finite ? GAL_STATUS_SUCCESS : GAL_STATUS_NOT_FINITE;
-          } else {
-            needOut = true;
+            for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
+            scales(y, c.massHalo, s);
+            t0 = b.tStart[node];
+            t1 = b.tEnd[node];
+            stepIn = b.step[node];
+            trial = 0;
+            nAcc = nRej = nRhs = 0;
+            phase = PH_TRIAL;
           }
         }
       }
-    }
-    // dydt_out at the accepted point, reused as the next dydt_in; then the
-    // post-step clamps (they return GSL_Continue: dydt_out is kept).
-    if (any(needOut)) eval(yr, k1, needOut);
-    if (needOut) {
-      ++nRhs;
-      post_step(y);
-      sync_yr();
-      if (budget && count >= budget) {
-        finished = true;
-        finalStatus = GAL_STATUS_XCPU;
+      if (__all_sync(FULL, phase == PH_DONE)) break;
+
+      // ---- start (or restart) an ODE trial: odeSolverSolve + driver reset
+      if (phase == PH_TRIAL && t0 == t1) {
+        b.step[node] = -1.0;  // node%timeStepSet(-1) when there is nothing to do
+        b.status[node] = GAL_STATUS_SUCCESS;
+        if (b.counters) {
+          b.counters[node] = 0; b.counters[n + node] = 0; b.counters[2 * n + node] = 0;
+        }
+        phase = PH_NEED;
       }
-    }
-    if (finished) {
-      if (finalStatus == GAL_STATUS_SUCCESS) {
+      const bool starting = phase == PH_TRIAL;
+      if (starting) {
+        const double stepSize = G.p.reuse_step_size ? stepIn / (double)(1u << trial) : -1.0;
+        h = t1 - t0;
+        if (stepSize > 0.0) h = fmin(stepSize, h);
+        if (trial > 0) {
 #pragma unroll
-        for (int v = 0; v < GAL_NY; ++v) b.state[v * n + node] = y[v];
-        b.step[node] = h;
+          for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
+        }
+        sync_yr();
+        t = t0;
+        count = 0;
       }
-      b.status[node] = finalStatus;
-      if (b.counters) {
-        b.counters[node] = nAcc;
-        b.counters[n + node] = nRej;
-        b.counters[2 * n + node] = nRhs;
+      // f(y): dydt_in of a trial's first step, or dydt_out at the point
+      // accepted in the previous pass (reused as the next dydt_in).
+      const bool atY = starting || needOut;
+      if (any(atY)) eval(yr, k1, atY);
+      bool finished = false;
+      int finalStatus = GAL_STATUS_SUCCESS;
+      if (starting) {
+        ++nRhs;
+        phase = PH_STEP;
       }
-      phase = PH_NEED;
+      if (needOut) {
+        // The post-step clamps return GSL_Continue: dydt_out is kept.
+        needOut = false;
+        ++nRhs;
+        post_step(y);
+        sync_yr();
+        if (budget && count >= budget) {
+          finished = true;
+          finalStatus = GAL_STATUS_XCPU;
+        }
+      }
+
+      // ---- one attempted step (one pass of gsl_odeiv2_evolve_apply's try_step)
+      const bool stepping = phase == PH_STEP && !finished;
+      if (any(stepping)) {
+        const double dt = t1 - t;
+        const bool finalStep = (dt >= 0.0 && h > dt) || (dt < 0.0 && h < dt);
+        const double hh = finalStep ? dt : h;
+        const RateT hr = (RateT)hh;
+#pragma unroll 1
+        for (int st = 1; st <= 5; ++st) {
+          // Stage argument y + h sum_j b_ij k_j (in the rate precision); st is warp-uniform.
+          switch (st) {
+            case 1:
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + (RateT)ck::b21 * hr * k1[i];
+              break;
+            case 2:
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + hr * ((RateT)ck::b31 * k1[i] + (RateT)ck::b32 * k2[i]);
+              break;
+            case 3:
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i)
+                x[i] = yr[i] + hr * ((RateT)ck::b41 * k1[i] + (RateT)ck::b42 * k2[i] + (RateT)ck::b43 * k3[i]);
+              break;
+            case 4:
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i)
+                x[i] = yr[i] + hr * ((RateT)ck::b51 * k1[i] + (RateT)ck::b52 * k2[i] + (RateT)ck::b53 * k3[i] +
+                                     (RateT)ck::b54 * k4[i]);
+              break;
+            default:
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i)
+                x[i] = yr[i] + hr * ((RateT)ck::b61 * k1[i] + (RateT)ck::b62 * k2[i] + (RateT)ck::b63 * k3[i] +
+                                     (RateT)ck::b64 * k4[i] + (RateT)ck::b65 * k5[i]);
+              break;
+          }
+          RateT d[GAL_NY];
+          eval(x, d, stepping);
+          switch (st) {
+            case 1:
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i) k2[i] = d[i];
+              break;
+            case 2:
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i) k3[i] = d[i];
+              break;
+            case 3:
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i) k4[i] = d[i];
+              break;
+            case 4:
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i) k5[i] = d[i];
+              break;
+            default:
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i) k6[i] = d[i];
+              break;
+          }
+        }
+        if (stepping) {
+          nRhs += 5;
+          // 5th-order solution, scaled error ratio (sc2_control_hadjust, a_y=1, a_dydt=0), FP64.
+          // The largest |err_i|/D_i is found by cross-multiplication and divided
+          // once (max of the quotients = quotient of the maximal pair).
+          double errMax = 0.0, dMax = 1.0;
+#pragma unroll
+          for (int i = 0; i < GAL_NY; ++i) {
+            const RateT inc = (RateT)ck::c1 * k1[i] + (RateT)ck::c3 * k3[i] + (RateT)ck::c4 * k4[i] + (RateT)ck::c6 * k6[i];
+            const RateT est = (RateT)ck::e1 * k1[i] + (RateT)ck::e3 * k3[i] + (RateT)ck::e4 * k4[i] + (RateT)ck::e5 * k5[i] +
+                              (RateT)ck::e6 * k6[i];
+            ynew[i] = y[i] + hh * (double)inc;
+            const double err = fabs(hh * (double)est);
+            const double D0 = fabs(epsRel * fabs(ynew[i]) + epsAbs * s[i]);
+            if (err * dMax > errMax * D0 || !(err == err)) {
+              errMax = err;
+              dMax = D0;
+            }
+          }
+          const double rmax = dmax(fast_div(errMax, dMax), 2.2250738585072014e-308);  // floor DBL_MIN as cscal2.c
+          ++count;
+          const double tNew = finalStep ? t1 : t + hh;
+          double hNew = hh;
+          bool decrease = false;
+          // 0.9 rmax^(-1/5), floored at 0.2 (reached for rmax >= 4.5^5 exactly),
+          // and 0.9 rmax^(-1/6) capped at 4.9 (reached below (0.9/4.9)^6).
+          if (rmax > 1.1) {
+            double r = rmax > 1845.28125 ? 0.2 : 0.9 * inv_root<5>(rmax);
+            if (r < 0.2) r = 0.2;
+            hNew = r * hh;
+            decrease = true;
+          } else if (rmax < 0.5) {
+            double r = rmax < 3.8394e-5 ? 4.9 : 0.9 * inv_root<6>(rmax);
+            if (r > 4.9) r = 4.9;
+            if (r < 1.0) r = 1.0;
+            hNew = r * hh;
+          }
+          if (decrease) {
+            const double tNext = tNew + hNew;
+            if (fabs(hNew) < fabs(hh) && tNext != tNew) {
+              h = hNew;  // reject: retry from the same (t, y) with the smaller step
+              ++nRej;
+              if (budget && count >= budget) { finished = true; finalStatus = GAL_STATUS_XCPU; }
+            } else {
+              // The step cannot shrink any further: this trial fails
+              // (GSL_FAILURE); the node evolver restarts with half the step.
+              ++trial;
+              if (trial >= G.p.trial_count_maximum) { finished = true; finalStatus = GAL_STATUS_UNDERFLOW; }
+              else phase = PH_TRIAL;
+            }
+          } else {
+            // Accept.
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) y[i] = ynew[i];
+            sync_yr();
+            t = tNew;
+            h = hNew;
+            ++nAcc;
+            const bool reached = !(t1 - t > 0.0 || t1 - t < 0.0);
+            if (reached) {
+              post_step(y);
+              finished = true;
+              bool finite = true;
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i) finite = finite && isfinite(y[i]);
+              finalStatus = finite ? GAL_STATUS_SUCCESS : GAL_STATUS_NOT_FINITE;
+            } else {
+              needOut = true;
+            }
+          }
+        }
+      }
+      if (finished) {
+        if (finalStatus == GAL_STATUS_SUCCESS) {
+#pragma unroll
+          for (int v = 0; v < GAL_NY; ++v) b.state[v * n + node] = y[v];
+          b.step[node] = h;
+        }
+        b.status[node] = finalStatus;
+        if (b.counters) {
+          b.counters[node] = nAcc;
+          b.counters[n + node] = nRej;
+          b.counters[2 * n + node] = nRhs;
+        }
+        phase = PH_NEED;
+      }
     }
   }
   if (SURR && sd.stats) {

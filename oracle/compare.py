@@ -36,3 +36,8 @@ def parity_ratio(gpu, ref, state0, param, params, factor=10.0):
     """|gpu-ref| / (factor * tolerance) per property and node; <= 1 passes."""
     tol = factor * (params.ode_tolerance_relative * np.abs(ref) + params.ode_tolerance_absolute * scales(state0, param))
     return np.abs(gpu - ref) / tol
+
+
+def parity_bound(ref, state0, param, params, factor=10.0):
+    """The allowed |gpu - ref| of parity_ratio: factor times the tolerance."""
+    return factor * (params.ode_tolerance_relative * np.abs(ref) + params.ode_tolerance_absolute * scales(state0, param))
