@@ -17,7 +17,12 @@ LIB = os.path.join(HERE, "libgalnode.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177"]
 SOURCES = ["galnode.cu", "evolve_plain.cu", "evolve_surrogate.cu", "evolve_fast.cu", "evolve_fast_surrogate.cu",
-           "calibrate.cu", "surrogate_train.cu"]
+           "evolve_forest_plain.cu", "evolve_forest_fast.cu", "forest.cu", "calibrate.cu", "surrogate_train.cu",
+           "trees.cpp"]
+# Host code whose FP64 results must match the oracle's bit for bit: no contraction.
+NO_CONTRACT = {"forest.cu"}
+# Host-only sources (compiled by nvcc through the host compiler) that use OpenMP.
+OPENMP = {"trees.cpp"}
 
 
 def nvcc():
@@ -30,6 +35,10 @@ def nvcc():
 def _compile(src, verbose):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc(), *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+    if src in OPENMP:
+        cmd[1:1] = ["-Xcompiler", "-fopenmp"]
+    if src in NO_CONTRACT:
+        cmd[1:1] = ["-Xcompiler", "-ffp-contract=off"]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -41,10 +50,10 @@ def _compile(src, verbose):
 def build(verbose=False):
     """Compile every CUDA source and link ``libgalnode.so``."""
     os.makedirs(BUILD, exist_ok=True)
-    with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+    with concurrent.futures.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
         results = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
     objs = [o for o, _ in results]
-    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lgomp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

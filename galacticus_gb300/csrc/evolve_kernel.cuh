@@ -85,6 +85,37 @@ struct SurrogateDev {
   unsigned long long* stats;   // [2]: network and table evaluations
 };
 
+// A forest resident on the device (gal_gpu_forest_*): topology, the
+// pieces ("segments") each node's interval is cut into at the output times,
+// and the per-node and per-snapshot results.  Progenitor-less nodes are the
+// initial work; the last progenitor of a node to finish merges them into it
+// and goes on with it.
+struct ForestDev {
+  int64_t n;                    // nodes
+  int64_t nLeaves;
+  const int32_t* leaves;        // [nLeaves] progenitor-less nodes
+  const int32_t* parent;        // [n], -1 for a root
+  const int32_t* childFirst;    // [n]
+  const int32_t* childCount;    // [n]
+  int32_t* pending;             // [n] progenitors not yet finished (reset before each evolution)
+  const int32_t* segFirst;      // [n]
+  const int32_t* segCount;      // [n]
+  const int32_t* snapInitial;   // [n] snapshot slot of an output at the node's own time, or -1
+  int64_t nSeg;
+  const double* segParam;       // [GAL_NP][nSeg]
+  const double* segT0;          // [nSeg]
+  const double* segT1;          // [nSeg]
+  const int32_t* segSnap;       // [nSeg] snapshot slot at the segment's end, or -1
+  const double* state0;         // [GAL_NY][n] initial states (progenitor-less nodes)
+  double* state;                // [GAL_NY][n] segment start states, then final states
+  double* stepOut;              // [n] the step size on finishing (carried to the parent)
+  int64_t nSnap;
+  double* snapshots;            // [GAL_NY][nSnap]
+  int32_t* status;              // [n]
+  uint32_t* counters;           // [3][n]
+  unsigned long long* head;     // next unclaimed leaf (zeroed before each evolution)
+};
+
 // Shared-memory layout.  FP64 forms: [nZ*nT] double2 tables, the short-log
 // table [128 double2], ln T [nT], ln Z [nZ], 1/(ln Z[i+1] - ln Z[i]) [nZ],
 // the 2^(j/64) table [64].  FP32 forms: [nZ*nT] float2 tables, ln Z and the
@@ -177,10 +208,10 @@ __device__ __forceinline__ CoolingValuesF surrogate_cooling(const Globals& G, co
   return cv;
 }
 
-template <int THREADS, int MODE>
+template <int THREADS, int MODE, bool FOREST>
 __global__ void __launch_bounds__(THREADS, 1)
 evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant__ DeviceTables T,
-              const __grid_constant__ SurrogateDev sd) {
+              const __grid_constant__ SurrogateDev sd, const __grid_constant__ ForestDev F) {
   constexpr bool SURR = (MODE & MODE_SURROGATE) != 0;
   constexpr bool FAST = (MODE & MODE_FAST) != 0;
   using RateT = typename std::conditional<FAST, float, double>::type;
@@ -297,6 +328,169 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
     }
   };
 
+  // ---- work source and completion: a batch of independent nodes, or a forest
+  int32_t seg = 0, segEnd = 0;
+  // (forest) Set up the current segment of the node: its constants, tolerance
+  // scales and interval; keep the starting state for trial restarts.
+  auto start_segment = [&]() {
+    double prm[GAL_NP];
+#pragma unroll
+    for (int v = 0; v < GAL_NP; ++v) prm[v] = F.segParam[v * F.nSeg + seg];
+    node_setup(G, sLnT, prm, c);
+    if constexpr (FAST) cf = node_fast(c);
+#pragma unroll
+    for (int v = 0; v < GAL_NY; ++v) F.state[v * F.n + node] = y[v];
+    scales(y, c.massHalo, s);
+    t0 = F.segT0[seg];
+    t1 = F.segT1[seg];
+    trial = 0;
+    phase = PH_TRIAL;
+  };
+  // (forest) Finish the node with state y and status st; while this lane is
+  // the last progenitor of the parent to finish, merge the progenitors into
+  // the parent (the primary's state plus the others', component by
+  // component in index order) and go on with the parent.
+  auto complete_node = [&](int st) {
+    for (;;) {
+#pragma unroll
+      for (int v = 0; v < GAL_NY; ++v) F.state[v * F.n + node] = y[v];
+      F.stepOut[node] = stepIn;
+      F.status[node] = st;
+      if (F.counters) {
+        F.counters[node] = nAcc;
+        F.counters[F.n + node] = nRej;
+        F.counters[2 * F.n + node] = nRhs;
+      }
+      __threadfence();  // the state is visible before the parent's counter drops
+      const int32_t par = F.parent[node];
+      if (par < 0 || atomicSub(&F.pending[par], 1) != 1) {
+        phase = PH_NEED;
+        return;
+      }
+      __threadfence();  // every progenitor's state is visible after the last decrement
+      const int32_t c0 = F.childFirst[par], cn = F.childCount[par];
+#pragma unroll
+      for (int v = 0; v < GAL_NY; ++v) y[v] = F.state[v * F.n + c0];
+      for (int32_t j = 1; j < cn; ++j) {
+#pragma unroll
+        for (int v = 0; v < GAL_NY; ++v) y[v] += F.state[v * F.n + c0 + j];
+      }
+      stepIn = F.stepOut[c0];
+      node = par;
+      nAcc = nRej = nRhs = 0;
+      const int32_t slot = F.snapInitial[node];
+      if (slot >= 0) {
+#pragma unroll
+        for (int v = 0; v < GAL_NY; ++v) F.snapshots[v * F.nSnap + slot] = y[v];
+      }
+      seg = F.segFirst[node];
+      segEnd = seg + F.segCount[node];
+      if (seg < segEnd) {
+        start_segment();
+        return;
+      }
+      st = GAL_STATUS_SUCCESS;  // a node with nothing to evolve (a root at its own time)
+    }
+  };
+  // Take work item idx of the queue.
+  auto take = [&](unsigned long long idx) {
+    if constexpr (FOREST) {
+      if ((int64_t)idx >= F.nLeaves) {
+        phase = PH_DONE;
+        return;
+      }
+      node = F.leaves[idx];
+#pragma unroll
+      for (int v = 0; v < GAL_NY; ++v) y[v] = F.state0[v * F.n + node];
+      stepIn = -1.0;
+      nAcc = nRej = nRhs = 0;
+      const int32_t slot = F.snapInitial[node];
+      if (slot >= 0) {
+#pragma unroll
+        for (int v = 0; v < GAL_NY; ++v) F.snapshots[v * F.nSnap + slot] = y[v];
+      }
+      seg = F.segFirst[node];
+      segEnd = seg + F.segCount[node];
+      if (seg < segEnd) start_segment();
+      else complete_node(GAL_STATUS_SUCCESS);
+    } else {
+      node = (int64_t)idx;
+      if (node >= n) {
+        phase = PH_DONE;
+        return;
+      }
+      double prm[GAL_NP];
+#pragma unroll
+      for (int v = 0; v < GAL_NP; ++v) prm[v] = b.param[v * n + node];
+      node_setup(G, sLnT, prm, c);
+      if constexpr (FAST) cf = node_fast(c);
+#pragma unroll
+      for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
+      scales(y, c.massHalo, s);
+      t0 = b.tStart[node];
+      t1 = b.tEnd[node];
+      stepIn = b.step[node];
+      trial = 0;
+      nAcc = nRej = nRhs = 0;
+      phase = PH_TRIAL;
+    }
+  };
+  unsigned long long* const queueHead = FOREST ? F.head : b.queue;
+  // The state this evolve call started from (trial restarts, failures).
+  auto restore_start = [&]() {
+#pragma unroll
+    for (int v = 0; v < GAL_NY; ++v) y[v] = FOREST ? F.state[v * F.n + node] : b.state[v * n + node];
+  };
+  // An interval of zero length: nothing to do (node%timeStepSet(-1) in the batch form).
+  auto zero_interval = [&]() {
+    if constexpr (FOREST) {
+      h = stepIn;
+      if (++seg < segEnd) start_segment();
+      else complete_node(GAL_STATUS_SUCCESS);
+    } else {
+      b.step[node] = -1.0;
+      b.status[node] = GAL_STATUS_SUCCESS;
+      if (b.counters) {
+        b.counters[node] = 0; b.counters[n + node] = 0; b.counters[2 * n + node] = 0;
+      }
+      phase = PH_NEED;
+    }
+  };
+  // An evolve call ended with status st.
+  auto finish = [&](int st) {
+    if constexpr (FOREST) {
+      if (st == GAL_STATUS_SUCCESS) {
+        const int32_t slot = F.segSnap[seg];
+        if (slot >= 0) {
+#pragma unroll
+          for (int v = 0; v < GAL_NY; ++v) F.snapshots[v * F.nSnap + slot] = y[v];
+        }
+        stepIn = h;  // node%timeStepSet: carried to the next piece
+        if (++seg < segEnd) {
+          start_segment();
+          return;
+        }
+        complete_node(st);
+      } else {
+        restore_start();  // a failed call leaves the node as it started
+        complete_node(st);
+      }
+    } else {
+      if (st == GAL_STATUS_SUCCESS) {
+#pragma unroll
+        for (int v = 0; v < GAL_NY; ++v) b.state[v * n + node] = y[v];
+        b.step[node] = h;
+      }
+      b.status[node] = st;
+      if (b.counters) {
+        b.counters[node] = nAcc;
+        b.counters[n + node] = nRej;
+        b.counters[2 * n + node] = nRhs;
+      }
+      phase = PH_NEED;
+    }
+  };
+
   if constexpr (MODE == MODE_PLAIN) {
     // The FP64 parity form: every right-hand side inlined at its stage, the
     // stage arguments computed by the whole warp at once.
@@ -306,50 +500,20 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       if (need) {
         const int leader = __ffs(need) - 1;
         unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(b.queue, (unsigned long long)__popc(need));
+        if (lane == leader) base = atomicAdd(queueHead, (unsigned long long)__popc(need));
         base = __shfl_sync(FULL, base, leader);
-        if (phase == PH_NEED) {
-          node = (int64_t)(base + __popc(need & ((1u << lane) - 1u)));
-          if (node >= n) {
-            phase = PH_DONE;
-          } else {
-            double prm[GAL_NP];
-#pragma unroll
-            for (int v = 0; v < GAL_NP; ++v) prm[v] = b.param[v * n + node];
-            node_setup(G, sLnT, prm, c);
-            if constexpr (FAST) cf = node_fast(c);
-#pragma unroll
-            for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
-            scales(y, c.massHalo, s);
-            t0 = b.tStart[node];
-            t1 = b.tEnd[node];
-            stepIn = b.step[node];
-            trial = 0;
-            nAcc = nRej = nRhs = 0;
-            phase = PH_TRIAL;
-          }
-        }
+        if (phase == PH_NEED) take(base + __popc(need & ((1u << lane) - 1u)));
       }
       if (__all_sync(FULL, phase == PH_DONE)) break;
 
       // ---- start (or restart) an ODE trial: odeSolverSolve + driver reset
-      if (phase == PH_TRIAL && t0 == t1) {
-        b.step[node] = -1.0;  // node%timeStepSet(-1) when there is nothing to do
-        b.status[node] = GAL_STATUS_SUCCESS;
-        if (b.counters) {
-          b.counters[node] = 0; b.counters[n + node] = 0; b.counters[2 * n + node] = 0;
-        }
-        phase = PH_NEED;
-      }
+      if (phase == PH_TRIAL && t0 == t1) zero_interval();
       const bool starting = phase == PH_TRIAL;
       if (starting) {
         const double stepSize = G.p.reuse_step_size ? stepIn / (double)(1u << trial) : -1.0;
         h = t1 - t0;
         if (stepSize > 0.0) h = fmin(stepSize, h);
-        if (trial > 0) {
-#pragma unroll
-          for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
-        }
+        if (trial > 0) restore_start();
         sync_yr();
         t = t0;
         count = 0;
@@ -475,29 +639,17 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
           finalStatus = GAL_STATUS_XCPU;
         }
       }
-      if (finished) {
-        if (finalStatus == GAL_STATUS_SUCCESS) {
-#pragma unroll
-          for (int v = 0; v < GAL_NY; ++v) b.state[v * n + node] = y[v];
-          b.step[node] = h;
-        }
-        b.status[node] = finalStatus;
-        if (b.counters) {
-          b.counters[node] = nAcc;
-          b.counters[n + node] = nRej;
-          b.counters[2 * n + node] = nRhs;
-        }
-        phase = PH_NEED;
-      }
+      if (finished) finish(finalStatus);
     }
   } else {
-    // The main loop makes two kinds of right-hand-side evaluation, each from
-    // one call site, so that the right-hand side (and the network) is
-    // compiled twice rather than once per stage: f(y) for lanes that start a
-    // trial (dydt_in) or accepted a step in the previous pass (dydt_out), and
-    // the five stage slopes of an attempt, in a loop whose stage index is the
-    // same for every lane of the warp (lanes attempt steps together, so the
-    // FP64 error norm and step control run once per attempt for the warp).
+    // One right-hand-side call site per pass, in a loop over the stage
+    // index st = 0..5 that is the same for every lane of the warp: st = 0
+    // is f(y) for lanes that start a trial (dydt_in) or accepted a step in
+    // the previous pass (dydt_out, reused as the next dydt_in); st = 1..5
+    // are the stage slopes k2..k6 of an attempt.  Lanes attempt steps
+    // together, so the FP64 error norm and step control run once per
+    // attempt for the warp, and the right-hand side (with the network) is
+    // compiled once.
     bool needOut = false;
     for (;;) {
       // ---- refill lanes whose node has finished (warp-aggregated queue pop)
@@ -505,224 +657,203 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       if (need) {
         const int leader = __ffs(need) - 1;
         unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(b.queue, (unsigned long long)__popc(need));
+        if (lane == leader) base = atomicAdd(queueHead, (unsigned long long)__popc(need));
         base = __shfl_sync(FULL, base, leader);
-        if (phase == PH_NEED) {
-          node = (int64_t)(base + __popc(need & ((1u << lane) - 1u)));
-          if (node >= n) {
-            phase = PH_DONE;
-          } else {
-            double prm[GAL_NP];
-#pragma unroll
-            for (int v = 0; v < GAL_NP; ++v) prm[v] = b.param[v * n + node];
-            node_setup(G, sLnT, prm, c);
-            if constexpr (FAST) cf = node_fast(c);
-#pragma unroll
-            for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
-            scales(y, c.massHalo, s);
-            t0 = b.tStart[node];
-            t1 = b.tEnd[node];
-            stepIn = b.step[node];
-            trial = 0;
-            nAcc = nRej = nRhs = 0;
-            phase = PH_TRIAL;
-          }
-        }
+        if (phase == PH_NEED) take(base + __popc(need & ((1u << lane) - 1u)));
       }
       if (__all_sync(FULL, phase == PH_DONE)) break;
 
       // ---- start (or restart) an ODE trial: odeSolverSolve + driver reset
-      if (phase == PH_TRIAL && t0 == t1) {
-        b.step[node] = -1.0;  // node%timeStepSet(-1) when there is nothing to do
-        b.status[node] = GAL_STATUS_SUCCESS;
-        if (b.counters) {
-          b.counters[node] = 0; b.counters[n + node] = 0; b.counters[2 * n + node] = 0;
-        }
-        phase = PH_NEED;
-      }
+      if (phase == PH_TRIAL && t0 == t1) zero_interval();
       const bool starting = phase == PH_TRIAL;
       if (starting) {
         const double stepSize = G.p.reuse_step_size ? stepIn / (double)(1u << trial) : -1.0;
         h = t1 - t0;
         if (stepSize > 0.0) h = fmin(stepSize, h);
-        if (trial > 0) {
-#pragma unroll
-          for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
-        }
+        if (trial > 0) restore_start();
         sync_yr();
         t = t0;
         count = 0;
       }
-      // f(y): dydt_in of a trial's first step, or dydt_out at the point
-      // accepted in the previous pass (reused as the next dydt_in).
       const bool atY = starting || needOut;
-      if (any(atY)) eval(yr, k1, atY);
       bool finished = false;
       int finalStatus = GAL_STATUS_SUCCESS;
-      if (starting) {
-        ++nRhs;
-        phase = PH_STEP;
-      }
-      if (needOut) {
-        // The post-step clamps return GSL_Continue: dydt_out is kept.
-        needOut = false;
-        ++nRhs;
-        post_step(y);
-        sync_yr();
-        if (budget && count >= budget) {
-          finished = true;
-          finalStatus = GAL_STATUS_XCPU;
-        }
-      }
-
-      // ---- one attempted step (one pass of gsl_odeiv2_evolve_apply's try_step)
-      const bool stepping = phase == PH_STEP && !finished;
-      if (any(stepping)) {
-        const double dt = t1 - t;
-        const bool finalStep = (dt >= 0.0 && h > dt) || (dt < 0.0 && h < dt);
-        const double hh = finalStep ? dt : h;
-        const RateT hr = (RateT)hh;
+      bool stepping = false;
+      bool finalStep = false;
+      double hh = 0.0;
+      RateT hr = (RateT)0;
+      const bool anyY = any(atY);
 #pragma unroll 1
-        for (int st = 1; st <= 5; ++st) {
-          // Stage argument y + h sum_j b_ij k_j (in the rate precision); st is warp-uniform.
-          switch (st) {
-            case 1:
-#pragma unroll
-              for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + (RateT)ck::b21 * hr * k1[i];
-              break;
-            case 2:
-#pragma unroll
-              for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + hr * ((RateT)ck::b31 * k1[i] + (RateT)ck::b32 * k2[i]);
-              break;
-            case 3:
-#pragma unroll
-              for (int i = 0; i < GAL_NY; ++i)
-                x[i] = yr[i] + hr * ((RateT)ck::b41 * k1[i] + (RateT)ck::b42 * k2[i] + (RateT)ck::b43 * k3[i]);
-              break;
-            case 4:
-#pragma unroll
-              for (int i = 0; i < GAL_NY; ++i)
-                x[i] = yr[i] + hr * ((RateT)ck::b51 * k1[i] + (RateT)ck::b52 * k2[i] + (RateT)ck::b53 * k3[i] +
-                                     (RateT)ck::b54 * k4[i]);
-              break;
-            default:
-#pragma unroll
-              for (int i = 0; i < GAL_NY; ++i)
-                x[i] = yr[i] + hr * ((RateT)ck::b61 * k1[i] + (RateT)ck::b62 * k2[i] + (RateT)ck::b63 * k3[i] +
-                                     (RateT)ck::b64 * k4[i] + (RateT)ck::b65 * k5[i]);
-              break;
+      for (int st = anyY ? 0 : 1; st <= 5; ++st) {
+        if (st == 1) {
+          // ---- the slopes at y are in: begin one attempted step (a pass of
+          // gsl_odeiv2_evolve_apply's try_step) for every lane that steps.
+          if (starting) {
+            ++nRhs;
+            phase = PH_STEP;
           }
-          RateT d[GAL_NY];
-          eval(x, d, stepping);
-          switch (st) {
-            case 1:
-#pragma unroll
-              for (int i = 0; i < GAL_NY; ++i) k2[i] = d[i];
-              break;
-            case 2:
-#pragma unroll
-              for (int i = 0; i < GAL_NY; ++i) k3[i] = d[i];
-              break;
-            case 3:
-#pragma unroll
-              for (int i = 0; i < GAL_NY; ++i) k4[i] = d[i];
-              break;
-            case 4:
-#pragma unroll
-              for (int i = 0; i < GAL_NY; ++i) k5[i] = d[i];
-              break;
-            default:
-#pragma unroll
-              for (int i = 0; i < GAL_NY; ++i) k6[i] = d[i];
-              break;
-          }
-        }
-        if (stepping) {
-          nRhs += 5;
-          // 5th-order solution, scaled error ratio (sc2_control_hadjust, a_y=1, a_dydt=0), FP64.
-          // The largest |err_i|/D_i is found by cross-multiplication and divided
-          // once (max of the quotients = quotient of the maximal pair).
-          double errMax = 0.0, dMax = 1.0;
-#pragma unroll
-          for (int i = 0; i < GAL_NY; ++i) {
-            const RateT inc = (RateT)ck::c1 * k1[i] + (RateT)ck::c3 * k3[i] + (RateT)ck::c4 * k4[i] + (RateT)ck::c6 * k6[i];
-            const RateT est = (RateT)ck::e1 * k1[i] + (RateT)ck::e3 * k3[i] + (RateT)ck::e4 * k4[i] + (RateT)ck::e5 * k5[i] +
-                              (RateT)ck::e6 * k6[i];
-            ynew[i] = y[i] + hh * (double)inc;
-            const double err = fabs(hh * (double)est);
-            const double D0 = fabs(epsRel * fabs(ynew[i]) + epsAbs * s[i]);
-            if (err * dMax > errMax * D0 || !(err == err)) {
-              errMax = err;
-              dMax = D0;
-            }
-          }
-          const double rmax = dmax(fast_div(errMax, dMax), 2.2250738585072014e-308);  // floor DBL_MIN as cscal2.c
-          ++count;
-          const double tNew = finalStep ? t1 : t + hh;
-          double hNew = hh;
-          bool decrease = false;
-          // 0.9 rmax^(-1/5), floored at 0.2 (reached for rmax >= 4.5^5 exactly),
-          // and 0.9 rmax^(-1/6) capped at 4.9 (reached below (0.9/4.9)^6).
-          if (rmax > 1.1) {
-            double r = rmax > 1845.28125 ? 0.2 : 0.9 * inv_root<5>(rmax);
-            if (r < 0.2) r = 0.2;
-            hNew = r * hh;
-            decrease = true;
-          } else if (rmax < 0.5) {
-            double r = rmax < 3.8394e-5 ? 4.9 : 0.9 * inv_root<6>(rmax);
-            if (r > 4.9) r = 4.9;
-            if (r < 1.0) r = 1.0;
-            hNew = r * hh;
-          }
-          if (decrease) {
-            const double tNext = tNew + hNew;
-            if (fabs(hNew) < fabs(hh) && tNext != tNew) {
-              h = hNew;  // reject: retry from the same (t, y) with the smaller step
-              ++nRej;
-              if (budget && count >= budget) { finished = true; finalStatus = GAL_STATUS_XCPU; }
-            } else {
-              // The step cannot shrink any further: this trial fails
-              // (GSL_FAILURE); the node evolver restarts with half the step.
-              ++trial;
-              if (trial >= G.p.trial_count_maximum) { finished = true; finalStatus = GAL_STATUS_UNDERFLOW; }
-              else phase = PH_TRIAL;
-            }
-          } else {
-            // Accept.
-#pragma unroll
-            for (int i = 0; i < GAL_NY; ++i) y[i] = ynew[i];
+          if (needOut) {
+            // The post-step clamps return GSL_Continue: dydt_out is kept.
+            needOut = false;
+            ++nRhs;
+            post_step(y);
             sync_yr();
-            t = tNew;
-            h = hNew;
-            ++nAcc;
-            const bool reached = !(t1 - t > 0.0 || t1 - t < 0.0);
-            if (reached) {
-              post_step(y);
+            if (budget && count >= budget) {
               finished = true;
-              bool finite = true;
-#pragma unroll
-              for (int i = 0; i < GAL_NY; ++i) finite = finite && isfinite(y[i]);
-              finalStatus = finite ? GAL_STATUS_SUCCESS : GAL_STATUS_NOT_FINITE;
-            } else {
-              needOut = true;
+              finalStatus = GAL_STATUS_XCPU;
             }
+          }
+          stepping = phase == PH_STEP && !finished;
+          if (!any(stepping)) break;
+          const double dt = t1 - t;
+          finalStep = (dt >= 0.0 && h > dt) || (dt < 0.0 && h < dt);
+          hh = finalStep ? dt : h;
+          hr = (RateT)hh;
+        }
+        // Argument of this evaluation: y, or y + h sum_j b_ij k_j (in the rate precision).
+        switch (st) {
+          case 0:
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i];
+            break;
+          case 1:
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + (RateT)ck::b21 * hr * k1[i];
+            break;
+          case 2:
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + hr * ((RateT)ck::b31 * k1[i] + (RateT)ck::b32 * k2[i]);
+            break;
+          case 3:
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i)
+              x[i] = yr[i] + hr * ((RateT)ck::b41 * k1[i] + (RateT)ck::b42 * k2[i] + (RateT)ck::b43 * k3[i]);
+            break;
+          case 4:
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i)
+              x[i] = yr[i] + hr * ((RateT)ck::b51 * k1[i] + (RateT)ck::b52 * k2[i] + (RateT)ck::b53 * k3[i] +
+                                   (RateT)ck::b54 * k4[i]);
+            break;
+          default:
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i)
+              x[i] = yr[i] + hr * ((RateT)ck::b61 * k1[i] + (RateT)ck::b62 * k2[i] + (RateT)ck::b63 * k3[i] +
+                                   (RateT)ck::b64 * k4[i] + (RateT)ck::b65 * k5[i]);
+            break;
+        }
+        RateT d[GAL_NY];
+        eval(x, d, st == 0 ? atY : stepping);
+        switch (st) {
+          case 0:
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) if (atY) k1[i] = d[i];
+            break;
+          case 1:
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) k2[i] = d[i];
+            break;
+          case 2:
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) k3[i] = d[i];
+            break;
+          case 3:
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) k4[i] = d[i];
+            break;
+          case 4:
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) k5[i] = d[i];
+            break;
+          default:
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) k6[i] = d[i];
+            break;
+        }
+      }
+      if (stepping) {
+        nRhs += 5;
+        // 5th-order solution (FP64) and the scaled error ratio of
+        // sc2_control_hadjust (a_y=1, a_dydt=0).  The component with the
+        // largest |err_i|/D_i is picked by cross-multiplied FP32 comparisons;
+        // the ratio of the picked component is then formed in FP64 from the
+        // FP64 error and the FP64 D_i.  (Picking at FP32 precision can only
+        // exchange two components whose ratios agree to ~1e-7.)
+        float errMaxF = 0.0f, dMaxF = 1.0f;
+        RateT estSel = (RateT)0;
+        double ySel = 0.0, sSel = 1.0;
+#pragma unroll
+        for (int i = 0; i < GAL_NY; ++i) {
+          const RateT inc = (RateT)ck::c1 * k1[i] + (RateT)ck::c3 * k3[i] + (RateT)ck::c4 * k4[i] + (RateT)ck::c6 * k6[i];
+          const RateT est = (RateT)ck::e1 * k1[i] + (RateT)ck::e3 * k3[i] + (RateT)ck::e4 * k4[i] + (RateT)ck::e5 * k5[i] +
+                            (RateT)ck::e6 * k6[i];
+          ynew[i] = y[i] + hh * (double)inc;
+          const float errF = fabsf((float)hr * (float)est);
+          const float dF = fabsf((float)epsRel * fabsf((float)ynew[i]) + (float)epsAbs * (float)s[i]);
+          if (errF * dMaxF > errMaxF * dF || !(errF == errF)) {
+            errMaxF = errF;
+            dMaxF = dF;
+            estSel = est;
+            ySel = ynew[i];
+            sSel = s[i];
+          }
+        }
+        // With nothing picked (every error zero) the ratio is 0, as in FP64.
+        const double errMax = fabs(hh * (double)estSel);
+        const double dMax = fabs(epsRel * fabs(ySel) + epsAbs * sSel);
+        const double rmax = dmax(fast_div(errMax, dMax), 2.2250738585072014e-308);  // floor DBL_MIN as cscal2.c
+        ++count;
+        const double tNew = finalStep ? t1 : t + hh;
+        double hNew = hh;
+        bool decrease = false;
+        // 0.9 rmax^(-1/5), floored at 0.2 (reached for rmax >= 4.5^5 exactly),
+        // and 0.9 rmax^(-1/6) capped at 4.9 (reached below (0.9/4.9)^6).
+        if (rmax > 1.1) {
+          double r = rmax > 1845.28125 ? 0.2 : 0.9 * inv_root<5>(rmax);
+          if (r < 0.2) r = 0.2;
+          hNew = r * hh;
+          decrease = true;
+        } else if (rmax < 0.5) {
+          double r = rmax < 3.8394e-5 ? 4.9 : 0.9 * inv_root<6>(rmax);
+          if (r > 4.9) r = 4.9;
+          if (r < 1.0) r = 1.0;
+          hNew = r * hh;
+        }
+        if (decrease) {
+          const double tNext = tNew + hNew;
+          if (fabs(hNew) < fabs(hh) && tNext != tNew) {
+            h = hNew;  // reject: retry from the same (t, y) with the smaller step
+            ++nRej;
+            if (budget && count >= budget) { finished = true; finalStatus = GAL_STATUS_XCPU; }
+          } else {
+            // The step cannot shrink any further: this trial fails
+            // (GSL_FAILURE); the node evolver restarts with half the step.
+            ++trial;
+            if (trial >= G.p.trial_count_maximum) { finished = true; finalStatus = GAL_STATUS_UNDERFLOW; }
+            else phase = PH_TRIAL;
+          }
+        } else {
+          // Accept.
+#pragma unroll
+          for (int i = 0; i < GAL_NY; ++i) y[i] = ynew[i];
+          sync_yr();
+          t = tNew;
+          h = hNew;
+          ++nAcc;
+          const bool reached = !(t1 - t > 0.0 || t1 - t < 0.0);
+          if (reached) {
+            post_step(y);
+            finished = true;
+            bool finite = true;
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) finite = finite && isfinite(y[i]);
+            finalStatus = finite ? GAL_STATUS_SUCCESS : GAL_STATUS_NOT_FINITE;
+          } else {
+            needOut = true;
           }
         }
       }
-      if (finished) {
-        if (finalStatus == GAL_STATUS_SUCCESS) {
-#pragma unroll
-          for (int v = 0; v < GAL_NY; ++v) b.state[v * n + node] = y[v];
-          b.step[node] = h;
-        }
-        b.status[node] = finalStatus;
-        if (b.counters) {
-          b.counters[node] = nAcc;
-          b.counters[n + node] = nRej;
-          b.counters[2 * n + node] = nRhs;
-        }
-        phase = PH_NEED;
-      }
+      if (finished) finish(finalStatus);
     }
   }
   if (SURR && sd.stats) {
@@ -744,16 +875,18 @@ struct LaunchArgs {
   Batch b;
   DeviceTables tables;
   SurrogateDev sd;
+  ForestDev forest;
   size_t shm;
   int64_t blocks;
   cudaStream_t stream;
 };
 
-template <int THREADS, int MODE>
+template <int THREADS, int MODE, bool FOREST = false>
 cudaError_t launch_evolve(const LaunchArgs& a) {
-  cudaError_t e = cudaFuncSetAttribute(evolve_kernel<THREADS, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a.shm);
+  cudaError_t e =
+      cudaFuncSetAttribute(evolve_kernel<THREADS, MODE, FOREST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a.shm);
   if (e != cudaSuccess) return e;
-  evolve_kernel<THREADS, MODE><<<(unsigned)a.blocks, THREADS, a.shm, a.stream>>>(a.G, a.b, a.tables, a.sd);
+  evolve_kernel<THREADS, MODE, FOREST><<<(unsigned)a.blocks, THREADS, a.shm, a.stream>>>(a.G, a.b, a.tables, a.sd, a.forest);
   return cudaGetLastError();
 }
 
@@ -764,6 +897,9 @@ cudaError_t evolve_launch_plain(int threads, const LaunchArgs& a);
 cudaError_t evolve_launch_surrogate(int threads, const LaunchArgs& a);
 cudaError_t evolve_launch_fast(int threads, const LaunchArgs& a);
 cudaError_t evolve_launch_fast_surrogate(int threads, const LaunchArgs& a);
+// Forest forms (evolve_forest_*.cu); cudaErrorInvalidConfiguration for a
+// form or block size not built.
+cudaError_t evolve_launch_forest(int mode, int threads, const LaunchArgs& a);
 
 inline cudaError_t evolve_launch(int mode, int threads, const LaunchArgs& a) {
   switch (mode) {

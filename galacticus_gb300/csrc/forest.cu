@@ -1,0 +1,404 @@
+// forest.cu -- whole-forest evolution on the GPU (include/galnode_forest.h).
+//
+// The tree evolver of the reference walks each tree node by node: a node is
+// evolved from its own time to its parent's, the evolve calls being cut at
+// the output times, and on reaching its parent it is promoted (the primary
+// progenitor) or merged (merger_trees/evolver/standard.F90:762-1035,
+// threaded.F90:418-840).  Here a forest is uploaded once -- its topology, the
+// dependency counter of every node, and a segment table with the halo
+// constants of every evolve call -- and each evolution is one CUDA graph:
+// reset the counters and the leaf queue, then one persistent kernel
+// (evolve_kernel with FOREST = true) in which the last progenitor of each
+// node to finish merges the progenitors and carries on with the node.  No
+// lane ever waits on another.
+//
+// The segment constants are computed on the host in FP64 without
+// contraction (the file is compiled with -ffp-contract=off), from the
+// analytic flat matter + Lambda time-redshift relation and the Bryan &
+// Norman (1998) virial contrast relative to the mean density
+// (structure_formation/virial_density_contrast/Bryan_Norman.F90:172-196).
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+#include <algorithm>
+
+#include "../../include/galnode_forest.h"
+#include "context.h"
+
+using namespace gal::host;
+
+namespace {
+
+constexpr double kMpc = 1.0e6 * 3.08567758135e16;
+constexpr double kGyr = 1.0e9 * 3.15581497635456e7;
+constexpr double kG = 6.673e-11 * 1.98892e30 / 1.0e6 / kMpc;  // km^2 s^-2 Mpc / Msun
+
+struct HostCosmology {
+  double om, ol, h0;
+  double redshift(double t) const {
+    const double hubbleGyr = h0 / (kMpc / 1.0e3 / kGyr);
+    const double x = std::sinh(1.5 * hubbleGyr * std::sqrt(ol) * t);
+    return 1.0 / std::pow(x / std::sqrt(ol / om), 2.0 / 3.0) - 1.0;
+  }
+  void virial(double M, double z, double& r, double& v) const {
+    const double zp = (1.0 + z) * (1.0 + z) * (1.0 + z);
+    const double omz = om * zp / (om * zp + ol);
+    const double x = omz - 1.0;
+    const double contrast = (18.0 * M_PI * M_PI + 82.0 * x - 39.0 * x * x) / (x + 1.0);
+    const double rhoMean = om * 3.0 * h0 * h0 / (8.0 * M_PI * kG) * zp;
+    r = std::cbrt(3.0 * M / (4.0 * M_PI * contrast * rhoMean));
+    v = std::sqrt(kG * M / r);
+  }
+};
+
+template <class T>
+cudaError_t upload(T** dst, const std::vector<T>& src) {
+  *dst = nullptr;
+  if (src.empty()) return cudaSuccess;
+  cudaError_t e = cudaMalloc((void**)dst, src.size() * sizeof(T));
+  if (e == cudaSuccess) e = cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+  return e;
+}
+
+}  // namespace
+
+struct gal_forest_dev {
+  int64_t n = 0, nLeaves = 0, nSeg = 0, nSnap = 0;
+  // device arrays
+  int32_t *dLeaves = nullptr, *dParent = nullptr, *dChildFirst = nullptr, *dChildCount = nullptr;
+  int32_t *dPending = nullptr, *dPending0 = nullptr, *dSegFirst = nullptr, *dSegCount = nullptr, *dSnapInitial = nullptr;
+  int32_t* dSegSnap = nullptr;
+  double *dSegParam = nullptr, *dSegT0 = nullptr, *dSegT1 = nullptr;
+  double *dState0 = nullptr, *dState = nullptr, *dStepOut = nullptr, *dSnap = nullptr;
+  int32_t* dStatus = nullptr;
+  uint32_t* dCounters = nullptr;
+  unsigned long long* dHead = nullptr;
+  // host copies of the snapshot labels
+  std::vector<int32_t> snapNode, snapOutput;
+  // the captured evolution and the form/shape it was captured for
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int graphMode = -1, graphThreads = 0, graphBlocks = 0;
+  cudaEvent_t done = nullptr;
+};
+
+namespace {
+
+void release(gal_forest_dev* f) {
+  if (!f) return;
+  if (f->exec) cudaGraphExecDestroy(f->exec);
+  if (f->graph) cudaGraphDestroy(f->graph);
+  if (f->done) cudaEventDestroy(f->done);
+  void* ptrs[] = {f->dLeaves, f->dParent, f->dChildFirst, f->dChildCount, f->dPending, f->dPending0, f->dSegFirst,
+                  f->dSegCount, f->dSnapInitial, f->dSegSnap, f->dSegParam, f->dSegT0, f->dSegT1, f->dState0,
+                  f->dState, f->dStepOut, f->dSnap, f->dStatus, f->dCounters, f->dHead};
+  for (void* p : ptrs) cudaFree(p);
+  delete f;
+}
+
+// The launch arguments of one forest evolution in the context's current form and shape.
+LaunchArgs forest_args(gal_ctx* ctx, gal_forest_dev* f, int mode, int threads, int blocksPerSm) {
+  LaunchArgs a{};
+  a.G = ctx->globals;
+  a.tables = DeviceTables{ctx->dTab, ctx->dLnT, ctx->dLnZ, ctx->dFastLog, ctx->dFastExp, ctx->dTabF, ctx->dLnZF};
+  if (mode & MODE_SURROGATE)
+    a.sd = SurrogateDev{ctx->dSurrSmall, ctx->dSurrPlanes, ctx->dSurrMap, ctx->surrInfo, ctx->dSurrStats};
+  ForestDev& F = a.forest;
+  F.n = f->n;
+  F.nLeaves = f->nLeaves;
+  F.leaves = f->dLeaves;
+  F.parent = f->dParent;
+  F.childFirst = f->dChildFirst;
+  F.childCount = f->dChildCount;
+  F.pending = f->dPending;
+  F.segFirst = f->dSegFirst;
+  F.segCount = f->dSegCount;
+  F.snapInitial = f->dSnapInitial;
+  F.nSeg = f->nSeg;
+  F.segParam = f->dSegParam;
+  F.segT0 = f->dSegT0;
+  F.segT1 = f->dSegT1;
+  F.segSnap = f->dSegSnap;
+  F.state0 = f->dState0;
+  F.state = f->dState;
+  F.stepOut = f->dStepOut;
+  F.nSnap = f->nSnap;
+  F.snapshots = f->dSnap;
+  F.status = f->dStatus;
+  F.counters = f->dCounters;
+  F.head = f->dHead;
+  a.shm = ctx_shared_bytes(ctx, mode);
+  const int64_t lanes = (f->nLeaves + 31) / 32 * 32;
+  a.blocks = std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->smCount * blocksPerSm, (lanes + threads - 1) / threads));
+  a.stream = ctx->stream;
+  return a;
+}
+
+// (Re)capture the evolution graph when the form or the launch shape changed.
+int ensure_graph(gal_ctx* ctx, gal_forest_dev* f) {
+  const int mode = ctx_mode(ctx);
+  int threads, blocksPerSm;
+  effective_shape(ctx, mode, threads, blocksPerSm);
+  if (f->exec && f->graphMode == mode && f->graphThreads == threads && f->graphBlocks == blocksPerSm) return GAL_OK;
+  if (f->exec) cudaGraphExecDestroy(f->exec);
+  if (f->graph) cudaGraphDestroy(f->graph);
+  f->exec = nullptr;
+  f->graph = nullptr;
+  const LaunchArgs a = forest_args(ctx, f, mode, threads, blocksPerSm);
+  cudaStream_t st = ctx->stream;
+  // The kernel attribute (dynamic shared memory) is set by an empty-forest
+  // launch outside the capture: with no leaves every block returns at once.
+  LaunchArgs warm = a;
+  warm.forest.nLeaves = 0;
+  warm.blocks = 1;
+  cudaError_t e = cudaMemsetAsync(f->dHead, 0, sizeof(unsigned long long), st);
+  if (e == cudaSuccess) e = evolve_launch_forest(mode, threads, warm);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(ctx, GAL_ERR_CUDA, "forest kernel set-up failed: %s", cudaGetErrorString(e));
+  e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    cudaError_t e1 = cudaMemcpyAsync(f->dPending, f->dPending0, f->n * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+    if (e1 == cudaSuccess) e1 = cudaMemsetAsync(f->dHead, 0, sizeof(unsigned long long), st);
+    if (e1 == cudaSuccess) e1 = evolve_launch_forest(mode, threads, a);
+    cudaError_t e2 = cudaStreamEndCapture(st, &f->graph);
+    e = e1 != cudaSuccess ? e1 : e2;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&f->exec, f->graph, 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, GAL_ERR_CUDA, "forest graph capture failed: %s", cudaGetErrorString(e));
+  }
+  f->graphMode = mode;
+  f->graphThreads = threads;
+  f->graphBlocks = blocksPerSm;
+  return GAL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const int32_t* childFirst,
+                          const int32_t* childCount, const double* time, const double* mass, const double* spin,
+                          const double* state0, int32_t nOut, const double* tOut, gal_forest_dev** out) {
+  if (!out) return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: out is NULL%s");
+  *out = nullptr;
+  if (!ctx) return fail(nullptr, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: NULL context%s");
+  if (n < 1 || n > (int64_t)INT32_MAX || !parent || !childFirst || !childCount || !time || !mass || !spin || !state0 ||
+      nOut < 0 || (nOut > 0 && !tOut))
+    return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: bad arguments%s");
+  for (int32_t k = 1; k < nOut; ++k)
+    if (!(tOut[k] > tOut[k - 1])) return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: output times must increase%s");
+  // Topology checks: parents in range and later, progenitors contiguous.
+  for (int64_t i = 0; i < n; ++i) {
+    const int32_t p = parent[i];
+    if (p >= n || p < -1 || (p >= 0 && !(time[p] > time[i])) || childCount[i] < 0 ||
+        (childCount[i] > 0 && (childFirst[i] < 0 || (int64_t)childFirst[i] + childCount[i] > n)))
+      return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: inconsistent forest topology%s");
+    for (int32_t c = 0; c < childCount[i]; ++c)
+      if (parent[childFirst[i] + c] != (int32_t)i)
+        return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: progenitors must be contiguous%s");
+  }
+  const gal_params& p = ctx->params;
+  const HostCosmology cos{p.omega_matter, p.omega_dark_energy, p.hubble_constant};
+  std::vector<int32_t> leaves, pending0(n), segFirst(n), segCount(n), snapInitial(n, -1), segSnap;
+  std::vector<double> segParam[GAL_NP], segT0, segT1;
+  gal_forest_dev* f = new (std::nothrow) gal_forest_dev();
+  if (!f) return fail(ctx, GAL_ERR_ARGUMENT, "out of host memory%s");
+  f->n = n;
+  int32_t slot = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    pending0[i] = childCount[i];
+    if (childCount[i] == 0) leaves.push_back((int32_t)i);
+    const int32_t par = parent[i];
+    const double t0 = time[i], t1 = par >= 0 ? time[par] : time[i];
+    const bool primary = par >= 0 && childFirst[par] == (int32_t)i;
+    double massEnd = mass[i], accretion = 0.0;
+    if (primary && t1 > t0) {
+      massEnd = mass[par];
+      double brought = 0.0;
+      for (int32_t c = 0; c < childCount[par]; ++c) brought += mass[childFirst[par] + c];
+      accretion = std::max(mass[par] - brought, 0.0) / (t1 - t0);
+    }
+    // Snapshot slots: outputs at the node's own time, then inside its interval.
+    for (int32_t k = 0; k < nOut; ++k)
+      if (tOut[k] == t0 && (par < 0 || t0 < t1)) {
+        snapInitial[i] = slot++;
+        f->snapNode.push_back((int32_t)i);
+        f->snapOutput.push_back(k);
+      }
+    segFirst[i] = (int32_t)segT0.size();
+    double a = t0;
+    int32_t k = 0;
+    while (k < nOut && !(tOut[k] > t0)) ++k;
+    while (a < t1) {
+      const bool atOutput = k < nOut && tOut[k] < t1;
+      const double b = atOutput ? tOut[k] : t1;
+      const double M = mass[i] + (massEnd - mass[i]) * (a - t0) / (t1 - t0);
+      double r, v;
+      cos.virial(M, cos.redshift(a), r, v);
+      segParam[GAL_P_MASS].push_back(M);
+      segParam[GAL_P_MASS_RATE].push_back(accretion);
+      segParam[GAL_P_RADIUS_VIRIAL].push_back(r);
+      segParam[GAL_P_VELOCITY_VIRIAL].push_back(v);
+      segParam[GAL_P_SPIN].push_back(spin[i]);
+      segT0.push_back(a);
+      segT1.push_back(b);
+      if (atOutput) {
+        segSnap.push_back(slot++);
+        f->snapNode.push_back((int32_t)i);
+        f->snapOutput.push_back(k);
+        ++k;
+      } else {
+        segSnap.push_back(-1);
+      }
+      a = b;
+    }
+    segCount[i] = (int32_t)segT0.size() - segFirst[i];
+  }
+  f->nLeaves = (int64_t)leaves.size();
+  f->nSeg = (int64_t)segT0.size();
+  f->nSnap = slot;
+  std::vector<double> segParamFlat((size_t)GAL_NP * f->nSeg);
+  for (int v = 0; v < GAL_NP; ++v) std::copy(segParam[v].begin(), segParam[v].end(), segParamFlat.begin() + v * f->nSeg);
+  std::vector<double> st0((size_t)GAL_NY * n);
+  std::memcpy(st0.data(), state0, st0.size() * sizeof(double));
+  cudaError_t e = cudaSetDevice(ctx->device);
+  std::vector<int32_t> par(parent, parent + n), cf(childFirst, childFirst + n), cc(childCount, childCount + n);
+  if (e == cudaSuccess) e = upload(&f->dLeaves, leaves);
+  if (e == cudaSuccess) e = upload(&f->dParent, par);
+  if (e == cudaSuccess) e = upload(&f->dChildFirst, cf);
+  if (e == cudaSuccess) e = upload(&f->dChildCount, cc);
+  if (e == cudaSuccess) e = upload(&f->dPending0, pending0);
+  if (e == cudaSuccess) e = upload(&f->dPending, pending0);
+  if (e == cudaSuccess) e = upload(&f->dSegFirst, segFirst);
+  if (e == cudaSuccess) e = upload(&f->dSegCount, segCount);
+  if (e == cudaSuccess) e = upload(&f->dSnapInitial, snapInitial);
+  if (e == cudaSuccess) e = upload(&f->dSegSnap, segSnap);
+  if (e == cudaSuccess) e = upload(&f->dSegParam, segParamFlat);
+  if (e == cudaSuccess) e = upload(&f->dSegT0, segT0);
+  if (e == cudaSuccess) e = upload(&f->dSegT1, segT1);
+  if (e == cudaSuccess) e = upload(&f->dState0, st0);
+  if (e == cudaSuccess) e = cudaMalloc(&f->dState, (size_t)GAL_NY * n * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&f->dStepOut, (size_t)n * sizeof(double));
+  if (e == cudaSuccess && f->nSnap > 0) e = cudaMalloc(&f->dSnap, (size_t)GAL_NY * f->nSnap * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&f->dStatus, (size_t)n * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&f->dCounters, (size_t)3 * n * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&f->dHead, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f->done, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    release(f);
+    return fail(ctx, GAL_ERR_CUDA, "gal_gpu_forest_create: device allocation or upload failed: %s", cudaGetErrorString(e));
+  }
+  *out = f;
+  return GAL_OK;
+}
+
+int gal_gpu_forest_evolve(gal_ctx* ctx, gal_forest_dev* f) {
+  if (!ctx || !f) return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_evolve: NULL argument%s");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return fail(ctx, GAL_ERR_CUDA, "CUDA error: %s", cudaGetErrorString(e));
+  int rc = ensure_graph(ctx, f);
+  if (rc) return rc;
+  e = cudaGraphLaunch(f->exec, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(f->done, ctx->stream);
+  if (e != cudaSuccess) return fail(ctx, GAL_ERR_CUDA, "forest graph launch failed: %s", cudaGetErrorString(e));
+  ++ctx->launches;
+  return GAL_OK;
+}
+
+int gal_gpu_forest_sync(gal_ctx* ctx, gal_forest_dev* f) {
+  if (!ctx || !f) return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_sync: NULL argument%s");
+  const cudaError_t e = cudaEventSynchronize(f->done);
+  if (e != cudaSuccess) return fail(ctx, GAL_ERR_CUDA, "forest evolution failed: %s", cudaGetErrorString(e));
+  return GAL_OK;
+}
+
+int64_t gal_gpu_forest_snapshot_count(const gal_forest_dev* f) { return f ? f->nSnap : -1; }
+
+int gal_gpu_forest_results(gal_ctx* ctx, gal_forest_dev* f, double* state, int32_t* status, uint32_t* counters,
+                           double* snapshot, int32_t* snapNode, int32_t* snapOutput) {
+  if (!ctx || !f) return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_results: NULL argument%s");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  const int64_t n = f->n;
+  if (e == cudaSuccess && state) e = cudaMemcpy(state, f->dState, (size_t)GAL_NY * n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && status) e = cudaMemcpy(status, f->dStatus, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && counters)
+    e = cudaMemcpy(counters, f->dCounters, (size_t)3 * n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && snapshot && f->nSnap > 0)
+    e = cudaMemcpy(snapshot, f->dSnap, (size_t)GAL_NY * f->nSnap * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail(ctx, GAL_ERR_CUDA, "gal_gpu_forest_results: %s", cudaGetErrorString(e));
+  if (snapNode && f->nSnap > 0) std::memcpy(snapNode, f->snapNode.data(), f->nSnap * sizeof(int32_t));
+  if (snapOutput && f->nSnap > 0) std::memcpy(snapOutput, f->snapOutput.data(), f->nSnap * sizeof(int32_t));
+  return GAL_OK;
+}
+
+int64_t gal_gpu_forest_accepted_steps(gal_ctx* ctx, gal_forest_dev* f) {
+  if (!ctx || !f) return -1;
+  std::vector<uint32_t> acc((size_t)f->n);
+  if (cudaSetDevice(ctx->device) != cudaSuccess || cudaStreamSynchronize(ctx->stream) != cudaSuccess ||
+      cudaMemcpy(acc.data(), f->dCounters, acc.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -1;
+  int64_t total = 0;
+  for (uint32_t a : acc) total += a;
+  return total;
+}
+
+int gal_gpu_forest_autotune(gal_ctx* ctx, gal_forest_dev* f, int32_t repeats, double* timesMs) {
+  if (!ctx || !f || repeats < 1) return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_autotune: bad arguments%s");
+  static const int shapes[6][2] = {{64, 1}, {128, 1}, {128, 2}, {256, 1}, {256, 2}, {512, 1}};
+  const int mode = ctx_mode(ctx);
+  const int keepThreads = ctx->threads, keepBlocks = ctx->blocksPerSm;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return fail(ctx, GAL_ERR_CUDA, "gal_gpu_forest_autotune: event creation failed%s");
+  double best = 1e300;
+  int bestI = -1;
+  int rc = GAL_OK;
+  for (int i = 0; i < 6 && rc == GAL_OK; ++i) {
+    if (timesMs) timesMs[i] = -1.0;
+    const int t = shapes[i][0], b = shapes[i][1];
+    if (!mode_has_threads(mode, t) || (size_t)b * ctx_shared_bytes(ctx, mode) > 228 * 1024) continue;
+    ctx->threads = t;
+    ctx->blocksPerSm = b;
+    rc = gal_gpu_forest_evolve(ctx, f);  // warm-up (and graph capture)
+    if (rc) break;
+    cudaEventRecord(e0, ctx->stream);
+    for (int r = 0; r < repeats && rc == GAL_OK; ++r) rc = gal_gpu_forest_evolve(ctx, f);
+    cudaEventRecord(e1, ctx->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = fail(ctx, GAL_ERR_CUDA, "gal_gpu_forest_autotune: evolution failed%s");
+      break;
+    }
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double mean = ms / repeats;
+    if (timesMs) timesMs[i] = mean;
+    if (mean < best) {
+      best = mean;
+      bestI = i;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (bestI >= 0) {
+    ctx->threads = shapes[bestI][0];
+    ctx->blocksPerSm = shapes[bestI][1];
+  } else {
+    ctx->threads = keepThreads;
+    ctx->blocksPerSm = keepBlocks;
+  }
+  return rc;
+}
+
+void gal_gpu_forest_free(gal_forest_dev* f) {
+  if (!f) return;
+  if (f->done) cudaEventSynchronize(f->done);  // the last evolution has finished with the arrays
+  release(f);
+}
+
+}  // extern "C"

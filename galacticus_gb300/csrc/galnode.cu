@@ -17,6 +17,7 @@
 #include "../../include/galnode.h"
 #include "../../include/galnode_surrogate.h"
 #include "evolve_kernel.cuh"
+#include "context.h"
 
 namespace gal {
 
@@ -40,41 +41,16 @@ const double* host_fast_exp_table() { return host_fast_tables().exp2; }
 // ===========================================================================
 using namespace gal;
 
-struct gal_ctx {
-  gal_params params;
-  Globals globals;
-  int device = 0;
-  int smCount = 0;
-  cudaStream_t stream = nullptr;
-  double2* dTab = nullptr;
-  double* dLnT = nullptr;
-  double* dLnZ = nullptr;
-  double2* dFastLog = nullptr;           // tables of the short FP64 log/exp
-  double* dFastExp = nullptr;
-  float2* dTabF = nullptr;               // FP32 copies of the tables (FP32-rate forms)
-  float* dLnZF = nullptr;
-  unsigned long long* dQueue = nullptr;  // work-queue head
-  void* dBuf = nullptr;                  // staging for the host-pointer API
-  // Installed cooling-function surrogate (dSurrSmall == nullptr: none).
-  float* dSurrSmall = nullptr;
-  __nv_bfloat16* dSurrPlanes = nullptr;
-  uint8_t* dSurrMap = nullptr;
-  unsigned long long* dSurrStats = nullptr;
-  SurrogateInfo surrInfo{};
-  size_t bufBytes = 0;
-  int threads = 128;
-  int blocksPerSm = 1;
-  int ratePrecision = GAL_RATES_FP64;
-  int64_t launches = 0;
-  int lastError = 0;
-  char message[512] = {0};
-};
-
 namespace {
 thread_local int gLibError = 0;
 thread_local char gLibMessage[512] = {0};
 
-int fail(gal_ctx* ctx, int code, const char* fmt, const char* detail = "") {
+}  // namespace
+
+namespace gal {
+namespace host {
+
+int fail(gal_ctx* ctx, int code, const char* fmt, const char* detail) {
   char buf[512];
   snprintf(buf, sizeof buf, fmt, detail);
   if (ctx) {
@@ -86,6 +62,12 @@ int fail(gal_ctx* ctx, int code, const char* fmt, const char* detail = "") {
   }
   return code;
 }
+
+}  // namespace host
+}  // namespace gal
+using namespace gal::host;
+
+namespace {
 
 #define CUDA_TRY(ctx, call)                                                  \
   do {                                                                       \
@@ -111,6 +93,11 @@ void set_uniform_metallicity_grid(Globals& g, const double* lnZ, int nZ) {
   g.invDlnZ = 1.0 / d;
   g.zUniform = 1;
 }
+
+}  // namespace
+
+namespace gal {
+namespace host {
 
 int ctx_mode(const gal_ctx* ctx) {
   return (ctx->ratePrecision == GAL_RATES_FP32 ? MODE_FAST : 0) | (ctx->dSurrSmall ? MODE_SURROGATE : 0);
@@ -138,6 +125,11 @@ void effective_shape(const gal_ctx* ctx, int mode, int& threads, int& blocksPerS
   blocksPerSm = ctx->blocksPerSm;
   while (blocksPerSm > 1 && (size_t)blocksPerSm * shm > 228 * 1024) --blocksPerSm;
 }
+
+}  // namespace host
+}  // namespace gal
+
+namespace {
 
 cudaError_t dispatch(gal_ctx* ctx, const Batch& b, cudaStream_t st) {
   const int mode = ctx_mode(ctx);

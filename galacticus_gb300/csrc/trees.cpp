@@ -1,0 +1,456 @@
+// trees.cpp -- host merger-tree builder: Cole et al. (2000) binary-split
+// trees with the Parkinson, Cole & Helly (2008, MNRAS 383, 557) branching
+// rates, as the reference builds them (merger_trees/construct/builder/
+// Cole2000/_class.F90:360-913, merger_trees/branching_probability/
+// Parkinson_Cole_Helly.F90:265-634).
+//
+// Each tree is grown backwards in time from its root in the variable
+// w = delta_c(z) = delta_c0 / D(z).  For a branch of mass M2 at w the
+// progenitor mass function per unit w is (extended Press-Schechter, with the
+// PCH modifier G)
+//   dN/dq = (1/sqrt(2 pi)) q^-2 |dS1/dln M1| (S1 - S2)^-3/2 G,
+//   G = G0 (sigma1/sigma2)^gamma1 (w/sigma2)^gamma2,   q = M1/M2,  S = sigma^2,
+// so a step dw splits off a resolved progenitor (q in [q_res, 1/2]) with
+// probability R dw, R = int dN/dq dq, and loses the fraction F dw of its mass
+// to progenitors below the resolution,
+//   F = (1/sqrt(2 pi)) int_{S_res}^inf (S1 - S2)^-3/2 G dS1
+//     = (2/sqrt(2 pi)) int_0^{u_res} G du,   u = (S1 - S2)^-1/2.
+// The step is limited so that R dw, F dw and dw / sqrt(2 (S(M2/2) - S2))
+// stay below the accuracy parameters.  A split creates two progenitor nodes
+// (the larger one first); a branch that drops below the resolution or
+// reaches the maximum redshift ends in a leaf node.
+//
+// sigma(M) is that of a power law n_s times the Eisenstein & Hu (1998)
+// zero-baryon transfer function, normalised to sigma8 (the reference's
+// default is the Eisenstein & Hu 1999 fit, transfer_function/
+// Eisenstein_Hu1999.F90); D(z) is the linear growth factor of a flat
+// matter + Lambda model; delta_c0 = 3 (12 pi)^(2/3) / 20.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <random>
+#include <vector>
+#include <algorithm>
+
+#include "../../include/galnode_forest.h"
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kGravity = 6.673e-11 * 1.98892e30 / 1.0e6 / (1.0e6 * 3.08567758135e16);  // km^2 s^-2 Mpc / Msun
+constexpr double kMpcPerKmPerSToGyr = 1.0e6 * 3.08567758135e16 / 1.0e3 / (1.0e9 * 3.15581497635456e7);
+
+struct Cosmo {
+  double om, ol, ob, h0;  // h0 in km/s/Mpc
+  double hubbleGyr() const { return h0 / kMpcPerKmPerSToGyr; }
+  double time(double z) const {
+    const double a = 1.0 / (1.0 + z);
+    return 2.0 / (3.0 * hubbleGyr() * std::sqrt(ol)) * std::asinh(std::sqrt(ol / om) * std::pow(a, 1.5));
+  }
+  double redshift(double t) const {
+    const double x = std::sinh(1.5 * hubbleGyr() * std::sqrt(ol) * t);
+    const double a = std::pow(x / std::sqrt(ol / om), 2.0 / 3.0);
+    return 1.0 / a - 1.0;
+  }
+};
+
+Cosmo cosmo_of(const gal_params* p) { return Cosmo{p->omega_matter, p->omega_dark_energy, p->omega_baryon, p->hubble_constant}; }
+
+// Eisenstein & Hu (1998) zero-baryon ("no wiggle") transfer function, k in 1/Mpc.
+double transfer_no_wiggle(double k, const Cosmo& c, double tcmb) {
+  const double h = c.h0 / 100.0;
+  const double omh2 = c.om * h * h, obh2 = c.ob * h * h, fb = c.ob / c.om;
+  const double theta = tcmb / 2.7;
+  const double s = 44.5 * std::log(9.83 / omh2) / std::sqrt(1.0 + 10.0 * std::pow(obh2, 0.75));
+  const double alpha = 1.0 - 0.328 * std::log(431.0 * omh2) * fb + 0.38 * std::log(22.3 * omh2) * fb * fb;
+  const double ks = 0.43 * k * s;
+  const double gammaEff = omh2 * (alpha + (1.0 - alpha) / (1.0 + ks * ks * ks * ks));  // Omega_m h^2 (...) per Mpc^-1
+  const double q = k * theta * theta / gammaEff;
+  const double l0 = std::log(2.0 * std::exp(1.0) + 1.8 * q);
+  const double c0 = 14.2 + 731.0 / (1.0 + 62.5 * q);
+  return l0 / (l0 + c0 * q * q);
+}
+
+double window_top_hat(double x) {
+  if (x < 1.0e-3) return 1.0 - x * x / 10.0;
+  return 3.0 * (std::sin(x) - x * std::cos(x)) / (x * x * x);
+}
+
+// sigma(M) at z = 0 tabulated in ln M, with its logarithmic slope.
+struct SigmaTable {
+  double lnMin = 0.0, dlnM = 0.0;
+  std::vector<double> lnSigma, slope;  // slope = dln sigma / dln M
+
+  void build(const Cosmo& c, const gal_pch_params& pch) {
+    const int nk = 8000;
+    const double lnk0 = std::log(1.0e-6), lnk1 = std::log(1.0e4), dlnk = (lnk1 - lnk0) / (nk - 1);
+    std::vector<double> kk(nk), pk(nk);
+    for (int i = 0; i < nk; ++i) {
+      kk[i] = std::exp(lnk0 + i * dlnk);
+      const double t = transfer_no_wiggle(kk[i], c, pch.temperature_cmb);
+      pk[i] = std::pow(kk[i], pch.n_s) * t * t;
+    }
+    auto sigma2R = [&](double R) {
+      double acc = 0.0;
+      for (int i = 0; i < nk; ++i) {
+        const double w = window_top_hat(kk[i] * R);
+        const double f = kk[i] * kk[i] * kk[i] * pk[i] * w * w;
+        acc += (i == 0 || i == nk - 1) ? 0.5 * f : f;
+      }
+      return acc * dlnk / (2.0 * kPi * kPi);
+    };
+    const double h = c.h0 / 100.0;
+    const double norm = pch.sigma8 * pch.sigma8 / sigma2R(8.0 / h);
+    const double rhoMean = c.om * 3.0 * c.h0 * c.h0 / (8.0 * kPi * kGravity);  // Msun/Mpc^3 (comoving, z = 0)
+    const int n = 400;
+    lnMin = std::log(1.0e4);
+    const double lnMax = std::log(1.0e17);
+    dlnM = (lnMax - lnMin) / (n - 1);
+    lnSigma.resize(n);
+    slope.resize(n);
+    for (int i = 0; i < n; ++i) {
+      const double M = std::exp(lnMin + i * dlnM);
+      const double R = std::cbrt(3.0 * M / (4.0 * kPi * rhoMean));
+      lnSigma[i] = 0.5 * std::log(norm * sigma2R(R));
+    }
+    for (int i = 0; i < n; ++i) {
+      const int a = i == 0 ? 0 : i - 1, b = i == n - 1 ? n - 1 : i + 1;
+      slope[i] = (lnSigma[b] - lnSigma[a]) / ((b - a) * dlnM);
+    }
+  }
+  // ln sigma and its slope at mass M (linear interpolation; clamped).
+  void at(double M, double& lns, double& sl) const {
+    double x = (std::log(M) - lnMin) / dlnM;
+    const int n = (int)lnSigma.size();
+    if (x < 0.0) x = 0.0;
+    if (x > n - 1.000001) x = n - 1.000001;
+    const int i = (int)x;
+    const double f = x - i;
+    lns = lnSigma[i] + f * (lnSigma[i + 1] - lnSigma[i]);
+    sl = slope[i] + f * (slope[i + 1] - slope[i]);
+  }
+  double sigma2(double M) const {
+    double lns, sl;
+    at(M, lns, sl);
+    return std::exp(2.0 * lns);
+  }
+};
+
+// w(z) = delta_c0 / D(z) tabulated in z for the inverse map.
+struct GrowthTable {
+  std::vector<double> z, w;
+  void build(const Cosmo& c) {
+    const int n = 4000;
+    const double zMax = 40.0;
+    auto E = [&](double a) { return std::sqrt(c.om / (a * a * a) + c.ol); };
+    // D(a) = (5 om / 2) E(a) int_0^a da' / (a' E(a'))^3, by Simpson's rule in a'.
+    auto growth = [&](double a) {
+      const int m = 2000;  // even
+      const double h = a / m;
+      double acc = 0.0;
+      for (int j = 0; j <= m; ++j) {
+        const double x = j * h;
+        double f = 0.0;
+        if (x > 0.0) {
+          const double ae = x * E(x);
+          f = 1.0 / (ae * ae * ae);
+        }
+        acc += (j == 0 || j == m) ? f : (j % 2 ? 4.0 * f : 2.0 * f);
+      }
+      return 2.5 * c.om * E(a) * acc * h / 3.0;
+    };
+    const double d0 = growth(1.0);
+    const double dc0 = 3.0 * std::pow(12.0 * kPi, 2.0 / 3.0) / 20.0;
+    z.resize(n);
+    w.resize(n);
+    for (int i = 0; i < n; ++i) {
+      z[i] = zMax * i / (n - 1);
+      w[i] = dc0 * d0 / growth(1.0 / (1.0 + z[i]));
+    }
+  }
+  double w_of_z(double zz) const {
+    const double x = zz / z.back() * (z.size() - 1);
+    const int i = std::min((int)x, (int)z.size() - 2);
+    const double f = x - i;
+    return w[i] + f * (w[i + 1] - w[i]);
+  }
+  double z_of_w(double ww) const {
+    if (ww <= w.front()) return 0.0;
+    const auto it = std::upper_bound(w.begin(), w.end(), ww);
+    const int i = std::min((int)(it - w.begin()) - 1, (int)w.size() - 2);
+    const double f = (ww - w[i]) / (w[i + 1] - w[i]);
+    return z[i] + f * (z[i + 1] - z[i]);
+  }
+};
+
+struct Builder {
+  const SigmaTable& sig;
+  gal_pch_params pch;
+  double mRes, wMax;
+
+  // G = G0 (sigma1/sigma2)^gamma1 (w/sigma2)^gamma2
+  double modifier(double s1, double s2, double w) const {
+    return pch.g0 * std::pow(s1 / s2, pch.gamma1) * std::pow(w / s2, pch.gamma2);
+  }
+
+  // Split rate R (per unit w) of a branch (M2, w) with its cumulative
+  // distribution over ln q on nq points from ln q_res to ln 1/2.
+  double split_rate(double M2, double w, std::vector<double>& lnq, std::vector<double>& cdf) const {
+    const int nq = 48;
+    const double qRes = mRes / M2;
+    lnq.resize(nq);
+    cdf.resize(nq);
+    if (qRes >= 0.5) {
+      std::fill(cdf.begin(), cdf.end(), 0.0);
+      return 0.0;
+    }
+    double lns2, sl2;
+    sig.at(M2, lns2, sl2);
+    const double S2 = std::exp(2.0 * lns2), s2 = std::sqrt(S2);
+    const double a = std::log(qRes), b = std::log(0.5), d = (b - a) / (nq - 1);
+    double prev = 0.0;
+    for (int i = 0; i < nq; ++i) {
+      lnq[i] = a + i * d;
+      const double q = std::exp(lnq[i]);
+      double lns1, sl1;
+      sig.at(q * M2, lns1, sl1);
+      const double S1 = std::exp(2.0 * lns1);
+      const double dS1 = 2.0 * S1 * std::fabs(sl1);  // |dS1/dln M1|
+      const double diff = S1 - S2;
+      // q dN/dq (the integrand in ln q)
+      const double f = diff > 0.0 ? dS1 / q * std::pow(diff, -1.5) * modifier(std::sqrt(S1), s2, w) / std::sqrt(2.0 * kPi) : 0.0;
+      cdf[i] = i == 0 ? 0.0 : cdf[i - 1] + 0.5 * (prev + f) * d;
+      prev = f;
+    }
+    return cdf[nq - 1];
+  }
+
+  // Sub-resolution mass-loss rate F (per unit w).
+  double accretion_rate(double M2, double w) const {
+    const double S2 = sig.sigma2(M2), s2 = std::sqrt(S2);
+    const double Sres = sig.sigma2(mRes);
+    if (!(Sres > S2)) return 0.0;
+    const double uRes = 1.0 / std::sqrt(Sres - S2);
+    const double g1 = pch.gamma1, p = 1.0 / (1.0 - g1);
+    const int nv = 32;
+    double acc = 0.0;
+    for (int j = 0; j < nv; ++j) {
+      const double v = (j + 0.5) / nv;
+      const double u = uRes * std::pow(v, p);
+      const double dudv = uRes * p * std::pow(v, p - 1.0);
+      const double s1 = std::sqrt(S2 + 1.0 / (u * u));
+      acc += modifier(s1, s2, w) * dudv;
+    }
+    return 2.0 / std::sqrt(2.0 * kPi) * acc / nv;
+  }
+
+  struct Node {
+    double mass, w;
+    int32_t parent, childFirst, childCount;
+  };
+
+  // Grow one tree from its root.
+  void grow(double rootMass, double rootW, std::mt19937_64& rng, std::vector<Node>& nodes) const {
+    nodes.clear();
+    nodes.push_back(Node{rootMass, rootW, -1, 0, 0});
+    std::vector<int32_t> stack{0};
+    std::vector<double> lnq, cdf;
+    std::uniform_real_distribution<double> U(0.0, 1.0);
+    while (!stack.empty()) {
+      const int32_t i = stack.back();
+      stack.pop_back();
+      double m = nodes[i].mass, w = nodes[i].w;
+      double mPrev = m, wPrev = w;
+      bool split = false;
+      int guard = 0;
+      while (w < wMax && m >= mRes && ++guard < 100000) {
+        const double R = split_rate(m, w, lnq, cdf);
+        const double F = accretion_rate(m, w);
+        const double S2 = sig.sigma2(m), Sh = sig.sigma2(0.5 * m);
+        double dw = pch.accuracy_second * std::sqrt(2.0 * std::max(Sh - S2, 0.0));
+        if (R > 0.0) dw = std::min(dw, pch.accuracy_first / R);
+        if (F > 0.0) dw = std::min(dw, pch.accuracy_first / F);
+        if (!(dw > 0.0)) dw = 1.0e-3;
+        bool last = false;
+        if (w + dw >= wMax) {
+          dw = wMax - w;
+          last = true;
+        }
+        const double wNext = last ? wMax : w + dw;
+        mPrev = m;
+        wPrev = w;
+        if (R > 0.0 && U(rng) < R * dw) {
+          // Split: q from the tabulated distribution in ln q.
+          const double target = U(rng) * cdf.back();
+          const int k = (int)(std::upper_bound(cdf.begin(), cdf.end(), target) - cdf.begin());
+          const int k1 = std::min(std::max(k, 1), (int)cdf.size() - 1);
+          const double f = (target - cdf[k1 - 1]) / std::max(cdf[k1] - cdf[k1 - 1], 1e-300);
+          const double q = std::exp(lnq[k1 - 1] + f * (lnq[k1] - lnq[k1 - 1]));
+          const double m1 = q * m;
+          const double m2 = m * (1.0 - F * dw) - m1;
+          const double wNew = wNext;
+          const double big = std::max(m1, m2), small = std::min(m1, m2);
+          const int32_t first = (int32_t)nodes.size();
+          int32_t count = 0;
+          if (big >= mRes) {
+            nodes.push_back(Node{big, wNew, i, 0, 0});
+            ++count;
+          }
+          if (small >= mRes) {
+            nodes.push_back(Node{small, wNew, i, 0, 0});
+            ++count;
+          }
+          nodes[i].childFirst = first;
+          nodes[i].childCount = count;
+          for (int32_t c = count - 1; c >= 0; --c) stack.push_back(first + c);
+          split = true;
+          break;
+        }
+        m *= 1.0 - F * dw;
+        w = wNext;
+        if (last) break;
+      }
+      if (!split) {
+        // The branch ends: its earliest resolved halo is a leaf progenitor.
+        double lm = m, lw = w;
+        if (m < mRes) {
+          lm = mPrev;
+          lw = wPrev;
+        }
+        if (lw > nodes[i].w && lm >= mRes) {
+          nodes[i].childFirst = (int32_t)nodes.size();
+          nodes[i].childCount = 1;
+          nodes.push_back(Node{lm, lw, i, 0, 0});
+        }
+      }
+    }
+  }
+};
+
+uint64_t splitmix64(uint64_t x) {
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+}  // namespace
+
+struct gal_forest {
+  std::vector<int32_t> tree, parent, childFirst, childCount;
+  std::vector<double> time, mass, spin;
+};
+
+extern "C" {
+
+void gal_pch_params_default(gal_pch_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof *p);
+  p->g0 = 0.57;
+  p->gamma1 = 0.38;
+  p->gamma2 = -0.01;
+  p->accuracy_first = 0.1;
+  p->accuracy_second = 0.1;
+  p->sigma8 = 0.8;
+  p->n_s = 0.96;
+  p->temperature_cmb = 2.72548;
+}
+
+double gal_cosmic_time(const gal_params* p, double z) { return p ? cosmo_of(p).time(z) : NAN; }
+double gal_redshift(const gal_params* p, double t) { return p ? cosmo_of(p).redshift(t) : NAN; }
+
+double gal_pch_sigma(const gal_params* p, const gal_pch_params* pch, double mass) {
+  if (!p || !pch || !(mass > 0.0)) return NAN;
+  SigmaTable s;
+  s.build(cosmo_of(p), *pch);
+  return std::sqrt(s.sigma2(mass));
+}
+
+int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec, gal_forest** out) {
+  if (!out) return GAL_ERR_ARGUMENT;
+  *out = nullptr;
+  if (!p || !pch || !spec || spec->n_trees < 0 || !(spec->mass_resolution > 0.0) ||
+      !(spec->root_mass_min >= spec->mass_resolution) || !(spec->root_mass_max >= spec->root_mass_min) ||
+      !(spec->redshift_max > spec->root_redshift) || spec->root_redshift < 0.0 || spec->redshift_max > 30.0)
+    return GAL_ERR_ARGUMENT;
+  const Cosmo c = cosmo_of(p);
+  SigmaTable sig;
+  sig.build(c, *pch);
+  GrowthTable gt;
+  gt.build(c);
+  const Builder B{sig, *pch, spec->mass_resolution, gt.w_of_z(spec->redshift_max)};
+  const int64_t nTrees = spec->n_trees;
+  std::vector<std::vector<Builder::Node>> trees((size_t)nTrees);
+  std::vector<std::vector<double>> spins((size_t)nTrees);
+  const double s = spec->root_mass_slope;
+  const double a = std::pow(spec->root_mass_min, s), b = std::pow(spec->root_mass_max, s);
+  const double wRoot = gt.w_of_z(spec->root_redshift);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t t = 0; t < nTrees; ++t) {
+    std::mt19937_64 rng(splitmix64(spec->seed ^ splitmix64((uint64_t)t)));
+    std::uniform_real_distribution<double> U(0.0, 1.0);
+    // dN/dln M ~ M^s on [min, max]: inverse of the cumulative M^s.
+    const double u = U(rng);
+    const double M = std::fabs(s) < 1e-12 ? spec->root_mass_min * std::pow(spec->root_mass_max / spec->root_mass_min, u)
+                                          : std::pow(a + u * (b - a), 1.0 / s);
+    B.grow(M, wRoot, rng, trees[(size_t)t]);
+    // Spins: log-normal about the peak of the Bett et al. (2007) distribution.
+    std::normal_distribution<double> N(0.0, 0.5);
+    spins[(size_t)t].resize(trees[(size_t)t].size());
+    for (double& x : spins[(size_t)t]) x = 0.04326 * std::exp(N(rng));
+  }
+  gal_forest* f = new (std::nothrow) gal_forest();
+  if (!f) return GAL_ERR_ARGUMENT;
+  size_t total = 0;
+  for (const auto& tr : trees) total += tr.size();
+  f->tree.resize(total);
+  f->parent.resize(total);
+  f->childFirst.resize(total);
+  f->childCount.resize(total);
+  f->time.resize(total);
+  f->mass.resize(total);
+  f->spin.resize(total);
+  size_t off = 0;
+  const double tMax = c.time(spec->redshift_max);
+  for (int64_t t = 0; t < nTrees; ++t) {
+    const auto& tr = trees[(size_t)t];
+    for (size_t j = 0; j < tr.size(); ++j) {
+      const size_t g = off + j;
+      f->tree[g] = (int32_t)t;
+      f->parent[g] = tr[j].parent < 0 ? -1 : (int32_t)(off + tr[j].parent);
+      f->childFirst[g] = tr[j].childCount ? (int32_t)(off + tr[j].childFirst) : 0;
+      f->childCount[g] = tr[j].childCount;
+      // Nodes on the maximum-redshift boundary get exactly that time.
+      f->time[g] = tr[j].w >= B.wMax ? tMax : c.time(gt.z_of_w(tr[j].w));
+      f->mass[g] = tr[j].mass;
+      f->spin[g] = spins[(size_t)t][j];
+    }
+    off += tr.size();
+  }
+  *out = f;
+  return GAL_OK;
+}
+
+int64_t gal_forest_node_count(const gal_forest* f) { return f ? (int64_t)f->tree.size() : -1; }
+
+int gal_forest_get(const gal_forest* f, int32_t* tree, int32_t* parent, int32_t* childFirst, int32_t* childCount,
+                   double* time, double* mass, double* spin) {
+  if (!f) return GAL_ERR_ARGUMENT;
+  const size_t n = f->tree.size();
+  auto put = [n](auto* dst, const auto& src) {
+    if (dst) std::memcpy(dst, src.data(), n * sizeof(src[0]));
+  };
+  put(tree, f->tree);
+  put(parent, f->parent);
+  put(childFirst, f->childFirst);
+  put(childCount, f->childCount);
+  put(time, f->time);
+  put(mass, f->mass);
+  put(spin, f->spin);
+  return GAL_OK;
+}
+
+void gal_forest_free(gal_forest* f) { delete f; }
+
+}  // extern "C"

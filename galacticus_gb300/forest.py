@@ -1,0 +1,202 @@
+"""Merger forests: the host tree builder and whole-forest evolution on the GPU.
+
+Mirrors the reference's tree layer around the node evolver: trees from the
+Cole et al. (2000) builder with Parkinson, Cole & Helly (2008) branching
+(merger_trees/construct/builder/Cole2000/_class.F90:360-913), evolved node by
+node to their parents' times with promotion and merging at each parent
+(merger_trees/evolver/standard.F90:762-1035).  The arrays and their meaning
+are those of include/galnode_forest.h.
+"""
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+
+
+class PchParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("g0", "gamma1", "gamma2", "accuracy_first", "accuracy_second",
+                                                "sigma8", "n_s", "temperature_cmb")]
+
+
+class ForestSpec(ctypes.Structure):
+    _fields_ = [("n_trees", ctypes.c_int64), ("seed", ctypes.c_uint64), ("root_mass_min", ctypes.c_double),
+                ("root_mass_max", ctypes.c_double), ("root_mass_slope", ctypes.c_double),
+                ("root_redshift", ctypes.c_double), ("redshift_max", ctypes.c_double),
+                ("mass_resolution", ctypes.c_double)]
+
+
+def _declare(lib):
+    if getattr(lib, "_forest_declared", False):
+        return lib
+    vp = ctypes.c_void_p
+    pp = ctypes.POINTER(_abi.Params)
+    lib.gal_pch_params_default.argtypes = [ctypes.POINTER(PchParams)]
+    lib.gal_pch_params_default.restype = None
+    lib.gal_forest_build.argtypes = [pp, ctypes.POINTER(PchParams), ctypes.POINTER(ForestSpec), ctypes.POINTER(vp)]
+    lib.gal_forest_build.restype = ctypes.c_int
+    lib.gal_forest_node_count.argtypes = [vp]
+    lib.gal_forest_node_count.restype = ctypes.c_int64
+    lib.gal_forest_get.argtypes = [vp] * 8
+    lib.gal_forest_get.restype = ctypes.c_int
+    lib.gal_forest_free.argtypes = [vp]
+    lib.gal_forest_free.restype = None
+    lib.gal_cosmic_time.argtypes = [pp, ctypes.c_double]
+    lib.gal_cosmic_time.restype = ctypes.c_double
+    lib.gal_redshift.argtypes = [pp, ctypes.c_double]
+    lib.gal_redshift.restype = ctypes.c_double
+    lib.gal_pch_sigma.argtypes = [pp, ctypes.POINTER(PchParams), ctypes.c_double]
+    lib.gal_pch_sigma.restype = ctypes.c_double
+    lib.gal_gpu_forest_create.argtypes = [vp, ctypes.c_int64] + [vp] * 7 + [ctypes.c_int32, vp, ctypes.POINTER(vp)]
+    lib.gal_gpu_forest_create.restype = ctypes.c_int
+    for name in ("gal_gpu_forest_evolve", "gal_gpu_forest_sync"):
+        getattr(lib, name).argtypes = [vp, vp]
+        getattr(lib, name).restype = ctypes.c_int
+    lib.gal_gpu_forest_snapshot_count.argtypes = [vp]
+    lib.gal_gpu_forest_snapshot_count.restype = ctypes.c_int64
+    lib.gal_gpu_forest_results.argtypes = [vp, vp] + [vp] * 6
+    lib.gal_gpu_forest_results.restype = ctypes.c_int
+    lib.gal_gpu_forest_accepted_steps.argtypes = [vp, vp]
+    lib.gal_gpu_forest_accepted_steps.restype = ctypes.c_int64
+    lib.gal_gpu_forest_autotune.argtypes = [vp, vp, ctypes.c_int32, vp]
+    lib.gal_gpu_forest_autotune.restype = ctypes.c_int
+    lib.gal_gpu_forest_free.argtypes = [vp]
+    lib.gal_gpu_forest_free.restype = None
+    lib._forest_declared = True
+    return lib
+
+
+def _vp(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+@dataclass
+class Forest:
+    tree: np.ndarray
+    parent: np.ndarray
+    child_first: np.ndarray
+    child_count: np.ndarray
+    time: np.ndarray
+    mass: np.ndarray
+    spin: np.ndarray
+
+    @property
+    def n(self):
+        return len(self.parent)
+
+
+def pch_params():
+    lib = _declare(_abi.load_library())
+    p = PchParams()
+    lib.gal_pch_params_default(ctypes.byref(p))
+    return p
+
+
+def build(params, n_trees, seed=3, root_mass_min=1e10, root_mass_max=1e14, root_mass_slope=-0.9, redshift_max=8.0,
+          mass_resolution=1e8, pch=None):
+    """Build a forest on the host (OpenMP over trees)."""
+    lib = _declare(_abi.load_library())
+    spec = ForestSpec(n_trees, seed, root_mass_min, root_mass_max, root_mass_slope, 0.0, redshift_max, mass_resolution)
+    pch = pch or pch_params()
+    handle = ctypes.c_void_p()
+    rc = lib.gal_forest_build(ctypes.byref(params), ctypes.byref(pch), ctypes.byref(spec), ctypes.byref(handle))
+    if rc:
+        raise RuntimeError(f"gal_forest_build failed ({rc})")
+    n = lib.gal_forest_node_count(handle)
+    arrays = [np.zeros(n, np.int32) for _ in range(4)] + [np.zeros(n) for _ in range(3)]
+    lib.gal_forest_get(handle, *[_vp(a) for a in arrays])
+    lib.gal_forest_free(handle)
+    return Forest(*arrays)
+
+
+def output_times(params, n=20, redshift_max=8.0):
+    """n output times from redshift_max to 0, evenly spaced in ln(1+z)."""
+    lib = _declare(_abi.load_library())
+    z = (1.0 + redshift_max) ** (1.0 - np.arange(n) / (n - 1)) - 1.0
+    z[-1] = 0.0
+    return np.array([lib.gal_cosmic_time(ctypes.byref(params), float(zz)) for zz in z])
+
+
+def initial_state(params, forest, black_hole_seed=100.0):
+    """Initial states of the progenitor-less nodes: hot gas at the universal
+    baryon fraction of the halo mass, primordial (metal-free), and a seed
+    black hole; everything else empty."""
+    state = np.zeros((_abi.NY, forest.n))
+    state[_abi.Y_HOT_MASS] = params.omega_baryon / params.omega_matter * forest.mass
+    state[_abi.Y_BLACK_HOLE] = black_hole_seed
+    return state
+
+
+class ForestEvolver:
+    """A forest resident on the GPU of an evolver context (one CUDA graph per
+    evolution)."""
+
+    def __init__(self, evolver, forest, state0, times):
+        self.lib = _declare(evolver.lib)
+        self.ev = evolver
+        self.forest = forest
+        self.n = forest.n
+        self._keep = [np.ascontiguousarray(a) for a in (forest.parent, forest.child_first, forest.child_count,
+                                                         forest.time, forest.mass, forest.spin)]
+        self.state0 = np.ascontiguousarray(state0, dtype=np.float64)
+        self.times = np.ascontiguousarray(times, dtype=np.float64)
+        handle = ctypes.c_void_p()
+        rc = self.lib.gal_gpu_forest_create(evolver.ctx, self.n, *[_vp(a) for a in self._keep], _vp(self.state0),
+                                            len(self.times), _vp(self.times), ctypes.byref(handle))
+        if rc:
+            raise RuntimeError(f"gal_gpu_forest_create failed ({rc}): {self._message()}")
+        self.handle = handle
+
+    def _message(self):
+        buf = ctypes.create_string_buffer(512)
+        self.lib.gal_gpu_last_error(self.ev.ctx, buf, 512)
+        return buf.value.decode()
+
+    def evolve(self, sync=True):
+        rc = self.lib.gal_gpu_forest_evolve(self.ev.ctx, self.handle)
+        if rc:
+            raise RuntimeError(f"gal_gpu_forest_evolve failed ({rc}): {self._message()}")
+        if sync:
+            self.sync()
+
+    def sync(self):
+        rc = self.lib.gal_gpu_forest_sync(self.ev.ctx, self.handle)
+        if rc:
+            raise RuntimeError(f"forest evolution failed ({rc}): {self._message()}")
+
+    def results(self):
+        m = self.lib.gal_gpu_forest_snapshot_count(self.handle)
+        state = np.zeros((_abi.NY, self.n))
+        status = np.zeros(self.n, np.int32)
+        counters = np.zeros((3, self.n), np.uint32)
+        snap = np.zeros((_abi.NY, max(m, 1)))
+        snap_node = np.zeros(max(m, 1), np.int32)
+        snap_out = np.zeros(max(m, 1), np.int32)
+        rc = self.lib.gal_gpu_forest_results(self.ev.ctx, self.handle, _vp(state), _vp(status), _vp(counters), _vp(snap),
+                                             _vp(snap_node), _vp(snap_out))
+        if rc:
+            raise RuntimeError(f"gal_gpu_forest_results failed ({rc}): {self._message()}")
+        return state, status, counters, snap[:, :m], snap_node[:m], snap_out[:m]
+
+    def accepted_steps(self):
+        return int(self.lib.gal_gpu_forest_accepted_steps(self.ev.ctx, self.handle))
+
+    def autotune(self, repeats=3):
+        times = np.full(8, -1.0)
+        rc = self.lib.gal_gpu_forest_autotune(self.ev.ctx, self.handle, repeats, _vp(times))
+        if rc:
+            raise RuntimeError(f"gal_gpu_forest_autotune failed ({rc}): {self._message()}")
+        return times[:6]
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.gal_gpu_forest_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,126 @@
+/*
+ * galnode_forest.h -- merger forests on the GB300 node evolver: a host
+ * merger-tree builder and whole-forest evolution in one persistent kernel.
+ *
+ * Reference: the tree evolver advances each node from its own time to its
+ * parent's, limited by the output times, and promotes or merges it there
+ * (merger_trees/evolver/standard.F90:762-1035, threaded.F90:418-840); trees
+ * come from the Cole et al. (2000) builder with the Parkinson, Cole & Helly
+ * (2008) branching rates (merger_trees/construct/builder/Cole2000/
+ * _class.F90:360-913, merger_trees/branching_probability/
+ * Parkinson_Cole_Helly.F90:265-634).  gal_gpu_evolve_forest replaces the
+ * per-node evolve calls of one forest (mergerTreeNodeEvolver%evolve, called
+ * from evolver/standard.F90:452 and threaded.F90:637) with one graph launch.
+ *
+ * Forest layout (caller-owned host arrays, n nodes): node 0 of each tree is
+ * its root; the progenitors of every node are contiguous, primary (most
+ * massive) first:
+ *   parent[n]       index of the parent, -1 for a root
+ *   child_first[n]  index of the first progenitor (any value if none)
+ *   child_count[n]  number of progenitors
+ *   time[n]         cosmic time of the node (Gyr); a progenitor's time is
+ *                   earlier than its parent's
+ *   mass[n]         halo mass at that time (Msun)
+ *   spin[n]         spin parameter
+ * A node evolves from time[i] to time[parent[i]].  On reaching it, the
+ * primary progenitor's state becomes the parent's initial state and the
+ * other progenitors' states are added to it component by component, in
+ * index order.  A primary progenitor's halo mass grows linearly to its
+ * parent's over the interval; its hot halo accretes (Omega_b/Omega_m) times
+ * the parent's mass not brought in by its progenitors.  The interval is cut
+ * at every output time inside it (each piece is one evolve call, with the
+ * step size carried over), and the state at each output time is recorded.
+ */
+#ifndef GALNODE_FOREST_H
+#define GALNODE_FOREST_H
+
+#include <stdint.h>
+#include "galnode.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- trees */
+
+typedef struct gal_pch_params {
+  double g0, gamma1, gamma2;  /* PCH merger-rate modifier G0 (s1/s2)^g1 (d2/s2)^g2 (quickTest: 0.57, 0.38, -0.01) */
+  double accuracy_first;      /* step limit on the split probability (0.1)                 */
+  double accuracy_second;     /* step limit on d(delta_c) relative to sigma (0.1)          */
+  double sigma8, n_s;         /* power-spectrum normalisation and slope                     */
+  double temperature_cmb;     /* K (2.72548)                                               */
+} gal_pch_params;
+
+typedef struct gal_forest_spec {
+  int64_t n_trees;
+  uint64_t seed;
+  double root_mass_min, root_mass_max; /* Msun                                                  */
+  double root_mass_slope;              /* dN/dln M ~ M^slope for the roots (-0.9)              */
+  double root_redshift;                /* 0                                                    */
+  double redshift_max;                 /* branches end here (8)                                */
+  double mass_resolution;              /* Msun                                                 */
+} gal_forest_spec;
+
+typedef struct gal_forest gal_forest;  /* host-side forest built by gal_forest_build */
+
+void gal_pch_params_default(gal_pch_params* p);
+
+/* Build n_trees trees with the Cole et al. (2000) algorithm and PCH
+ * branching rates, in the cosmology of p (omega_*, hubble_constant),
+ * OpenMP-parallel over trees; every tree is a deterministic function of
+ * (seed, tree index). */
+int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec, gal_forest** out);
+int64_t gal_forest_node_count(const gal_forest* f);
+/* Copy the forest out in the layout above (any pointer may be NULL);
+ * tree[n] receives the tree index of each node. */
+int gal_forest_get(const gal_forest* f, int32_t* tree, int32_t* parent, int32_t* child_first, int32_t* child_count,
+                   double* time, double* mass, double* spin);
+void gal_forest_free(gal_forest* f);
+
+/* Cosmic time (Gyr) at redshift z and its inverse, in the cosmology of p. */
+double gal_cosmic_time(const gal_params* p, double z);
+double gal_redshift(const gal_params* p, double t);
+/* sigma(M) of the builder's power spectrum at z = 0 (for tests). */
+double gal_pch_sigma(const gal_params* p, const gal_pch_params* pch, double mass);
+
+/* -------------------------------------------------------------- evolution */
+
+typedef struct gal_forest_dev gal_forest_dev;  /* a forest resident on the GPU of a context */
+
+/* Upload a forest and its output times (sorted, Gyr) to the context's GPU:
+ * the segment table (per piece: halo mass, accretion rate, virial radius
+ * and velocity, spin, start and end time) is built on the host, and
+ * state0[GAL_NY][n] holds the initial states (only progenitor-less nodes
+ * are read).  The returned object owns every device array and a CUDA graph
+ * of one evolution (reset, counters, kernel). */
+int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const int32_t* child_first,
+                          const int32_t* child_count, const double* time, const double* mass, const double* spin,
+                          const double* state0, int32_t n_outputs, const double* output_times, gal_forest_dev** out);
+/* Evolve the whole forest from state0 (one graph launch on the context
+ * stream; asynchronous: gal_gpu_forest_sync waits). */
+int gal_gpu_forest_evolve(gal_ctx* ctx, gal_forest_dev* f);
+int gal_gpu_forest_sync(gal_ctx* ctx, gal_forest_dev* f);
+/* Results of the last evolution:
+ *   state[GAL_NY][n]     each node's state on reaching its parent's time
+ *                        (a root: its state at its own time);
+ *   status[n], counters[3][n] (accepted, rejected, RHS over all pieces);
+ *   snapshot[GAL_NY][m]  states at the output times, m = snapshot count;
+ *   snap_node[m], snap_output[m]: node and output index of each snapshot. */
+int64_t gal_gpu_forest_snapshot_count(const gal_forest_dev* f);
+int gal_gpu_forest_results(gal_ctx* ctx, gal_forest_dev* f, double* state, int32_t* status, uint32_t* counters,
+                           double* snapshot, int32_t* snap_node, int32_t* snap_output);
+/* Node-timesteps (accepted steps) of the last evolution. */
+int64_t gal_gpu_forest_accepted_steps(gal_ctx* ctx, gal_forest_dev* f);
+/* Time a few evolutions at each launch shape the current form is built for
+ * (threads per block x blocks per SM) and keep the fastest in the context;
+ * times_ms[i] (may be NULL, length >= 8) receives the mean time of shape i
+ * in the order 64x1, 128x1, 128x2, 256x1, 256x2, 512x1 (negative: not
+ * available). */
+int gal_gpu_forest_autotune(gal_ctx* ctx, gal_forest_dev* f, int32_t repeats, double* times_ms);
+void gal_gpu_forest_free(gal_forest_dev* f);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

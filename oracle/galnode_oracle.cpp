@@ -918,6 +918,93 @@ static int evolve_node(const gal_params& p, const Table& tb, const double* prm, 
   return status;
 }
 
+// ---------------------------------------------------------------------------
+// Forests: the tree evolver's node loop (merger_trees/evolver/standard.F90:
+// 762-1035) over a whole forest.  A node evolves from its own time to its
+// parent's, in pieces cut at the output times (each piece one evolve call,
+// the step size carried over as node%timeStep), and on reaching the parent
+// the primary progenitor's state is promoted and the other progenitors'
+// states are added to it, component by component in index order.
+// ---------------------------------------------------------------------------
+struct Cosmology {
+  double om, ol, h0;
+  double hubbleGyr() const { return h0 / (1.0e6 * 3.08567758135e16 / 1.0e3 / (1.0e9 * 3.15581497635456e7)); }
+  // cosmologyFunctionsMatterLambda for a flat model: a(t) from the analytic solution.
+  double redshift(double t) const {
+    const double x = std::sinh(1.5 * hubbleGyr() * std::sqrt(ol) * t);
+    return 1.0 / std::pow(x / std::sqrt(ol / om), 2.0 / 3.0) - 1.0;
+  }
+  // Bryan & Norman (1998) contrast relative to the mean density
+  // (virial_density_contrast/Bryan_Norman.F90:172-196); r_vir and V_vir.
+  void virial(double M, double z, double& r, double& v) const {
+    const double G = 6.673e-11 * 1.98892e30 / 1.0e6 / (1.0e6 * 3.08567758135e16);
+    const double zp = (1.0 + z) * (1.0 + z) * (1.0 + z);
+    const double omz = om * zp / (om * zp + ol);
+    const double x = omz - 1.0;
+    const double contrast = (18.0 * M_PI * M_PI + 82.0 * x - 39.0 * x * x) / (x + 1.0);
+    const double rhoMean = om * 3.0 * h0 * h0 / (8.0 * M_PI * G) * zp;
+    r = std::cbrt(3.0 * M / (4.0 * M_PI * contrast * rhoMean));
+    v = std::sqrt(G * M / r);
+  }
+};
+
+struct ForestIn {
+  int64_t n;
+  const int32_t *parent, *childFirst, *childCount;
+  const double *time, *mass, *spin, *state0;
+  int32_t nOut;
+  const double* tOut;
+};
+
+// Evolve one node of a forest whose progenitors are done; y holds its
+// initial state, stepIo the carried step size.
+static int evolve_forest_node(const gal_params& p, const Table& tb, const Cosmology& cos, const ForestIn& F, int64_t i,
+                              double* y, double& stepIo, uint32_t counters[3], bool brent,
+                              const std::vector<int64_t>& snapFirst, double* snapshot, int64_t snapTotal) {
+  const int32_t par = F.parent[i];
+  const double t0 = F.time[i], t1 = par >= 0 ? F.time[par] : F.time[i];
+  const bool primary = par >= 0 && F.childFirst[par] == i;
+  double massEnd = F.mass[i], accretion = 0.0;
+  if (primary && t1 > t0) {
+    massEnd = F.mass[par];
+    double brought = 0.0;
+    for (int32_t c = 0; c < F.childCount[par]; ++c) brought += F.mass[F.childFirst[par] + c];
+    accretion = std::max(F.mass[par] - brought, 0.0) / (t1 - t0);
+  }
+  int64_t slot = snapFirst[i];
+  auto snap = [&](const double* v) {
+    for (int k = 0; k < GAL_NY; ++k) snapshot[k * snapTotal + slot] = v[k];
+    ++slot;
+  };
+  for (int32_t k = 0; k < F.nOut; ++k)
+    if (F.tOut[k] == t0 && (par < 0 || t0 < t1)) snap(y);
+  counters[0] = counters[1] = counters[2] = 0;
+  int status = GAL_STATUS_SUCCESS;
+  double a = t0;
+  int32_t k = 0;
+  while (k < F.nOut && !(F.tOut[k] > t0)) ++k;
+  while (a < t1 && status == GAL_STATUS_SUCCESS) {
+    const bool atOutput = k < F.nOut && F.tOut[k] < t1;
+    const double b = atOutput ? F.tOut[k] : t1;
+    const double M = F.mass[i] + (massEnd - F.mass[i]) * (a - t0) / (t1 - t0);
+    double prm[GAL_NP];
+    double r, v;
+    cos.virial(M, cos.redshift(a), r, v);
+    prm[GAL_P_MASS] = M;
+    prm[GAL_P_MASS_RATE] = accretion;
+    prm[GAL_P_RADIUS_VIRIAL] = r;
+    prm[GAL_P_VELOCITY_VIRIAL] = v;
+    prm[GAL_P_SPIN] = F.spin[i];
+    uint32_t c[3];
+    status = evolve_node<double>(p, tb, prm, y, a, b, stepIo, c, brent);
+    for (int j = 0; j < 3; ++j) counters[j] += c[j];
+    if (status == GAL_STATUS_SUCCESS && atOutput) snap(y);
+    a = b;
+    if (atOutput) ++k;
+  }
+  return status;
+}
+
 }  // namespace orc
 
 // ===========================================================================
@@ -1030,6 +1117,84 @@ int oracle_count_flops(const gal_params* p, const gal_cie_table* table, const do
   int s = orc::evolve_node<orc::Counted>(*p, tb, param, y, t0, t1, h, counters, false);
   for (int i = 0; i < orc::OP_N; ++i) ops[i] = orc::g_ops[i];
   return s;
+}
+
+
+// Snapshot slots of a forest: for each node in index order, one slot per
+// output time equal to its own time (a non-root only if it has an interval
+// to evolve) and one per output time strictly inside its interval.
+int64_t oracle_forest_snapshots(int64_t n, const int32_t* parent, const double* time, int32_t nOut, const double* tOut,
+                                int64_t* snapFirst) {
+  int64_t total = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const double t0 = time[i], t1 = parent[i] >= 0 ? time[parent[i]] : time[i];
+    if (snapFirst) snapFirst[i] = total;
+    for (int32_t k = 0; k < nOut; ++k) {
+      if (tOut[k] == t0 && (parent[i] < 0 || t0 < t1)) ++total;
+      else if (tOut[k] > t0 && tOut[k] < t1) ++total;
+    }
+  }
+  return total;
+}
+
+// Evolve a forest on the host: every tree (from each root) in post-order,
+// OpenMP-parallel over trees.  state[GAL_NY][n] receives each node's state
+// on reaching its parent's time; snapshot[GAL_NY][m] the states at the
+// output times (slots of oracle_forest_snapshots).
+int oracle_evolve_forest(const gal_params* p, const gal_cie_table* table, int64_t n, const int32_t* parent,
+                         const int32_t* childFirst, const int32_t* childCount, const double* time, const double* mass,
+                         const double* spin, const double* state0, int32_t nOut, const double* tOut, double* state,
+                         int32_t* status, uint32_t* counters, double* snapshot, int threads, int cooling_brent) {
+  if (!p || !table || n < 0 || !parent || !childFirst || !childCount || !time || !mass || !spin || !state0 || !state ||
+      !status || (nOut > 0 && !tOut))
+    return GAL_ERR_ARGUMENT;
+  orc::Table tb;
+  int rc = orc::table_load(table, tb);
+  if (rc) return rc;
+  if (threads <= 0) threads = omp_get_max_threads();
+  const orc::Cosmology cos{p->omega_matter, p->omega_dark_energy, p->hubble_constant};
+  const orc::ForestIn F{n, parent, childFirst, childCount, time, mass, spin, state0, nOut, tOut};
+  std::vector<int64_t> snapFirst((size_t)n);
+  const int64_t snapTotal = oracle_forest_snapshots(n, parent, time, nOut, tOut, snapFirst.data());
+  std::vector<double> stepOf((size_t)n, -1.0);
+  std::vector<int64_t> roots;
+  for (int64_t i = 0; i < n; ++i)
+    if (parent[i] < 0) roots.push_back(i);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
+  for (int64_t r = 0; r < (int64_t)roots.size(); ++r) {
+    // Post-order walk of this tree with an explicit stack.
+    std::vector<std::pair<int64_t, int32_t>> stack{{roots[(size_t)r], 0}};
+    while (!stack.empty()) {
+      auto& top = stack.back();
+      const int64_t i = top.first;
+      if (top.second < childCount[i]) {
+        const int64_t c = childFirst[i] + top.second;
+        ++top.second;
+        stack.push_back({c, 0});
+        continue;
+      }
+      stack.pop_back();
+      double y[GAL_NY];
+      double h = -1.0;
+      if (childCount[i] == 0) {
+        for (int v = 0; v < GAL_NY; ++v) y[v] = state0[v * n + i];
+      } else {
+        const int64_t c0 = childFirst[i];
+        for (int v = 0; v < GAL_NY; ++v) y[v] = state[v * n + c0];
+        for (int32_t c = 1; c < childCount[i]; ++c)
+          for (int v = 0; v < GAL_NY; ++v) y[v] += state[v * n + c0 + c];
+        h = stepOf[(size_t)c0];
+      }
+      uint32_t cnt[3];
+      status[i] = orc::evolve_forest_node(*p, tb, cos, F, i, y, h, cnt, cooling_brent != 0, snapFirst, snapshot,
+                                          snapTotal);
+      for (int v = 0; v < GAL_NY; ++v) state[v * n + i] = y[v];
+      stepOf[(size_t)i] = h;
+      if (counters)
+        for (int v = 0; v < 3; ++v) counters[v * n + i] = cnt[v];
+    }
+  }
+  return GAL_OK;
 }
 
 }  // extern "C"

@@ -111,3 +111,40 @@ def count_flops(params, table, param_node, y, t0, t1, step=-1.0):
                              ops.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
                              counters.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
     return ops, counters
+
+
+def forest_snapshots(forest, output_times):
+    """Snapshot slot layout of a forest: (first slot per node, total)."""
+    n = forest.n
+    first = np.zeros(n, dtype=np.int64)
+    t_out = np.ascontiguousarray(output_times, dtype=np.float64)
+    l = lib()
+    l.oracle_forest_snapshots.restype = ctypes.c_int64
+    total = l.oracle_forest_snapshots(ctypes.c_int64(n), forest.parent.ctypes.data_as(ctypes.c_void_p),
+                                      forest.time.ctypes.data_as(ctypes.c_void_p), ctypes.c_int32(len(t_out)),
+                                      t_out.ctypes.data_as(ctypes.c_void_p), first.ctypes.data_as(ctypes.c_void_p))
+    return first, int(total)
+
+
+def evolve_forest(params, table, forest, state0, output_times, threads=0, brent=True):
+    """Evolve a forest (galacticus_gb300.forest.Forest) on the CPU.  Returns
+    (state [NY][n] on reaching each parent, status, counters [3][n],
+    snapshots [NY][m] at the output times)."""
+    n = forest.n
+    t_out = np.ascontiguousarray(output_times, dtype=np.float64)
+    _, m = forest_snapshots(forest, t_out)
+    state0 = np.ascontiguousarray(state0, dtype=np.float64)
+    state = np.zeros((_abi.NY, n))
+    status = np.zeros(n, dtype=np.int32)
+    counters = np.zeros((3, n), dtype=np.uint32)
+    snap = np.zeros((_abi.NY, max(m, 1)))
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    l = lib()
+    l.oracle_evolve_forest.restype = ctypes.c_int
+    rc = l.oracle_evolve_forest(ctypes.byref(params), ctypes.byref(table.struct), ctypes.c_int64(n), vp(forest.parent),
+                                vp(forest.child_first), vp(forest.child_count), vp(forest.time), vp(forest.mass),
+                                vp(forest.spin), vp(state0), ctypes.c_int32(len(t_out)), vp(t_out), vp(state), vp(status),
+                                vp(counters), vp(snap), ctypes.c_int(threads), ctypes.c_int(1 if brent else 0))
+    if rc != 0:
+        raise RuntimeError(f"oracle_evolve_forest failed with code {rc}")
+    return state, status, counters, snap[:, :m]

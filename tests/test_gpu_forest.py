@@ -1,0 +1,175 @@
+"""Whole-forest evolution on the GPU (one CUDA graph per evolution) against the
+oracle's restatement of the tree evolver: final states, snapshots at the
+output times, counters, replay determinism, the autotuner, and baryon
+conservation."""
+
+import numpy as np
+import pytest
+
+from galacticus_gb300 import _abi, forest, workloads
+
+pytestmark = pytest.mark.gpu
+
+MASSES = [_abi.Y_HOT_MASS, _abi.Y_OUTFLOWED_MASS, _abi.Y_DISK_GAS, _abi.Y_DISK_STARS, _abi.Y_SPHEROID_GAS,
+          _abi.Y_SPHEROID_STARS, _abi.Y_BLACK_HOLE]
+
+
+@pytest.fixture(scope="module")
+def params():
+    return workloads.isolated_params()
+
+
+@pytest.fixture(scope="module")
+def case(params, table, oracle_mod):
+    f = forest.build(params, n_trees=48, seed=3, root_mass_min=1e10, root_mass_max=3e12, mass_resolution=1e8)
+    state0 = forest.initial_state(params, f)
+    times = forest.output_times(params)
+    # The oracle with the closed-form cooling radius the kernels use (the
+    # Brent root it replaces agrees to 1e-6; tests/test_oracle_golden.py).
+    ref = oracle_mod.evolve_forest(params, table, f, state0, times, brent=False)
+    return f, state0, times, ref
+
+
+def _evolver(params, table, rates="fp64"):
+    from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
+    return MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision=rates)
+
+
+def _bound(ref, params, f, nodes=None):
+    """Ten times the tolerance in the solver's mixed norm (oracle/compare.py),
+    with the absolute-tolerance scales of each node's state and halo mass."""
+    from oracle import compare
+    nodes = np.arange(f.n) if nodes is None else nodes
+    param = np.zeros((_abi.NP, len(nodes)))
+    param[_abi.P_MASS] = f.mass[nodes]
+    return compare.parity_bound(ref, ref, param, params)
+
+
+def _worst(a, ref, bound):
+    bad = np.argwhere(np.abs(a - ref) > bound)
+    return [(int(v), int(i), float(a[v, i]), float(ref[v, i])) for v, i in bad[:5]]
+
+
+def test_plain_forest_matches_oracle(case, params, table, oracle_mod):
+    f, state0, times, (ref, ref_status, ref_counters, ref_snaps) = case
+    ev = _evolver(params, table)
+    fe = forest.ForestEvolver(ev, f, state0, times)
+    fe.evolve()
+    state, status, counters, snaps, snap_node, snap_out = fe.results()
+    assert np.all(status == 0) and np.all(ref_status == 0)
+    # The plain form is the reference's FP64 arithmetic: every final mass and
+    # metal mass of every node within ten times the tolerance of the oracle
+    # (in practice to rounding).
+    bound = _bound(ref, params, f)
+    assert np.all(np.abs(state - ref) <= bound), _worst(state, ref, bound)
+    assert np.median(np.abs(state - ref) / np.maximum(np.abs(ref), 1e-300)) < 1e-12
+    # Snapshots: same slots, same values.
+    first, m = oracle_mod.forest_snapshots(f, times)
+    assert snaps.shape == ref_snaps.shape == (_abi.NY, m)
+    expected_node = np.repeat(np.arange(f.n), np.diff(np.append(first, m)))
+    sbound = _bound(ref_snaps, params, f, expected_node)
+    assert np.all(np.abs(snaps - ref_snaps) <= sbound), _worst(snaps, ref_snaps, sbound)
+    np.testing.assert_array_equal(snap_node, expected_node)
+    assert np.all(times[snap_out] >= f.time[snap_node])
+    # Same step sequences for almost every node: a rounding-level difference
+    # (the short FP64 log/exp of the kernels against the C library's) that
+    # flips one step decision is inherited by every later node of the branch.
+    same = np.all(counters == ref_counters, axis=0)
+    assert same.mean() > 0.97
+    assert fe.accepted_steps() == int(counters[0].sum())
+    fe.close()
+    ev.close()
+
+
+def test_graph_replays_are_identical(case, params, table):
+    f, state0, times, _ = case
+    ev = _evolver(params, table)
+    fe = forest.ForestEvolver(ev, f, state0, times)
+    fe.evolve()
+    a = fe.results()
+    fe.evolve()
+    fe.evolve()
+    b = fe.results()
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    fe.close()
+    ev.close()
+
+
+def test_fast_forest_within_tolerance(case, params, table):
+    f, state0, times, (ref, _, _, _) = case
+    ev = _evolver(params, table, "fp32")
+    fe = forest.ForestEvolver(ev, f, state0, times)
+    fe.evolve()
+    state, status, _, _, _, _ = fe.results()
+    assert np.all(status == 0)
+    within = np.all(np.abs(state - ref) <= _bound(ref, params, f), axis=0)
+    assert within.mean() > 0.995, within.mean()
+    roots = f.parent < 0
+    stars = state[_abi.Y_DISK_STARS][roots] + state[_abi.Y_SPHEROID_STARS][roots]
+    stars_ref = ref[_abi.Y_DISK_STARS][roots] + ref[_abi.Y_SPHEROID_STARS][roots]
+    assert abs(stars.sum() / stars_ref.sum() - 1.0) < 1e-4
+    fe.close()
+    ev.close()
+
+
+def test_autotune_picks_a_built_shape(case, params, table):
+    f, state0, times, _ = case
+    ev = _evolver(params, table, "fp32")
+    fe = forest.ForestEvolver(ev, f, state0, times)
+    t = fe.autotune(repeats=2)
+    valid = t > 0
+    assert valid.sum() >= 3 and t[0] < 0  # 64 threads is not built for the FP32 form
+    shapes = [(64, 1), (128, 1), (128, 2), (256, 1), (256, 2), (512, 1)]
+    best = shapes[int(np.argmin(np.where(valid, t, np.inf)))]
+    assert ev.get_launch() == best
+    fe.evolve()
+    assert np.all(fe.results()[1] == 0)
+    fe.close()
+    ev.close()
+
+
+def test_forest_matches_reference_root_finder(case, params, table, oracle_mod):
+    """Against the oracle with the reference's Brent cooling radius: within
+    ten times the tolerance everywhere."""
+    f, state0, times, _ = case
+    ref, _, _, _ = oracle_mod.evolve_forest(params, table, f, state0, times, brent=True)
+    ev = _evolver(params, table)
+    fe = forest.ForestEvolver(ev, f, state0, times)
+    fe.evolve()
+    state = fe.results()[0]
+    bound = _bound(ref, params, f)
+    assert np.all(np.abs(state - ref) <= bound), _worst(state, ref, bound)
+    fe.close()
+    ev.close()
+
+
+def test_surrogate_forest_conserves_baryons(case, params, table, trained):
+    from galacticus_gb300 import surrogate
+    f, state0, times, (ref, _, _, _) = case
+    ev = _evolver(params, table, "fp32")
+    trained.install(ev)
+    fe = forest.ForestEvolver(ev, f, state0, times)
+    fe.evolve()
+    state, status, _, _, _, _ = fe.results()
+    assert np.all(status == 0)
+    network, tab = surrogate.stats(ev)
+    assert network > 0
+    roots = np.flatnonzero(f.parent < 0)
+    fb = params.omega_baryon / params.omega_matter
+    baryons = state[MASSES][:, roots].sum(axis=0)
+    assert np.abs(baryons / (fb * f.mass[roots]) - 1.0).max() < 1e-3
+    fe.close()
+    ev.close()
+
+
+def test_forest_rejects_bad_topology(params, table):
+    ev = _evolver(params, table)
+    f = forest.build(params, n_trees=2, seed=1, root_mass_min=1e10, root_mass_max=1e10)
+    bad = forest.Forest(f.tree.copy(), f.parent.copy(), f.child_first.copy(), f.child_count.copy(), f.time.copy(),
+                        f.mass.copy(), f.spin.copy())
+    i = int(np.flatnonzero(bad.parent >= 0)[0])
+    bad.time[i] = bad.time[bad.parent[i]] + 1.0  # a progenitor after its parent
+    with pytest.raises(RuntimeError):
+        forest.ForestEvolver(ev, bad, forest.initial_state(params, bad), forest.output_times(params))
+    ev.close()

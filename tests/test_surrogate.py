@@ -24,12 +24,6 @@ def test_training_gradients_match_cpu_oracle():
     assert np.abs(g - ref_g).max() < 1e-5 * scale
 
 
-@pytest.fixture(scope="module")
-def trained(table):
-    # The full configuration: 2M samples, 90/10 split, Adam 1e-3, 20 epochs.
-    return surrogate.train(table, n_samples=2_000_000, epochs=20)
-
-
 def test_training_converges(trained):
     h = trained.history
     assert h[-1, 1] < 0.02 * h[0, 1] or h[-1, 1] < 1e-4
