@@ -46,6 +46,8 @@ METRIC = "node-timesteps/s on 1 GB300: batched+surrogate vs plain GPU at <=1e-3 
 UNIT = "node-timesteps/s"
 N_NODES = 65536
 WORKLOAD = "isolated-halo step: 65,536 halos/GPU, M 1e10-1e14 Msun, dt 0.01-1 Gyr, rel tol 1e-3, P-std physics"
+TREES_WORKLOAD = ("uneven trees: {} PCH trees (seed 3), roots dN/dlnM ~ M^-0.9 on 1e10-1e14 Msun, resolution "
+                  "1e8 Msun, z=8->0 with 20 outputs, rel tol 1e-3")
 GATES = (0.01, 0.005, 0.003, 0.002)  # error-map tolerances tried for the surrogate form (dex)
 MLP_FLOPS = 2 * (3 * 64 + 64 * 64 + 64 * 64 + 64)  # per network evaluation
 
@@ -60,6 +62,8 @@ def parse():
     ap.add_argument("--form", choices=["compare", "plain", "fast", "surrogate"], default="compare",
                     help="compare: the headline run; otherwise time one form alone (for profiling)")
     ap.add_argument("--gate", type=float, default=0.003, help="error-map tolerance of --form surrogate (dex)")
+    ap.add_argument("--trees", type=int, default=4096, help="trees of the uneven-trees workload (0: skip it)")
+    ap.add_argument("--tree-steps", type=int, default=2, help="timed evolutions of the whole forest per form")
     return ap.parse_args()
 
 
@@ -211,6 +215,101 @@ def mass_errors(gpu, ref):
                      "p99": float(np.percentile(rel, 99)), "max": float(rel.max()),
                      "share_within_1e-3": float(np.mean(rel <= 1e-3))}
     out["max_total"] = max(out["stellar"]["total"], out["cold_gas"]["total"])
+    return out
+
+
+def forest_mass_errors(state, ref, forest_):
+    """Root-level final stellar and cold-gas masses of a forest against the
+    FP64 oracle: relative error of the totals and per-root quantiles."""
+    from galacticus_gb300 import _abi
+    roots = forest_.parent < 0
+    out = {}
+    for name, idx in (("stellar", (_abi.Y_DISK_STARS, _abi.Y_SPHEROID_STARS)),
+                      ("cold_gas", (_abi.Y_DISK_GAS, _abi.Y_SPHEROID_GAS))):
+        g = state[idx[0]][roots] + state[idx[1]][roots]
+        r = ref[idx[0]][roots] + ref[idx[1]][roots]
+        big = r > 1e6
+        rel = np.abs(g[big] / r[big] - 1.0)
+        out[name] = {"total": float(abs(g.sum() / r.sum() - 1.0)), "median": float(np.median(rel)),
+                     "p99": float(np.percentile(rel, 99)), "max": float(rel.max())}
+    out["max_total"] = max(out["stellar"]["total"], out["cold_gas"]["total"])
+    return out
+
+
+def run_trees(args, params, table, net, gate, rank, dist, device):
+    """The uneven-trees workload: 4,096 PCH trees evolved z=8->0 with 20
+    outputs, one CUDA graph (one persistent kernel) per evolution, in the
+    plain, FP32-rate and surrogate forms; the launch shape of the surrogate
+    form picked by the autotuner."""
+    import torch
+    from galacticus_gb300 import forest, surrogate
+    from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
+    t0 = time.perf_counter()
+    f = forest.build(params, n_trees=args.trees, seed=3 + rank)
+    build_s = time.perf_counter() - t0
+    state0 = forest.initial_state(params, f)
+    times = forest.output_times(params)
+    out = {"workload": TREES_WORKLOAD.format(args.trees), "nodes": f.n, "leaves": int((f.child_count == 0).sum()),
+           "max_tree_nodes": int(np.bincount(f.tree).max()), "build_s": build_s,
+           "graph": "one CUDA graph per evolution: counter reset, leaf-queue reset, one persistent kernel",
+           "timing": "host clock around the graph launch and its completion event, after 1 warm-up evolution", "forms": {}}
+    results = {}
+    for name, rates in (("plain", "fp64"), ("fast_no_network", "fp32"), ("surrogate", "fp32")):
+        ev = MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision=rates)
+        if name == "surrogate":
+            net.build_error_map(table, tolerance=gate)
+            net.install(ev)
+        fe = forest.ForestEvolver(ev, f, state0, times)
+        if name == "surrogate":
+            tuned = fe.autotune(repeats=2)
+            out["autotune"] = {"shapes": ["64x1", "128x1", "128x2", "256x1", "256x2", "512x1"],
+                               "ms": [None if x < 0 else float(x) for x in tuned], "chosen": list(ev.get_launch()),
+                               "note": "one lane per node: the warps-per-node axis is 1 by construction"}
+        elif name == "fast_no_network":
+            ev.set_launch(128, 2)
+        fe.evolve()
+        s0 = surrogate.stats(ev) if name == "surrogate" else (0, 0)
+        reps = max(1, args.tree_steps)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(device)
+        tb = time.perf_counter()
+        for _ in range(reps):
+            fe.evolve(sync=False)
+        fe.sync()
+        dt = (time.perf_counter() - tb) / reps
+        if dist:
+            tt = torch.tensor([dt], device=device)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            dt = float(tt.item())
+        acc = fe.accepted_steps()
+        accepted_all = acc
+        if dist:
+            a = torch.tensor([acc], device=device, dtype=torch.int64)
+            dist.all_reduce(a, op=dist.ReduceOp.SUM)
+            accepted_all = int(a.item())
+        state, status = fe.results()[:2]
+        entry = {"value": accepted_all / dt, "s_per_evolution": dt, "accepted_steps": acc, "launch": list(ev.get_launch()),
+                 "failed_nodes": int((status != 0).sum())}
+        if name == "surrogate":
+            s1 = surrogate.stats(ev)
+            entry["network_share"] = (s1[0] - s0[0]) / max(1, (s1[0] - s0[0]) + (s1[1] - s0[1]))
+            entry["gate_dex"] = gate
+        results[name] = state
+        out["forms"][name] = entry
+        fe.close()
+        ev.close()
+    if rank == 0:
+        from oracle import oracle
+        tb = time.perf_counter()
+        ref = oracle.evolve_forest(params, table, f, state0, times, threads=os.cpu_count() or 1, brent=True)[0]
+        cpu_s = time.perf_counter() - tb
+        acc = out["forms"]["plain"]["accepted_steps"]
+        out["cpu_baseline"] = {"value": acc / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": f"one evolution of the whole forest ({cpu_s:.1f} s)"}
+        for name, state in results.items():
+            out["forms"][name]["mass_error"] = forest_mass_errors(state, ref, f)
+        out["speedup_surrogate_vs_plain"] = out["forms"]["surrogate"]["value"] / out["forms"]["plain"]["value"]
     return out
 
 
@@ -388,6 +487,8 @@ def run_ours(args):
         for name in ("plain", "fast"):
             others[name]["mass_error"] = mass_errors(final_state(forms[name]), ref)
 
+    trees = run_trees(args, params, table, net, chosen, rank, dist, dev) if args.trees > 0 else None
+
     # End-to-end through the public host API (pinned host buffers, copies in the timed region).
     ev = forms["surrogate"]
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -470,6 +571,8 @@ def run_ours(args):
             "clocks": headline["clocks"],
             "cpu_baseline": cpu,
         }
+        if trees:
+            line["trees"] = trees
         if spec:
             line["forms"]["surrogate_gate_0.01"] = {k: spec.get(k) for k in ("value", "ms_per_step", "errors", "table_cells")}
         print(json.dumps(line), flush=True)
