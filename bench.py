@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--nodes", type=int, default=N_NODES)
-    ap.add_argument("--form", choices=["compare", "plain", "fast", "surrogate"], default="compare",
+    ap.add_argument("--form", choices=["compare", "plain", "fast", "surrogate", "trees-plain", "trees-fast",
+                                       "trees-surrogate"], default="compare",
                     help="compare: the headline run; otherwise time one form alone (for profiling)")
     ap.add_argument("--gate", type=float, default=0.003, help="error-map tolerance of --form surrogate (dex)")
     ap.add_argument("--trees", type=int, default=4096, help="trees of the uneven-trees workload (0: skip it)")
@@ -426,6 +427,32 @@ def run_ours(args):
                 "kernel_ms": kernel_ms, "accepted_per_pass": accepted, "launches": lib.gal_gpu_launch_count(ev.ctx) - launches0,
                 "wall_ms": wall * 1e3, "clocks": sampler.summary() if sampler else None}
 
+    if args.form.startswith("trees-"):
+        # One forest form alone (profiling runs): W + K evolutions of the forest.
+        from galacticus_gb300 import forest as forest_mod
+        name = args.form[len("trees-"):]
+        ev = forms[name]
+        if name == "surrogate":
+            net.build_error_map(table, tolerance=args.gate)
+            net.install(ev)
+        f = forest_mod.build(params, n_trees=args.trees, seed=3 + rank)
+        fe = forest_mod.ForestEvolver(ev, f, forest_mod.initial_state(params, f), forest_mod.output_times(params))
+        for _ in range(args.warmup):
+            fe.evolve()
+        tb = time.perf_counter()
+        for _ in range(args.steps):
+            fe.evolve()
+        dt = (time.perf_counter() - tb) / max(1, args.steps)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "form": args.form, "value": fe.accepted_steps() / dt, "unit": UNIT,
+                              "s_per_evolution": dt, "nodes": f.n, "steps": args.steps, "warmup": args.warmup,
+                              "launch": list(ev.get_launch())}), flush=True)
+        fe.close()
+        for e in forms.values():
+            e.close()
+        if dist:
+            dist.destroy_process_group()
+        return
     if args.form != "compare":
         # One form alone (profiling runs): no oracle, no comparison.
         ev = forms[args.form]

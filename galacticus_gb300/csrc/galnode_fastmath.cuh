@@ -13,11 +13,12 @@
 //  * rcp/div/rsqrt/sqrt: the single-precision hardware approximation
 //    (relative error ~1e-7) refined by two Newton-Raphson steps in FP64,
 //    which square the error twice (~1e-28) before the final rounding.
-//  * log: the classical table-driven reduction.  x = 2^e m, m in [1,2);
+//  * log: the table-driven reduction of Tang (1990, ACM TOMS 16, 378).  x = 2^e m, m in [1,2);
 //    c = 1 + (j + 1/2)/128 from the top seven mantissa bits; then
 //    ln x = e ln 2 + ln c + ln(1 + r), r = m/c - 1, |r| < 2^-8, with
 //    ln(1 + r) from its Taylor series to r^6 (truncation < 2^-58).
-//  * exp: x = (64 k + j) ln2/64 + r, |r| <= ln2/128, so
+//  * exp: the table-driven reduction of Tang (1989, ACM TOMS 15, 144):
+//    x = (64 k + j) ln2/64 + r, |r| <= ln2/128, so
 //    e^x = 2^k 2^(j/64) e^r with e^r from its Taylor series to r^6
 //    (truncation < 2^-65) and 2^(j/64) from a table.
 //  * inv_root: x^(-1/Q) from the single-precision seed and Newton steps
