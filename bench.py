@@ -50,6 +50,9 @@ TREES_WORKLOAD = ("uneven trees: {} PCH trees (seed 3), roots dN/dlnM ~ M^-0.9 o
                   "1e8 Msun, z=8->0 with 20 outputs, rel tol 1e-3")
 GATES = (0.01, 0.005, 0.003, 0.002)  # error-map tolerances tried for the surrogate form (dex)
 MLP_FLOPS = 2 * (3 * 64 + 64 * 64 + 64 * 64 + 64)  # per network evaluation
+# dram__bytes_read.sum + dram__bytes_write.sum of the headline kernel (the
+# surrogate form on this workload) from one ncu --set full capture, per launch.
+HEADLINE_DRAM_BYTES = 10.753024e6 + 4.864e3
 
 
 def parse():
@@ -585,7 +588,8 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(headline["launches"]),
             "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": flops_peak.value / 1e12, "unit": "TFLOP/s",
-                         "frac": achieved / flops_peak.value, "traffic": None,
+                         "frac": achieved / flops_peak.value, "traffic": HEADLINE_DRAM_BYTES,
+                         "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
                          "basis": "the reference's FP64 work per node-timestep (counted by the oracle) over the surrogate-form kernel time",
                          "peak_source": "measured by gal_calibrate_fp64 (DFMA loop on all SMs); MEASURED_PEAKS.json has no FP64 figure",
                          "flops_per_node_timestep": f_step, "kernel_ms": k_ms,

@@ -132,9 +132,14 @@ __host__ __device__ inline size_t surrogate_shared_bytes(int mapCells) {
   return (size_t)((kSurrSmall + 3) & ~3) * sizeof(float) + 4 * (size_t)kSurrPlane * sizeof(__nv_bfloat16) +
          (size_t)((mapCells + 15) & ~15);
 }
-__host__ __device__ inline size_t evolve_shared_bytes(int mode, int nT, int nZ, int mapCells) {
+// The surrogate block starts on a 16-byte boundary (ldmatrix row addresses).
+__host__ __device__ inline size_t surrogate_offset(int mode, int nT, int nZ) {
   const size_t base = (mode & MODE_FAST) ? shared_bytes_fast(nT, nZ) : shared_bytes(nT, nZ);
-  return base + ((mode & MODE_SURROGATE) ? surrogate_shared_bytes(mapCells) : 0);
+  return (base + 15) & ~(size_t)15;
+}
+__host__ __device__ inline size_t evolve_shared_bytes(int mode, int nT, int nZ, int mapCells) {
+  if (!(mode & MODE_SURROGATE)) return (mode & MODE_FAST) ? shared_bytes_fast(nT, nZ) : shared_bytes(nT, nZ);
+  return surrogate_offset(mode, nT, nZ) + surrogate_shared_bytes(mapCells);
 }
 
 // Cooling function (without the n_H^2 factor) and n_e/n_H of one
@@ -230,7 +235,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
     for (int i = threadIdx.x; i < nZ * nT; i += blockDim.x) sTab[i] = T.tabF[i];
     for (int i = threadIdx.x; i < 2 * nZ; i += blockDim.x) sLnZ[i] = T.lnZF[i];
     SF = SmemF{sTab, sLnZ, sLnZ + nZ};
-    tail = reinterpret_cast<unsigned char*>(smem) + shared_bytes_fast(nT, nZ);
+    tail = reinterpret_cast<unsigned char*>(smem) + surrogate_offset(MODE, nT, nZ);
   } else {
     double2* sTab = smem;
     double2* sFastLog = sTab + nZ * nT;
@@ -245,7 +250,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
     for (int i = threadIdx.x; i < kExpTableSize; i += blockDim.x) sFastExp[i] = T.fastExp[i];
     S = Smem{sTab, sLnZ, sInvDlnZ, FastTables{sFastLog, sFastExp}};
     sLnT = lnT;
-    tail = reinterpret_cast<unsigned char*>(smem) + shared_bytes(nT, nZ);
+    tail = reinterpret_cast<unsigned char*>(smem) + surrogate_offset(MODE, nT, nZ);
   }
   const float* sSmall = nullptr;
   const __nv_bfloat16* sPlanes = nullptr;

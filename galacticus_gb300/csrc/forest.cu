@@ -258,6 +258,19 @@ int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const 
     }
     segCount[i] = (int32_t)segT0.size() - segFirst[i];
   }
+  // Longest chains first: a leaf's chain to its root is the sequence of
+  // nodes that can only run one after another, so leaves are queued by the
+  // number of their ancestors, largest first (ties in index order).  The
+  // deep branches of the largest trees then start at once instead of
+  // setting the end of the evolution.
+  {
+    std::vector<int64_t> byTime((size_t)n);
+    for (int64_t i = 0; i < n; ++i) byTime[(size_t)i] = i;
+    std::stable_sort(byTime.begin(), byTime.end(), [&](int64_t a, int64_t b) { return time[a] > time[b]; });
+    std::vector<int32_t> depth((size_t)n, 0);
+    for (int64_t i : byTime) depth[(size_t)i] = parent[i] < 0 ? 0 : depth[(size_t)parent[i]] + 1;
+    std::stable_sort(leaves.begin(), leaves.end(), [&](int32_t a, int32_t b) { return depth[(size_t)a] > depth[(size_t)b]; });
+  }
   f->nLeaves = (int64_t)leaves.size();
   f->nSeg = (int64_t)segT0.size();
   f->nSnap = slot;

@@ -452,7 +452,7 @@ int gal_gpu_set_surrogate(gal_ctx* ctx, const gal_surrogate* sg) {
   I.mapLoZ = sg->map_lo_z;
   I.mapInvDT = 1.0f / sg->map_dt;
   I.mapInvDZ = 1.0f / sg->map_dz;
-  if (shared_bytes(ctx->globals.nT, ctx->globals.nZ) + surrogate_shared_bytes(cells) > 227 * 1024)
+  if (evolve_shared_bytes(MODE_SURROGATE, ctx->globals.nT, ctx->globals.nZ, cells) > 227 * 1024)
     return fail(ctx, GAL_ERR_TOO_LARGE, "gal_gpu_set_surrogate: shared memory footprint too large%s");
   if (cudaMalloc(&ctx->dSurrSmall, small.size() * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&ctx->dSurrPlanes, planes.size() * sizeof(__nv_bfloat16)) != cudaSuccess ||
