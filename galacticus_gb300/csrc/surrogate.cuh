@@ -94,11 +94,26 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+// Four 8x8 BF16 matrices from shared memory (ldmatrix): lanes 8m..8m+7 give
+// the row addresses of matrix m; each lane receives, of every matrix, the
+// pair of row (lane/4), columns 2 (lane%4), +1 -- a B fragment when the
+// matrix rows are rows of W.
+__device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], const __nv_bfloat16* rowAddress) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(rowAddress);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+
 // One 64 -> 64 layer for one 16-row tile: acc[nt] (columns nt*8 + 2t, +1 of
-// rows g and g+8) = bias + A W^T with the split products.
+// rows g and g+8) = bias + A W^T with the split products.  The B fragments
+// of one (n-tile, k-step) -- hi and lo planes, k 0-7 and 8-15 -- come from one
+// ldmatrix: lane l addresses row l%8 of the n-tile in the hi (l < 16) or lo
+// plane, at k offset 8 ((l/8) % 2).
 __device__ __forceinline__ void mlp_layer_tile(const uint32_t (&ahi)[4][4], const uint32_t (&alo)[4][4],
                                                const __nv_bfloat16* whi, const __nv_bfloat16* wlo, const float* bias,
-                                               float (&acc)[8][4], int g, int t) {
+                                               float (&acc)[8][4], int g, int t, int lane) {
+  const __nv_bfloat16* laneRow = (lane < 16 ? whi : wlo) + (lane & 7) * kMlpStride + ((lane >> 3) & 1) * 8;
 #pragma unroll
   for (int nt = 0; nt < 8; ++nt) {
     const int col = nt * 8 + 2 * t;
@@ -106,16 +121,13 @@ __device__ __forceinline__ void mlp_layer_tile(const uint32_t (&ahi)[4][4], cons
     acc[nt][1] = bias[col + 1];
     acc[nt][2] = bias[col];
     acc[nt][3] = bias[col + 1];
-    const int wrow = (nt * 8 + g) * kMlpStride + 2 * t;
 #pragma unroll
     for (int ks = 0; ks < 4; ++ks) {
-      const uint32_t bh0 = *reinterpret_cast<const uint32_t*>(whi + wrow + ks * 16);
-      const uint32_t bh1 = *reinterpret_cast<const uint32_t*>(whi + wrow + ks * 16 + 8);
-      const uint32_t bl0 = *reinterpret_cast<const uint32_t*>(wlo + wrow + ks * 16);
-      const uint32_t bl1 = *reinterpret_cast<const uint32_t*>(wlo + wrow + ks * 16 + 8);
-      mma_bf16(acc[nt], alo[ks], bh0, bh1);
-      mma_bf16(acc[nt], ahi[ks], bl0, bl1);
-      mma_bf16(acc[nt], ahi[ks], bh0, bh1);
+      uint32_t b[4];  // hi k0-7, hi k8-15, lo k0-7, lo k8-15
+      ldmatrix_x4(b, laneRow + nt * 8 * kMlpStride + ks * 16);
+      mma_bf16(acc[nt], alo[ks], b[0], b[1]);
+      mma_bf16(acc[nt], ahi[ks], b[2], b[3]);
+      mma_bf16(acc[nt], ahi[ks], b[0], b[1]);
     }
   }
 }
@@ -129,8 +141,13 @@ __device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0
                                                unsigned need = 0xffffffffu) {
   const unsigned FULLMASK = 0xffffffffu;
   const int g = lane >> 2, t = lane & 3;
-  float part[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};  // [m-tile][row g, row g+8]: this lane's share of the output
-#pragma unroll
+  // Row `lane` of the warp is row (lane & 7) of half (lane >> 3) & 1 of
+  // tile lane >> 4; its sum ends up in lane 4 (lane & 7) of that tile's pass.
+  float out = 0.0f;
+  const int src = 4 * (lane & 7);
+  // The tiles are not unrolled: one copy of the network code (the kernel
+  // that calls it is otherwise instruction-fetch bound).
+#pragma unroll 1
   for (int mt = 0; mt < 2; ++mt) {
     if (((need >> (16 * mt)) & 0xffffu) == 0u) continue;
     const int r0 = mt * 16 + g, r1 = r0 + 8;
@@ -155,7 +172,7 @@ __device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0
       }
     }
     float acc[8][4];
-    mlp_layer_tile(ahi, alo, N.w2hi, N.w2lo, N.b2, acc, g, t);
+    mlp_layer_tile(ahi, alo, N.w2hi, N.w2lo, N.b2, acc, g, t, lane);
     // Layer 2's accumulators (n-tiles 2ks and 2ks+1) are layer 3's A fragments for k-step ks.
 #pragma unroll
     for (int ks = 0; ks < 4; ++ks) {
@@ -164,7 +181,7 @@ __device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0
       split_bf16(silu(acc[2 * ks + 1][0]), silu(acc[2 * ks + 1][1]), ahi[ks][2], alo[ks][2]);
       split_bf16(silu(acc[2 * ks + 1][2]), silu(acc[2 * ks + 1][3]), ahi[ks][3], alo[ks][3]);
     }
-    mlp_layer_tile(ahi, alo, N.w3hi, N.w3lo, N.b3, acc, g, t);
+    mlp_layer_tile(ahi, alo, N.w3hi, N.w3lo, N.b3, acc, g, t, lane);
     // Output layer (FP32): this lane's 16 columns of rows r0 and r1, then the
     // sum over the four lanes of the row group.
     float p0 = 0.0f, p1 = 0.0f;
@@ -178,16 +195,10 @@ __device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0
     p0 += __shfl_xor_sync(FULLMASK, p0, 2);
     p1 += __shfl_xor_sync(FULLMASK, p1, 1);
     p1 += __shfl_xor_sync(FULLMASK, p1, 2);
-    part[mt][0] = p0;
-    part[mt][1] = p1;
+    const float o0 = __shfl_sync(FULLMASK, p0, src), o1 = __shfl_sync(FULLMASK, p1, src);
+    if ((lane >> 4) == mt) out = ((lane >> 3) & 1) ? o1 : o0;
   }
-  // Row `lane` is row g' = lane & 7 of half (lane >> 3) of the two tiles: its
-  // sum sits in lane 4 (lane & 7).
-  const int src = 4 * (lane & 7);
-  const float a = __shfl_sync(FULLMASK, part[0][0], src), b = __shfl_sync(FULLMASK, part[0][1], src);
-  const float c = __shfl_sync(FULLMASK, part[1][0], src), d = __shfl_sync(FULLMASK, part[1][1], src);
-  const int q = lane >> 3;
-  return N.b4 + (q == 0 ? a : (q == 1 ? b : (q == 2 ? c : d)));
+  return N.b4 + out;
 }
 
 // Host-side packing of the FP32 parameters into the block the kernels

@@ -173,3 +173,24 @@ def test_forest_rejects_bad_topology(params, table):
     with pytest.raises(RuntimeError):
         forest.ForestEvolver(ev, bad, forest.initial_state(params, bad), forest.output_times(params))
     ev.close()
+
+
+def test_small_cpu_configuration(table, oracle_mod):
+    """The reference's small plain configuration: 32 PCH trees (seed 1), roots
+    log-uniform 1e10-1e12 Msun, resolution 1e9, z=8 to 0, relative tolerance
+    1e-2: the GPU forest against the oracle's, node by node."""
+    params = workloads.isolated_params(tolerance_relative=1e-2)
+    f = forest.build(params, n_trees=32, seed=1, root_mass_min=1e10, root_mass_max=1e12, root_mass_slope=0.0,
+                     mass_resolution=1e9)
+    state0 = forest.initial_state(params, f)
+    times = forest.output_times(params)
+    ref, ref_status, _, _ = oracle_mod.evolve_forest(params, table, f, state0, times, brent=False)
+    ev = _evolver(params, table)
+    fe = forest.ForestEvolver(ev, f, state0, times)
+    fe.evolve()
+    state, status = fe.results()[:2]
+    assert np.all(status == 0) and np.all(ref_status == 0)
+    bound = _bound(ref, params, f)
+    assert np.all(np.abs(state - ref) <= bound), _worst(state, ref, bound)
+    fe.close()
+    ev.close()
