@@ -68,6 +68,9 @@ def parse():
     ap.add_argument("--gate", type=float, default=0.003, help="error-map tolerance of --form surrogate (dex)")
     ap.add_argument("--trees", type=int, default=4096, help="trees of the uneven-trees workload (0: skip it)")
     ap.add_argument("--tree-steps", type=int, default=2, help="timed evolutions of the whole forest per form")
+    ap.add_argument("--workload", choices=["isolated", "scale"], default="isolated",
+                    help="scale: the full chosen form on a forest at scale (one JSON line of its own)")
+    ap.add_argument("--trees-scale", type=int, default=65536, help="trees of the scale workload")
     return ap.parse_args()
 
 
@@ -292,7 +295,7 @@ def run_trees(args, params, table, net, gate, rank, dist, device):
             a = torch.tensor([acc], device=device, dtype=torch.int64)
             dist.all_reduce(a, op=dist.ReduceOp.SUM)
             accepted_all = int(a.item())
-        state, status = fe.results()[:2]
+        state, status = fe.results(snapshots=False)[:2]
         entry = {"value": accepted_all / dt, "s_per_evolution": dt, "accepted_steps": acc, "launch": list(ev.get_launch()),
                  "failed_nodes": int((status != 0).sum())}
         if name == "surrogate":
@@ -315,6 +318,90 @@ def run_trees(args, params, table, net, gate, rank, dist, device):
             out["forms"][name]["mass_error"] = forest_mass_errors(state, ref, f)
         out["speedup_surrogate_vs_plain"] = out["forms"]["surrogate"]["value"] / out["forms"]["plain"]["value"]
     return out
+
+
+def run_scale(args):
+    """The full chosen form at scale: 65,536 PCH trees (seed 5), z=10->0 with
+    50 outputs, the surrogate form with the table fallback against the plain
+    GPU form and the CPU oracle (one evolution of each, after a warm-up)."""
+    import torch
+    from galacticus_gb300 import _abi, forest, surrogate, workloads
+    from galacticus_gb300.cie_tables import CieTable
+    from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
+    from oracle import oracle
+    torch.cuda.set_device(0)
+    params = workloads.isolated_params()
+    table = CieTable()
+    t0 = time.perf_counter()
+    f = forest.build(params, n_trees=args.trees_scale, seed=5, redshift_max=10.0)
+    build_s = time.perf_counter() - t0
+    state0 = forest.initial_state(params, f)
+    times = forest.output_times(params, n=50, redshift_max=10.0)
+    net = surrogate.train(table)
+    out = {"workload": f"scale: {args.trees_scale} PCH trees (seed 5), roots dN/dlnM ~ M^-0.9 on 1e10-1e14 Msun, resolution "
+                       f"1e8 Msun, z=10->0 with 50 outputs, rel tol 1e-3", "metric": METRIC, "unit": UNIT,
+           "nodes": f.n, "leaves": int((f.child_count == 0).sum()), "max_tree_nodes": int(np.bincount(f.tree).max()),
+           "build_s": build_s, "forms": {}}
+    states = {}
+    for name, rates in (("plain", "fp64"), ("surrogate", "fp32")):
+        ev = MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision=rates)
+        ev.set_launch(128, 1 if rates == "fp64" else 2)
+        if name == "surrogate":
+            net.build_error_map(table, tolerance=args.gate)
+            net.install(ev)
+        fe = forest.ForestEvolver(ev, f, state0, times)
+        out["snapshots"] = fe.snapshot_count()
+        fe.evolve()
+        s0 = surrogate.stats(ev) if name == "surrogate" else (0, 0)
+        tb = time.perf_counter()
+        fe.evolve()
+        dt = time.perf_counter() - tb
+        state, status, counters = fe.results(snapshots=False)[:3]
+        entry = {"value": float(counters[0].sum()) / dt, "s_per_evolution": dt, "accepted_steps": int(counters[0].sum()),
+                 "rhs_evaluations": int(counters[2].sum()), "failed_nodes": int((status != 0).sum())}
+        if name == "surrogate":
+            s1 = surrogate.stats(ev)
+            served = s1[0] - s0[0]
+            entry["gate_dex"] = args.gate
+            entry["fallback_rate"] = 1.0 - served / max(1, served + (s1[1] - s0[1]))
+        states[name] = state
+        out["forms"][name] = entry
+        fe.close()
+        ev.close()
+    tb = time.perf_counter()
+    ref = oracle.evolve_forest(params, table, f, state0, times, threads=os.cpu_count() or 1, brent=True)[0]
+    cpu_s = time.perf_counter() - tb
+    out["cpu_baseline"] = {"value": out["forms"]["plain"]["accepted_steps"] / cpu_s, "unit": UNIT,
+                           "cores": os.cpu_count() or 1, "kind": "port", "sample": f"one evolution of the whole forest ({cpu_s:.1f} s)"}
+    out["forms"]["plain"]["mass_error_vs_cpu"] = forest_mass_errors(states["plain"], ref, f)
+    out["forms"]["surrogate"]["mass_error_vs_cpu"] = forest_mass_errors(states["surrogate"], ref, f)
+    out["forms"]["surrogate"]["mass_error_vs_plain_gpu"] = forest_mass_errors(states["surrogate"], states["plain"], f)
+    out["speedup_surrogate_vs_plain"] = out["forms"]["surrogate"]["value"] / out["forms"]["plain"]["value"]
+    # Rooflines: the reference's FP64 work per RHS evaluation (counted by the
+    # oracle on the isolated-halo workload) times the RHS evaluations, and the
+    # forest arrays each evolution reads and writes.
+    flops_peak, calib_ms = ctypes.c_double(), ctypes.c_double()
+    lib = _abi.load_library()
+    lib.gal_calibrate_fp64(ctypes.byref(flops_peak), ctypes.byref(calib_ms))
+    batch = workloads.isolated_halos(n=4096, seed=2)
+    f_step = algorithmic_flops_per_step(params, table, batch, os.path.join(ROOT, "oracle", "flop_weights.json"))
+    _, _, _, cb = oracle.evolve_batch(params, table, batch.state, batch.param, batch.t_start, batch.t_end, batch.step)
+    f_rhs = f_step * cb[0].sum() / cb[2].sum()
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    nbytes = f.n * (2 * _abi.NY * 8 + 6 * 4 + 8) + out["snapshots"] * _abi.NY * 8
+    for name, entry in out["forms"].items():
+        achieved = f_rhs * entry["rhs_evaluations"] / entry["s_per_evolution"]
+        entry["roofline"] = {"fp64": {"achieved_tflops": achieved / 1e12, "peak_tflops": flops_peak.value / 1e12,
+                                      "frac": achieved / flops_peak.value},
+                             "hbm": {"achieved_gbs": nbytes / entry["s_per_evolution"] / 1e9, "peak_gbs": peaks.get("hbm_gbs"),
+                                     "frac": (nbytes / entry["s_per_evolution"] / 1e9 / peaks["hbm_gbs"]) if peaks.get("hbm_gbs") else None}}
+    out["flops_per_rhs"] = f_rhs
+    print(json.dumps(out), flush=True)
 
 
 def run_ours(args):
@@ -615,6 +702,9 @@ def run_ours(args):
 
 def main():
     args = parse()
+    if args.workload == "scale":
+        run_scale(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

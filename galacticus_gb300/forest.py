@@ -166,19 +166,27 @@ class ForestEvolver:
         if rc:
             raise RuntimeError(f"forest evolution failed ({rc}): {self._message()}")
 
-    def results(self):
-        m = self.lib.gal_gpu_forest_snapshot_count(self.handle)
+    def results(self, snapshots=True):
+        """(state, status, counters, snapshots, snapshot node, snapshot output);
+        the last three are None with snapshots=False."""
+        m = self.lib.gal_gpu_forest_snapshot_count(self.handle) if snapshots else 0
         state = np.zeros((_abi.NY, self.n))
         status = np.zeros(self.n, np.int32)
         counters = np.zeros((3, self.n), np.uint32)
-        snap = np.zeros((_abi.NY, max(m, 1)))
-        snap_node = np.zeros(max(m, 1), np.int32)
-        snap_out = np.zeros(max(m, 1), np.int32)
-        rc = self.lib.gal_gpu_forest_results(self.ev.ctx, self.handle, _vp(state), _vp(status), _vp(counters), _vp(snap),
-                                             _vp(snap_node), _vp(snap_out))
+        snap = np.zeros((_abi.NY, max(m, 1))) if snapshots else None
+        snap_node = np.zeros(max(m, 1), np.int32) if snapshots else None
+        snap_out = np.zeros(max(m, 1), np.int32) if snapshots else None
+        vp = lambda a: None if a is None else _vp(a)
+        rc = self.lib.gal_gpu_forest_results(self.ev.ctx, self.handle, _vp(state), _vp(status), _vp(counters), vp(snap),
+                                             vp(snap_node), vp(snap_out))
         if rc:
             raise RuntimeError(f"gal_gpu_forest_results failed ({rc}): {self._message()}")
+        if not snapshots:
+            return state, status, counters, None, None, None
         return state, status, counters, snap[:, :m], snap_node[:m], snap_out[:m]
+
+    def snapshot_count(self):
+        return int(self.lib.gal_gpu_forest_snapshot_count(self.handle))
 
     def accepted_steps(self):
         return int(self.lib.gal_gpu_forest_accepted_steps(self.ev.ctx, self.handle))
