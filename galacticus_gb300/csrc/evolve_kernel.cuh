@@ -701,8 +701,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
             // The post-step clamps return GSL_Continue: dydt_out is kept.
             needOut = false;
             ++nRhs;
-            post_step(y);
-            sync_yr();
+            if (post_step(y)) sync_yr();
             if (budget && count >= budget) {
               finished = true;
               finalStatus = GAL_STATUS_XCPU;
@@ -793,8 +792,12 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
           const RateT est = (RateT)ck::e1 * k1[i] + (RateT)ck::e3 * k3[i] + (RateT)ck::e4 * k4[i] + (RateT)ck::e5 * k5[i] +
                             (RateT)ck::e6 * k6[i];
           ynew[i] = y[i] + hh * (double)inc;
+          // (float)ynew: the FP32 state copy if the step is accepted (kept in
+          // the free stage-argument array of the FP32 forms).
+          const float ynf = (float)ynew[i];
+          if constexpr (FAST) x[i] = ynf;
           const float errF = fabsf((float)hr * (float)est);
-          const float dF = fabsf((float)epsRel * fabsf((float)ynew[i]) + (float)epsAbs * (float)s[i]);
+          const float dF = fabsf((float)epsRel * fabsf(ynf) + (float)epsAbs * (float)s[i]);
           if (errF * dMaxF > errMaxF * dF || !(errF == errF)) {
             errMaxF = errF;
             dMaxF = dF;
@@ -841,7 +844,10 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
           // Accept.
 #pragma unroll
           for (int i = 0; i < GAL_NY; ++i) y[i] = ynew[i];
-          sync_yr();
+          if constexpr (FAST) {
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) yf[i] = x[i];
+          }
           t = tNew;
           h = hNew;
           ++nAcc;

@@ -312,6 +312,10 @@ int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const 
 
 int gal_gpu_forest_evolve(gal_ctx* ctx, gal_forest_dev* f) {
   if (!ctx || !f) return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_evolve: NULL argument%s");
+  if (ctx_mode(ctx) == MODE_SURROGATE)
+    return fail(ctx, GAL_ERR_ARGUMENT,
+                "gal_gpu_forest_evolve: forests are built for the FP64 form, the FP32-rate form and the FP32-rate "
+                "form with the surrogate; with a surrogate installed, set GAL_RATES_FP32%s");
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return fail(ctx, GAL_ERR_CUDA, "CUDA error: %s", cudaGetErrorString(e));
   int rc = ensure_graph(ctx, f);

@@ -449,8 +449,12 @@ __device__ __forceinline__ void rhs(const Globals& G, const Smem& S, const NodeC
 
 // Post-step clamps of the standard components (hot_halo/standard/_class.F90:
 // 455-530, disk/standard/_class.F90:473-677, spheroid/standard/_class.F90:
-// 464-636); all return GSL_Continue, so the evolver is not reset.
-__device__ __forceinline__ void post_step(double* y) {
+// 464-636); all return GSL_Continue, so the evolver is not reset.  Returns
+// whether any value was changed.
+__device__ __forceinline__ bool post_step(double* y) {
+  const bool any = y[GAL_Y_HOT_MASS] < 0.0 || y[GAL_Y_DISK_GAS] < 0.0 || y[GAL_Y_DISK_STARS] < 0.0 ||
+                   y[GAL_Y_SPHEROID_GAS] < 0.0 || y[GAL_Y_SPHEROID_STARS] < 0.0;
+  if (!any) return false;
   if (y[GAL_Y_HOT_MASS] < 0.0) y[GAL_Y_HOT_MASS] = 0.0;
   if (y[GAL_Y_DISK_GAS] < 0.0) {
     if (y[GAL_Y_DISK_GAS] + y[GAL_Y_DISK_STARS] == 0.0) {
@@ -480,6 +484,7 @@ __device__ __forceinline__ void post_step(double* y) {
     }
     y[GAL_Y_SPHEROID_STARS] = 0.0;
   }
+  return true;
 }
 
 // Absolute-tolerance scales from the initial state (scaleSetTask hooks of

@@ -8,13 +8,13 @@
  * come from the Cole et al. (2000) builder with the Parkinson, Cole & Helly
  * (2008) branching rates (merger_trees/construct/builder/Cole2000/
  * _class.F90:360-913, merger_trees/branching_probability/
- * Parkinson_Cole_Helly.F90:265-634).  gal_gpu_evolve_forest replaces the
+ * Parkinson_Cole_Helly.F90:265-634).  gal_gpu_forest_evolve replaces the
  * per-node evolve calls of one forest (mergerTreeNodeEvolver%evolve, called
  * from evolver/standard.F90:452 and threaded.F90:637) with one graph launch.
  *
- * Forest layout (caller-owned host arrays, n nodes): node 0 of each tree is
- * its root; the progenitors of every node are contiguous, primary (most
- * massive) first:
+ * Forest layout (caller-owned host arrays, n nodes; gal_forest_build puts
+ * each tree's root first): the progenitors of every node are contiguous,
+ * primary (most massive) first:
  *   parent[n]       index of the parent, -1 for a root
  *   child_first[n]  index of the first progenitor (any value if none)
  *   child_count[n]  number of progenitors
@@ -97,7 +97,9 @@ int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const 
                           const int32_t* child_count, const double* time, const double* mass, const double* spin,
                           const double* state0, int32_t n_outputs, const double* output_times, gal_forest_dev** out);
 /* Evolve the whole forest from state0 (one graph launch on the context
- * stream; asynchronous: gal_gpu_forest_sync waits). */
+ * stream; asynchronous: gal_gpu_forest_sync waits).  Available in the FP64
+ * form and the FP32-rate forms (with or without the surrogate); with a
+ * surrogate and FP64 rates it returns GAL_ERR_ARGUMENT. */
 int gal_gpu_forest_evolve(gal_ctx* ctx, gal_forest_dev* f);
 int gal_gpu_forest_sync(gal_ctx* ctx, gal_forest_dev* f);
 /* Results of the last evolution:

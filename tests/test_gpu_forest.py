@@ -194,3 +194,19 @@ def test_small_cpu_configuration(table, oracle_mod):
     assert np.all(np.abs(state - ref) <= bound), _worst(state, ref, bound)
     fe.close()
     ev.close()
+
+
+def test_forest_needs_a_built_form(params, table, trained):
+    """A surrogate with FP64 rates has no forest kernel: a clear error, and
+    the context stays usable once the rates are FP32."""
+    ev = _evolver(params, table, "fp64")
+    trained.install(ev)
+    f = forest.build(params, n_trees=2, seed=2, root_mass_min=1e10, root_mass_max=1e10)
+    fe = forest.ForestEvolver(ev, f, forest.initial_state(params, f), forest.output_times(params))
+    with pytest.raises(RuntimeError, match="FP32"):
+        fe.evolve()
+    ev.set_rate_precision("fp32")
+    fe.evolve()
+    assert np.all(fe.results(snapshots=False)[1] == 0)
+    fe.close()
+    ev.close()
