@@ -189,13 +189,13 @@ __device__ __forceinline__ CoolingValuesF surrogate_cooling(const Globals& G, co
     // n_e/n_H: bilinear interpolation of the log table in FP32.
     int iZ;
     float hZ;
-    if (G.firstZero && zs < (float)G.firstNonZero) {
+    if (G.firstZero && zs < G.f.firstNonZero) {
       iZ = 0;
-      hZ = zs * (float)G.invFirstNonZero;
+      hZ = zs * G.f.invFirstNonZero;
     } else {
       const float lnZ = lz * 2.302585093f;
       const int last = G.nZ - 2;
-      int j = G.zFirstLog + (int)floorf((lnZ - (float)G.lnZFirst) * (float)G.invDlnZ);
+      int j = G.zFirstLog + (int)floorf((lnZ - G.f.lnZFirst) * G.f.invDlnZ);
       j = min(max(j, G.zFirstLog), last);
       iZ = j;
       hZ = fminf(fmaxf((lnZ - (float)lnZTab[j]) * (float)invDlnZTab[j], 0.0f), 1.0f);
@@ -273,6 +273,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
 
   const int64_t n = b.n;
   const double epsAbs = G.p.ode_tolerance_absolute, epsRel = G.p.ode_tolerance_relative;
+  const float epsAbsF = (float)epsAbs, epsRelF = (float)epsRel;
   const uint32_t budget = (uint32_t)max(G.p.step_budget, 0);
 
   int phase = PH_NEED;
@@ -283,7 +284,11 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
   // the stage arguments x are FP64 or FP32 with the rates.
   // In the FP64 forms yr is y itself and ynew shares the stage argument
   // array x, so those forms keep the register footprint of a plain stepper.
-  double y[GAL_NY], s[GAL_NY];
+  // The tolerance scales s are FP64 in the FP64 forms; in the FP32-rate
+  // forms they are kept in FP32 (coarse scales: 1e-3 of the halo mass and
+  // the like) and the picked component's D is formed in FP64 from them.
+  double y[GAL_NY];
+  RateT s[GAL_NY];
   RateT k1[GAL_NY], k2[GAL_NY], k3[GAL_NY], k4[GAL_NY], k5[GAL_NY], k6[GAL_NY], x[GAL_NY];
   float yf[GAL_NY];
   double ynewF[GAL_NY];
@@ -325,6 +330,13 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
   };
   // Whether the warp must enter a right-hand-side evaluation.
   auto any = [&](bool p) { return SURR ? __any_sync(FULL, p) : p; };
+  // Absolute-tolerance scales of the current evolve call.
+  auto set_scales = [&]() {
+    double sd[GAL_NY];
+    scales(y, c.massHalo, sd);
+#pragma unroll
+    for (int v = 0; v < GAL_NY; ++v) s[v] = (RateT)sd[v];
+  };
   // The FP32 copy of y in the FAST forms.
   auto sync_yr = [&]() {
     if constexpr (FAST) {
@@ -345,7 +357,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
     if constexpr (FAST) cf = node_fast(c);
 #pragma unroll
     for (int v = 0; v < GAL_NY; ++v) F.state[v * F.n + node] = y[v];
-    scales(y, c.massHalo, s);
+    set_scales();
     t0 = F.segT0[seg];
     t1 = F.segT1[seg];
     trial = 0;
@@ -431,7 +443,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       if constexpr (FAST) cf = node_fast(c);
 #pragma unroll
       for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
-      scales(y, c.massHalo, s);
+      set_scales();
       t0 = b.tStart[node];
       t1 = b.tEnd[node];
       stepIn = b.step[node];
@@ -797,7 +809,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
           const float ynf = (float)ynew[i];
           if constexpr (FAST) x[i] = ynf;
           const float errF = fabsf((float)hr * (float)est);
-          const float dF = fabsf((float)epsRel * fabsf(ynf) + (float)epsAbs * (float)s[i]);
+          const float dF = fabsf(epsRelF * fabsf(ynf) + epsAbsF * (float)s[i]);
           if (errF * dMaxF > errMaxF * dF || !(errF == errF)) {
             errMaxF = errF;
             dMaxF = dF;

@@ -270,6 +270,7 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
   for (int j = 0; j + 1 < nZ; ++j) lnZ[nZ + j] = 1.0 / (lnZ[j + 1] - lnZ[j]);
   g.invFirstNonZero = 1.0 / g.firstNonZero;
   set_uniform_metallicity_grid(g, lnZ.data(), nZ);
+  fill_fast_constants(g);
   for (int i = 0; i < nZ * nT; ++i) tab[i] = make_double2(std::log(t->cooling_rate[i]), std::log(t->electron_density[i]));
   std::vector<float2> tabF(tab.size());
   std::vector<float> lnZF(2 * nZ);
@@ -607,6 +608,7 @@ extern "C" int gal_gpu_evolve_batch_noalloc(const gal_params* p, const gal_cie_t
   g.bhRadiusSpheroidCoef = k::gravitationalConstantInternal / (cs * cs);
   g.coolingCoef = p->cooling_degrees_of_freedom / 2.0 * k::boltzmannsConstant / k::ergs / k::gigaYear / k::densityToHydrogenNumber;
   g.accretionFraction = p->omega_baryon / p->omega_matter;
+  fill_fast_constants(g);
 
   cudaStream_t st = (cudaStream_t)stream;
   int sms = 0;

@@ -66,7 +66,35 @@ struct Globals {
   double bhRadiusSpheroidCoef;  // G / c_s^2
   double coolingCoef;         // (dof/2) k_B / ergs / Gyr / densityToHydrogenNumber
   double accretionFraction;   // Omega_b / Omega_m
+  // FP32 copies for the FP32-rate forms, derived once on the host
+  // (fill_fast_constants) so that no rate evaluation converts or divides in FP64.
+  struct Fast {
+    float oneMinusR, metalYield;
+    float eddingtonOverEps;   // eddingtonPerMass / epsilon_radiative (0: no Eddington cap)
+    float bhRetained;         // 1 - epsilon_radiative - epsilon_jet
+    float bhRadiusSpheroidCoef, jeansPrefactor, bhSpheroidCoef;
+    float Zmin, Zmax, firstNonZero, invFirstNonZero, lnZFirst, invDlnZ;
+    int capped;               // epsilon_radiative > 0
+  } f;
 };
+
+// Fill Globals::f from the FP64 constants (host).
+inline void fill_fast_constants(Globals& g) {
+  g.f.oneMinusR = (float)(1.0 - g.p.recycled_fraction);
+  g.f.metalYield = (float)g.p.metal_yield;
+  g.f.capped = g.p.bh_efficiency_radiative > 0.0;
+  g.f.eddingtonOverEps = g.f.capped ? (float)(k::eddingtonPerMass / g.p.bh_efficiency_radiative) : 0.0f;
+  g.f.bhRetained = (float)(1.0 - g.p.bh_efficiency_radiative - g.p.bh_efficiency_jet);
+  g.f.bhRadiusSpheroidCoef = (float)g.bhRadiusSpheroidCoef;
+  g.f.jeansPrefactor = (float)g.jeansPrefactor;
+  g.f.bhSpheroidCoef = (float)g.bhSpheroidCoef;
+  g.f.Zmin = (float)g.Zmin;
+  g.f.Zmax = (float)g.Zmax;
+  g.f.firstNonZero = (float)g.firstNonZero;
+  g.f.invFirstNonZero = (float)g.invFirstNonZero;
+  g.f.lnZFirst = (float)g.lnZFirst;
+  g.f.invDlnZ = (float)g.invDlnZ;
+}
 
 // Per-node constants of one evolve call.  Reciprocals of the per-node
 // lengths and times are taken here once, so that the right-hand side

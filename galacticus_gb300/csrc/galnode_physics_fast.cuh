@@ -95,18 +95,18 @@ struct CoolingValuesF {
 // interpolation of the logs, exp.
 __device__ __forceinline__ void cie_lookup_fast(const Globals& G, const SmemF& S, const NodeF& c, float zSolar, float& lambda,
                                                float& electrons) {
-  zSolar = fminf(fmaxf(zSolar, (float)G.Zmin), (float)G.Zmax);  // "fix" extrapolation in metallicity
+  zSolar = fminf(fmaxf(zSolar, G.f.Zmin), G.f.Zmax);  // "fix" extrapolation in metallicity
   const float zUse = fmaxf(zSolar, 0.0f);
   int iZ;
   float hZ;
-  if (G.firstZero && zUse < (float)G.firstNonZero) {
+  if (G.firstZero && zUse < G.f.firstNonZero) {
     iZ = 0;
-    hZ = zUse * (float)G.invFirstNonZero;
+    hZ = zUse * G.f.invFirstNonZero;
   } else {
     const float lnZ = __logf(zUse);
     const int last = G.nZ - 2;
     if (G.zUniform) {
-      int j = G.zFirstLog + (int)floorf((lnZ - (float)G.lnZFirst) * (float)G.invDlnZ);
+      int j = G.zFirstLog + (int)floorf((lnZ - G.f.lnZFirst) * G.f.invDlnZ);
       iZ = j < G.zFirstLog ? G.zFirstLog : (j > last ? last : j);
     } else {
       int lo = G.zFirstLog, hi = G.nZ - 1;
@@ -151,7 +151,8 @@ __device__ __forceinline__ float cooling_radius_fast(const Globals& G, const Sme
   const float q = massHot > 0.0f ? __fdividef(num, den) : 0.0f;
   if (q > c.onePlusXOuter2) return c.rOuter;
   if (q < 1.0f) return 0.0f;
-  return c.rcore * sqrtf(q - 1.0f);
+  const float q1 = q - 1.0f;
+  return c.rcore * (q1 * rsqrtf(q1));  // sqrt by the hardware reciprocal square root (~2 ulp)
 }
 
 __device__ __forceinline__ float mass_fraction_f(float metals, float mass, float invMass) {
@@ -166,10 +167,11 @@ __device__ __forceinline__ void rhs_fast(const Globals& G, const SmemF& S, const
   const uint32_t ph = p.physics;
 #pragma unroll
   for (int i = 0; i < GAL_NY; ++i) dydt[i] = 0.0f;
-  const float oneMinusR = (float)(1.0 - p.recycled_fraction), yield = (float)p.metal_yield;
+  const float oneMinusR = G.f.oneMinusR, yield = G.f.metalYield;
   const float massHot = y[GAL_Y_HOT_MASS], metalsHot = y[GAL_Y_HOT_METALS];
   const float gasDisk = y[GAL_Y_DISK_GAS], gasSph = y[GAL_Y_SPHEROID_GAS];
-  const float invHot = massHot > 0.0f ? __frcp_rn(massHot) : 0.0f;
+  // Reciprocals by the hardware approximation (~1 ulp): these are FP32 rates.
+  const float invHot = massHot > 0.0f ? __fdividef(1.0f, massHot) : 0.0f;
   const float zHot = mass_fraction_f(metalsHot, massHot, invHot);
   bool coolingRadiusKnown = false;
   float rCool = 0.0f;
@@ -178,7 +180,7 @@ __device__ __forceinline__ void rhs_fast(const Globals& G, const SmemF& S, const
   // (stellar_populations/properties/instantaneous.F90:133-219).
   const bool diskOk = !(c.radiusDisk < 0.0f || gasDisk < 0.0f);
   const float sfrDisk = diskOk ? gasDisk * c.sfrDisk : 0.0f;
-  const float zDisk = mass_fraction_f(y[GAL_Y_DISK_GAS_METALS], gasDisk, gasDisk > 0.0f ? __frcp_rn(gasDisk) : 0.0f);
+  const float zDisk = mass_fraction_f(y[GAL_Y_DISK_GAS_METALS], gasDisk, gasDisk > 0.0f ? __fdividef(1.0f, gasDisk) : 0.0f);
   if ((ph & GAL_PHYS_STAR_FORMATION_DISK) && diskOk) {
     const float rateStars = oneMinusR * sfrDisk;
     const float rateMetals = zDisk * rateStars;
@@ -190,7 +192,7 @@ __device__ __forceinline__ void rhs_fast(const Globals& G, const SmemF& S, const
   // starFormationSpheroids (star_formation/spheroids.F90:152-)
   const bool sphOk = !(c.aSph < 1.0e-12f || gasSph < 1.0e-6f);
   const float sfrSph = sphOk ? gasSph * c.sfrSph : 0.0f;
-  const float invSph = gasSph > 0.0f ? __frcp_rn(gasSph) : 0.0f;
+  const float invSph = gasSph > 0.0f ? __fdividef(1.0f, gasSph) : 0.0f;
   const float zSph = mass_fraction_f(y[GAL_Y_SPHEROID_GAS_METALS], gasSph, invSph);
   if ((ph & GAL_PHYS_STAR_FORMATION_SPHEROID) && sphOk) {
     const float rateStars = oneMinusR * sfrSph;
@@ -226,23 +228,22 @@ __device__ __forceinline__ void rhs_fast(const Globals& G, const SmemF& S, const
   // blackHoleAccretionRateStandard (black_holes/accretion_rates/standard.F90:221-440).
   const float massBH = y[GAL_Y_BLACK_HOLE];
   if ((ph & GAL_PHYS_BLACK_HOLE_ACCRETION) && massBH > 0.0f) {
-    const double epsD = p.bh_efficiency_radiative;
-    const bool capped = epsD > 0.0;
-    const float eddingtonCap = capped ? (float)(k::eddingtonPerMass / epsD) * massBH : 0.0f;
+    const bool capped = G.f.capped;
+    const float eddingtonCap = G.f.eddingtonOverEps * massBH;
     float rateSph = 0.0f;
     if (gasSph > 0.0f && c.aSph > 0.0f) {
       // Bondi-Hoyle from the spheroid gas (Hernquist density at max(r_BHL, Jeans length)).
-      const float rAcc = fmaxf((float)G.bhRadiusSpheroidCoef * massBH, 0.0f);
+      const float rAcc = fmaxf(G.f.bhRadiusSpheroidCoef * massBH, 0.0f);
       float xx = rAcc * c.invASph, opx = 1.0f + xx;
       float rho = __fdividef(gasSph * c.rhoSphPerMass, xx * opx * opx * opx);
       if (rho > 1.0f) {
-        const float jeans = fminf((float)G.jeansPrefactor * rsqrtf(rho), c.aSph);
+        const float jeans = fminf(G.f.jeansPrefactor * rsqrtf(rho), c.aSph);
         if (jeans > rAcc) {
           xx = jeans * c.invASph;
           opx = 1.0f + xx;
           rho = __fdividef(gasSph * c.rhoSphPerMass, xx * opx * opx * opx);
         }
-        rateSph = fmaxf((float)G.bhSpheroidCoef * massBH * massBH * rho, 0.0f);
+        rateSph = fmaxf(G.f.bhSpheroidCoef * massBH * massBH * rho, 0.0f);
         if (capped) rateSph = fminf(rateSph, eddingtonCap);
       }
     }
@@ -274,7 +275,7 @@ __device__ __forceinline__ void rhs_fast(const Globals& G, const SmemF& S, const
     }
     const float total = rateSph + rateHot;
     if (total > 0.0f) {
-      dydt[GAL_Y_BLACK_HOLE] += total * (float)(1.0 - p.bh_efficiency_radiative - p.bh_efficiency_jet);
+      dydt[GAL_Y_BLACK_HOLE] += total * G.f.bhRetained;
       // spheroid gas sink (spheroid/standard/_class.F90:638-671)
       if (rateSph != 0.0f && gasSph > 0.0f && gasSph + y[GAL_Y_SPHEROID_STARS] > 0.0f) {
         dydt[GAL_Y_SPHEROID_GAS] += -rateSph;
