@@ -796,28 +796,37 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
         // FP64 error and the FP64 D_i.  (Picking at FP32 precision can only
         // exchange two components whose ratios agree to ~1e-7.)
         float errMaxF = 0.0f, dMaxF = 1.0f;
-        RateT estSel = (RateT)0;
+        RateT estSel = (RateT)0, incSel = (RateT)0;
         double ySel = 0.0, sSel = 1.0;
 #pragma unroll
         for (int i = 0; i < GAL_NY; ++i) {
           const RateT inc = (RateT)ck::c1 * k1[i] + (RateT)ck::c3 * k3[i] + (RateT)ck::c4 * k4[i] + (RateT)ck::c6 * k6[i];
           const RateT est = (RateT)ck::e1 * k1[i] + (RateT)ck::e3 * k3[i] + (RateT)ck::e4 * k4[i] + (RateT)ck::e5 * k5[i] +
                             (RateT)ck::e6 * k6[i];
-          ynew[i] = y[i] + hh * (double)inc;
-          // (float)ynew: the FP32 state copy if the step is accepted (kept in
-          // the free stage-argument array of the FP32 forms).
-          const float ynf = (float)ynew[i];
-          if constexpr (FAST) x[i] = ynf;
+          float ynf;
+          if constexpr (FAST) {
+            // The FP64 new state is formed only for the picked component and,
+            // on acceptance, for all of them: here an FP32 estimate of it
+            // serves the D_i of the pick, and the increment is kept (in the
+            // free stage-argument array) for the update.
+            x[i] = inc;
+            ynf = yf[i] + hr * inc;
+          } else {
+            ynew[i] = y[i] + hh * (double)inc;
+            ynf = (float)ynew[i];
+          }
           const float errF = fabsf((float)hr * (float)est);
           const float dF = fabsf(epsRelF * fabsf(ynf) + epsAbsF * (float)s[i]);
           if (errF * dMaxF > errMaxF * dF || !(errF == errF)) {
             errMaxF = errF;
             dMaxF = dF;
             estSel = est;
-            ySel = ynew[i];
+            incSel = inc;
+            ySel = FAST ? y[i] : ynew[i];
             sSel = s[i];
           }
         }
+        if constexpr (FAST) ySel += hh * (double)incSel;  // the picked component's new state, FP64
         // With nothing picked (every error zero) the ratio is 0, as in FP64.
         const double errMax = fabs(hh * (double)estSel);
         const double dMax = fabs(epsRel * fabs(ySel) + epsAbs * sSel);
@@ -854,11 +863,15 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
           }
         } else {
           // Accept.
-#pragma unroll
-          for (int i = 0; i < GAL_NY; ++i) y[i] = ynew[i];
           if constexpr (FAST) {
 #pragma unroll
-            for (int i = 0; i < GAL_NY; ++i) yf[i] = x[i];
+            for (int i = 0; i < GAL_NY; ++i) {
+              y[i] += hh * (double)x[i];
+              yf[i] = (float)y[i];
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) y[i] = ynew[i];
           }
           t = tNew;
           h = hNew;
