@@ -330,12 +330,29 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
   };
   // Whether the warp must enter a right-hand-side evaluation.
   auto any = [&](bool p) { return SURR ? __any_sync(FULL, p) : p; };
+  // Per-node constants of the current evolve call (FP32 in the FP32-rate
+  // forms, where the FP64 ones would only be rounded to FP32).
+  auto setup = [&](const double* prm) {
+    if constexpr (FAST) {
+      node_setup_fast(G, sLnT, prm, cf);
+      c.massHalo = prm[GAL_P_MASS];
+    } else {
+      node_setup(G, sLnT, prm, c);
+    }
+  };
   // Absolute-tolerance scales of the current evolve call.
   auto set_scales = [&]() {
-    double sd[GAL_NY];
-    scales(y, c.massHalo, sd);
+    if constexpr (FAST) {
+      float yv[GAL_NY];
 #pragma unroll
-    for (int v = 0; v < GAL_NY; ++v) s[v] = (RateT)sd[v];
+      for (int v = 0; v < GAL_NY; ++v) yv[v] = (float)y[v];
+      scales_fast(yv, (float)c.massHalo, s);
+    } else {
+      double sd[GAL_NY];
+      scales(y, c.massHalo, sd);
+#pragma unroll
+      for (int v = 0; v < GAL_NY; ++v) s[v] = (RateT)sd[v];
+    }
   };
   // The FP32 copy of y in the FAST forms.
   auto sync_yr = [&]() {
@@ -353,8 +370,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
     double prm[GAL_NP];
 #pragma unroll
     for (int v = 0; v < GAL_NP; ++v) prm[v] = F.segParam[v * F.nSeg + seg];
-    node_setup(G, sLnT, prm, c);
-    if constexpr (FAST) cf = node_fast(c);
+    setup(prm);
 #pragma unroll
     for (int v = 0; v < GAL_NY; ++v) F.state[v * F.n + node] = y[v];
     set_scales();
@@ -439,8 +455,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       double prm[GAL_NP];
 #pragma unroll
       for (int v = 0; v < GAL_NP; ++v) prm[v] = b.param[v * n + node];
-      node_setup(G, sLnT, prm, c);
-      if constexpr (FAST) cf = node_fast(c);
+      setup(prm);
 #pragma unroll
       for (int v = 0; v < GAL_NY; ++v) y[v] = b.state[v * n + node];
       set_scales();

@@ -94,6 +94,18 @@ void set_uniform_metallicity_grid(Globals& g, const double* lnZ, int nZ) {
   g.zUniform = 1;
 }
 
+// The same for the temperature rows (the Cloudy grid is evenly spaced in
+// log T), for the FP32 node setup of the FP32-rate forms.
+void set_uniform_temperature_grid(Globals& g, const double* lnT, int nT) {
+  g.tUniform = 0;
+  const double d = (lnT[nT - 1] - lnT[0]) / (nT - 1);
+  for (int i = 0; i + 1 < nT; ++i)
+    if (std::fabs(lnT[i + 1] - lnT[i] - d) > 1.0e-9 * std::fabs(d)) return;
+  g.f.lnTFirst = (float)lnT[0];
+  g.f.invDlnT = (float)(1.0 / d);
+  g.tUniform = 1;
+}
+
 }  // namespace
 
 namespace gal {
@@ -271,6 +283,7 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
   g.invFirstNonZero = 1.0 / g.firstNonZero;
   set_uniform_metallicity_grid(g, lnZ.data(), nZ);
   fill_fast_constants(g);
+  set_uniform_temperature_grid(g, lnT.data(), nT);
   for (int i = 0; i < nZ * nT; ++i) tab[i] = make_double2(std::log(t->cooling_rate[i]), std::log(t->electron_density[i]));
   std::vector<float2> tabF(tab.size());
   std::vector<float> lnZF(2 * nZ);

@@ -9,6 +9,7 @@
 // Galacticus repository root).
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include "../../include/galnode.h"
 #include "galnode_fastmath.cuh"
@@ -75,7 +76,28 @@ struct Globals {
     float bhRadiusSpheroidCoef, jeansPrefactor, bhSpheroidCoef;
     float Zmin, Zmax, firstNonZero, invFirstNonZero, lnZFirst, invDlnZ;
     int capped;               // epsilon_radiative > 0
+    // Coefficients of node_setup_fast(): every per-node constant is one of
+    // these times powers of r_vir, V_vir and the spin.
+    float tempPerV2;          // T_vir / V_vir^2 (K s^2 km^-2)
+    float tdynCoef;           // MpcPerKmPerSToGyr
+    float coreFraction;       // r_core / r_vir
+    float rho0Norm;           // 1/(4 pi (x - atan x)), x = r_vir/r_core
+    float twoPiRho0Norm;      // 2 pi rho0Norm
+    float onePlusXOuter2;     // 1 + x^2
+    float Tmin, Tmax;         // table temperature range ("extrapolate" = clamp)
+    float lnTFirst, invDlnT;  // ln T of the first row, reciprocal spacing (tUniform)
+    float coolingCoef;        // Globals::coolingCoef
+    float radiusFactorDisk, radiusFactorSpheroid;
+    float csSquaredPerT;      // c_s^2 / T of the primordial gas (km^2 s^-2 K^-1)
+    float gravitationalConstant;  // G in Mpc (km/s)^2 / Msun
+    float bhHotPrefactor;     // enhancement (hot halo) * Bondi-Hoyle-Lyttleton prefactor
+    float accretionFraction;  // Omega_b / Omega_m
+    float reincorporationMultiplier;
+    float invTwoPi;
+    struct Sf { float fixed, efficiency, exponent, minimum; } sfDisk, sfSph;
+    struct Out { float fraction, velocity, exponent, fractionalMinimum; } outDisk, outSph;
   } f;
+  int tUniform;               // temperature rows evenly spaced in ln T: cell by arithmetic
 };
 
 // Fill Globals::f from the FP64 constants (host).
@@ -94,6 +116,37 @@ inline void fill_fast_constants(Globals& g) {
   g.f.invFirstNonZero = (float)g.invFirstNonZero;
   g.f.lnZFirst = (float)g.lnZFirst;
   g.f.invDlnZ = (float)g.invDlnZ;
+  // node_setup() with r_vir, V_vir and the spin factored out.
+  g.f.tempPerV2 = (float)(0.5 * k::atomicMassUnit * k::meanAtomicMassPrimordial * k::kilo * k::kilo / k::boltzmannsConstant);
+  g.f.tdynCoef = (float)k::MpcPerKmPerSToGyr;
+  g.f.coreFraction = (float)g.p.core_radius_fraction;
+  const double x = 1.0 / g.p.core_radius_fraction;
+  const double norm = x < 1.0e-6 ? 3.0 / (x * x * x) + 9.0 / 5.0 / x - 36.0 * x / 175.0 : 1.0 / (x - std::atan(x));
+  g.f.rho0Norm = (float)(norm / (4.0 * k::Pi));
+  g.f.twoPiRho0Norm = (float)(2.0 * k::Pi * norm / (4.0 * k::Pi));
+  g.f.onePlusXOuter2 = (float)(1.0 + x * x);
+  g.f.Tmin = (float)g.Tmin;
+  g.f.Tmax = (float)g.Tmax;
+  g.f.coolingCoef = (float)g.coolingCoef;
+  g.f.radiusFactorDisk = (float)g.p.radius_factor_disk;
+  g.f.radiusFactorSpheroid = (float)g.p.radius_factor_spheroid;
+  g.f.csSquaredPerT = (float)(5.0 * k::boltzmannsConstant / 3.0 / k::meanAtomicMassPrimordial / k::atomicMassUnit / (k::kilo * k::kilo));
+  g.f.gravitationalConstant = (float)k::gravitationalConstantInternal;
+  g.f.bhHotPrefactor = (float)(g.p.bh_enhancement_hot_halo * k::bhlPrefactor);
+  g.f.accretionFraction = (float)g.accretionFraction;
+  g.f.reincorporationMultiplier = (float)g.p.reincorporation_multiplier;
+  g.f.invTwoPi = (float)(1.0 / (2.0 * k::Pi));
+  auto sf = [](const gal_star_formation& s) {
+    return Globals::Fast::Sf{(float)s.timescale_fixed, (float)s.efficiency, (float)s.exponent_velocity, (float)s.timescale_minimum};
+  };
+  auto out = [](const gal_outflow& o) {
+    return Globals::Fast::Out{(float)o.fraction, (float)o.velocity_characteristic, (float)o.exponent,
+                              (float)o.timescale_fractional_minimum};
+  };
+  g.f.sfDisk = sf(g.p.sf_disk);
+  g.f.sfSph = sf(g.p.sf_spheroid);
+  g.f.outDisk = out(g.p.outflow_disk);
+  g.f.outSph = out(g.p.outflow_spheroid);
 }
 
 // Per-node constants of one evolve call.  Reciprocals of the per-node

@@ -14,16 +14,16 @@
 //
 // Every branch restates the same reference function as the FP64 rhs() in
 // galnode_physics.cuh (same operators, same order, same clamps); the
-// constants are the per-node constants of node_setup() rounded to FP32,
-// grouped so that no intermediate leaves the FP32 range for halo masses of
-// 1e6-1e16 Msun.
+// constants are the per-node constants of node_setup(), formed in FP32 by
+// node_setup_fast() and grouped so that no intermediate leaves the FP32
+// range for halo masses of 1e6-1e16 Msun.
 #pragma once
 
 #include "galnode_physics.cuh"
 
 namespace gal {
 
-// FP32 copies of the per-node constants of NodeC.
+// The per-node constants of NodeC in FP32 (node_setup_fast()).
 struct NodeF {
   float tdyn, invTdyn;
   float rcore, invRcore;
@@ -43,38 +43,113 @@ struct NodeF {
   float accretionRate, reincorporationRate;
 };
 
-__device__ __forceinline__ NodeF node_fast(const NodeC& c) {
-  NodeF f;
-  f.tdyn = (float)c.tdyn;
-  f.invTdyn = (float)c.invTdyn;
-  f.rcore = (float)c.rcore;
-  f.invRcore = (float)c.invRcore;
-  f.rho0PerMass = (float)c.rho0PerMass;
-  f.rOuter = (float)c.rOuter;
-  f.invRvir = (float)c.invRvir;
-  f.onePlusXOuter2 = (float)c.onePlusXOuter2;
-  f.coolingQCoef = (float)(c.tdyn * c.rho0PerMass / c.coolingTimeCoef);
-  f.coolingRateCoef = (float)c.coolingRateCoef;
-  f.hT = (float)c.hT;
-  f.iT = c.iT;
-  f.coolingAllowed = c.coolingAllowed;
-  f.log10T = c.log10T;
-  f.sfrDisk = (float)c.sfrDisk;
-  f.sfrSph = (float)c.sfrSph;
-  f.outDisk = (float)c.outDisk;
-  f.outSph = (float)c.outSph;
-  f.outDiskMax = (float)c.outDiskMax;
-  f.outSphMax = (float)c.outSphMax;
-  f.aSph = (float)c.aSph;
-  f.invASph = (float)c.invASph;
-  f.rhoSphPerMass = (float)c.rhoSphPerMass;
-  f.radiusDisk = (float)c.radiusDisk;
-  f.bhRadiusHotCoef = (float)c.bhRadiusHotCoef;
-  f.bhHotCoef = (float)c.bhHotCoef;
-  f.bhHotMaxCoef = (float)c.bhHotMaxCoef;
-  f.accretionRate = (float)c.accretionRate;
-  f.reincorporationRate = (float)c.reincorporationRate;
-  return f;
+// node_setup() for the FP32-rate forms: the same constants (same reference
+// functions, same guards), formed in FP32 from r_vir, V_vir, the spin and
+// the host-folded coefficients of Globals::Fast, so that setting up a node
+// issues no FP64 division, logarithm or power.  Its values agree with the
+// FP64 node_setup() rounded to FP32 to a few FP32 ulps (the powers to ~1e-6
+// relative), far inside the rates' own FP32 rounding against the tolerance.
+// The T cell is found by arithmetic when the table rows are evenly spaced
+// in ln T.
+__device__ __forceinline__ void node_setup_fast(const Globals& G, const double* sLnT, const double* prm, NodeF& f) {
+  const Globals::Fast& g = G.f;
+  const gal_params& p = G.p;
+  const double vvirD = prm[GAL_P_VELOCITY_VIRIAL];
+  const float rvir = (float)prm[GAL_P_RADIUS_VIRIAL], vvir = (float)vvirD, spin = (float)prm[GAL_P_SPIN];
+  const double mdot = prm[GAL_P_MASS_RATE];
+  // virialDensityContrastDefinition{VirialTemperature,DynamicalTimescale} (virial_density_contrast.F90:195-262)
+  const float T = g.tempPerV2 * vvir * vvir;
+  f.tdyn = g.tdynCoef * rvir / vvir;
+  f.invTdyn = 1.0f / f.tdyn;
+  const float rcore = g.coreFraction * rvir;
+  f.rcore = rcore;
+  f.invRcore = 1.0f / rcore;
+  f.rOuter = rvir;  // hot_halo/standard/_class.F90:430-450
+  f.invRvir = 1.0f / rvir;
+  // beta-profile normalisation (beta_profile.F90:190-320): r_outer/r_core is the same for every node.
+  f.rho0PerMass = g.rho0Norm / (rcore * rcore * rcore);
+  f.onePlusXOuter2 = g.onePlusXOuter2;
+  f.coolingRateCoef = g.twoPiRho0Norm / rcore * f.invTdyn;
+  f.coolingQCoef = f.tdyn * f.rho0PerMass / (g.coolingCoef * T);
+  // Temperature coordinate of the CIE tables ("extrapolate" in T = clamp).
+  const float lnT = logf(fminf(fmaxf(T, g.Tmin), g.Tmax));
+  const int last = G.nT - 2;
+  if (G.tUniform) {
+    const float u = (lnT - g.lnTFirst) * g.invDlnT;
+    int j = (int)floorf(u);
+    j = j < 0 ? 0 : (j > last ? last : j);
+    f.iT = j;
+    f.hT = u - (float)j;
+  } else {
+    int lo = 0, hi = G.nT - 1;
+    if (lnT >= (float)sLnT[hi]) lo = last;
+    else
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if ((float)sLnT[mid] <= lnT) lo = mid; else hi = mid;
+      }
+    f.iT = lo;
+    f.hT = (lnT - (float)sLnT[lo]) / ((float)sLnT[lo + 1] - (float)sLnT[lo]);
+  }
+  f.log10T = T > 0.0f ? log10f(T) : -1.0e30f;
+  f.coolingAllowed = !(vvirD > p.cooling_velocity_cutoff);
+  // galacticStructureSolverFixed: r = f lambda r_vir.
+  const float Rd = g.radiusFactorDisk * spin * rvir, Rs = g.radiusFactorSpheroid * spin * rvir;
+  f.radiusDisk = Rd;
+  f.aSph = Rs;
+  f.invASph = Rs > 0.0f ? 1.0f / Rs : 0.0f;
+  f.rhoSphPerMass = Rs > 0.0f ? g.invTwoPi / (Rs * Rs * Rs) : 0.0f;
+  // Star-formation timescales (star_formation/timescales/dynamical_time.F90:121-189).
+  auto timescale = [&](const gal_star_formation& sf, const Globals::Fast::Sf& s, float R) -> float {
+    if (sf.timescale_type == GAL_SF_TIMESCALE_FIXED) return s.fixed;
+    if (vvir <= 0.0f || s.efficiency == 0.0f) return 0.0f;
+    const float t = g.tdynCoef * R / vvir;
+    return fmaxf(t * powf(vvir * (1.0f / 200.0f), s.exponent) / s.efficiency, s.minimum);
+  };
+  const float tsD = timescale(p.sf_disk, g.sfDisk, Rd), tsS = timescale(p.sf_spheroid, g.sfSph, Rs);
+  f.sfrDisk = tsD > 0.0f ? 1.0f / tsD : 0.0f;
+  f.sfrSph = tsS > 0.0f ? 1.0f / tsS : 0.0f;
+  // Outflow loading (power_law/_class.F90:118-164, fixed.F90) and rateLimit (rate_limit.F90).
+  auto loading = [&](const gal_outflow& o, const Globals::Fast::Out& s) -> float {
+    if (o.type == GAL_OUTFLOW_FIXED) return s.fraction;
+    if (vvir <= 0.0f) return 0.0f;
+    return powf(s.velocity / vvir, s.exponent);
+  };
+  auto limit = [&](const Globals::Fast::Out& s, float R) -> float {
+    if (!(s.fractionalMinimum > 0.0f)) return -1.0f;
+    const float t = (vvir <= 0.0f || R <= 0.0f) ? 1.0f : g.tdynCoef * R / vvir;
+    return 1.0f / t / s.fractionalMinimum;
+  };
+  f.outDisk = loading(p.outflow_disk, g.outDisk);
+  f.outSph = loading(p.outflow_spheroid, g.outSph);
+  f.outDiskMax = limit(g.outDisk, Rd);
+  f.outSphMax = limit(g.outSph, Rs);
+  // Hot-halo Bondi accretion constants at the virial temperature.
+  const float cs2 = g.csSquaredPerT * T, cs = sqrtf(cs2);
+  f.bhRadiusHotCoef = T > 0.0f ? g.gravitationalConstant / cs2 : 0.0f;
+  f.bhHotCoef = g.bhHotPrefactor * cs;
+  f.bhHotMaxCoef = cs / (f.rOuter * g.tdynCoef);
+  f.accretionRate = mdot > 0.0 ? g.accretionFraction * (float)mdot : 0.0f;
+  f.reincorporationRate = g.reincorporationMultiplier * f.invTdyn;
+}
+
+// Absolute-tolerance scales of the components (scales() in FP32, from the
+// FP32 copy of the state): hot-halo and outflowed components 1e-3 of the
+// halo mass (hot_halo/standard/_class.F90:804-850), disk and spheroid
+// masses and metals from the galaxy's total (disk :735-824, spheroid
+// :804-897), the black hole from the seed and the spheroid (:195-257).
+__device__ __forceinline__ void scales_fast(const float* y, float massHalo, float* s) {
+  const float hot = massHalo * 1.0e-3f;
+  s[GAL_Y_HOT_MASS] = s[GAL_Y_HOT_METALS] = s[GAL_Y_OUTFLOWED_MASS] = s[GAL_Y_OUTFLOWED_METALS] = hot;
+  const float mass = fmaxf(fabsf(y[GAL_Y_DISK_GAS]) + fabsf(y[GAL_Y_SPHEROID_GAS]) + fabsf(y[GAL_Y_DISK_STARS]) +
+                               fabsf(y[GAL_Y_SPHEROID_STARS]), 1.0f);
+  const float metals = fmaxf(fabsf(y[GAL_Y_DISK_GAS_METALS]) + fabsf(y[GAL_Y_DISK_STARS_METALS]) +
+                                 fabsf(y[GAL_Y_SPHEROID_GAS_METALS]),
+                             fmaxf(mass * 1.0e-4f, 1.0f));
+  s[GAL_Y_DISK_GAS] = s[GAL_Y_DISK_STARS] = s[GAL_Y_SPHEROID_GAS] = s[GAL_Y_SPHEROID_STARS] = mass;
+  s[GAL_Y_DISK_GAS_METALS] = s[GAL_Y_DISK_STARS_METALS] = s[GAL_Y_SPHEROID_GAS_METALS] = metals;
+  const float stars = y[GAL_Y_SPHEROID_STARS] > 0.0f ? y[GAL_Y_SPHEROID_STARS] : 0.0f;
+  s[GAL_Y_BLACK_HOLE] = fmaxf(fmaxf(1.0f, 1.0e-4f * stars), y[GAL_Y_BLACK_HOLE]);
 }
 
 // FP32 copy of the CIE tables in shared memory: (ln Lambda, ln n_e/n_H)
