@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--workload", choices=["isolated", "scale"], default="isolated",
                     help="scale: the full chosen form on a forest at scale (one JSON line of its own)")
     ap.add_argument("--trees-scale", type=int, default=65536, help="trees of the scale workload")
+    ap.add_argument("--halo", type=int, default=-1,
+                    help="with a single --form: evolve only this halo of the batch (profiling the batch's tail)")
     return ap.parse_args()
 
 
@@ -396,8 +398,14 @@ def run_scale(args):
     nbytes = f.n * (2 * _abi.NY * 8 + 6 * 4 + 8) + out["snapshots"] * _abi.NY * 8
     for name, entry in out["forms"].items():
         achieved = f_rhs * entry["rhs_evaluations"] / entry["s_per_evolution"]
-        entry["roofline"] = {"fp64": {"achieved_tflops": achieved / 1e12, "peak_tflops": flops_peak.value / 1e12,
-                                      "frac": achieved / flops_peak.value},
+        # In the FP32-rate forms most of the reference's FP64 work runs on the
+        # FP32 pipe: the same ratio is then an FP64-equivalent rate and may
+        # exceed the FP64 peak.
+        key = "fp64" if name == "plain" else "fp64_equivalent"
+        entry["roofline"] = {key: {"achieved_tflops": achieved / 1e12, "peak_tflops": flops_peak.value / 1e12,
+                                   "frac": achieved / flops_peak.value,
+                                   "basis": "the reference's FP64 flops per RHS evaluation (counted by the oracle) "
+                                            "times the RHS evaluations, over the evolution time"},
                              "hbm": {"achieved_gbs": nbytes / entry["s_per_evolution"] / 1e9, "peak_gbs": peaks.get("hbm_gbs"),
                                      "frac": (nbytes / entry["s_per_evolution"] / 1e9 / peaks["hbm_gbs"]) if peaks.get("hbm_gbs") else None}}
     out["flops_per_rhs"] = f_rhs
@@ -431,11 +439,16 @@ def run_ours(args):
         ev.set_launch(128, 2 if ev is not forms["plain"] else 1)
     lib = forms["plain"].lib
     batch = workloads.isolated_halos(n=args.nodes, seed=2 + rank)
+    if args.halo >= 0:
+        if args.form == "compare" or args.form.startswith("trees-"):
+            raise SystemExit("--halo needs one batch form (--form plain, fast or surrogate)")
+        batch = batch.subset(np.array([args.halo]))
     n = batch.n
 
-    # The learned cooling surrogate: trained on this GPU by the library's own kernels.
+    # The learned cooling surrogate: trained on this GPU by the library's own
+    # kernels (not needed when one form without it is profiled alone).
     tt0 = time.perf_counter()
-    net = surrogate.train(table)
+    net = surrogate.train(table) if args.form in ("compare", "surrogate", "trees-surrogate") else None
     train_s = time.perf_counter() - tt0
 
     def dev_tensor(a, dtype=torch.float64):
@@ -677,7 +690,9 @@ def run_ours(args):
             "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": flops_peak.value / 1e12, "unit": "TFLOP/s",
                          "frac": achieved / flops_peak.value, "traffic": HEADLINE_DRAM_BYTES,
                          "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
-                         "basis": "the reference's FP64 work per node-timestep (counted by the oracle) over the surrogate-form kernel time",
+                         "basis": "the reference's FP64 work per node-timestep (counted by the oracle) over the surrogate-form "
+                                  "kernel time: an FP64-equivalent rate, since this form runs the rates on the FP32 pipe "
+                                  "and keeps FP64 for the state, error norm and step control",
                          "peak_source": "measured by gal_calibrate_fp64 (DFMA loop on all SMs); MEASURED_PEAKS.json has no FP64 figure",
                          "flops_per_node_timestep": f_step, "kernel_ms": k_ms,
                          "tensor": {"achieved": mlp_tflops, "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",

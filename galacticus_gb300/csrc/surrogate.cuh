@@ -7,8 +7,8 @@
 // network learns the temperature and metallicity dependence.
 //
 // Layers 2 and 3 (64 -> 64) run on the tensor cores (mma.sync m16n8k16,
-// BF16 x BF16 with FP32 accumulation; the warp's 32 nodes are two 16-row
-// tiles).  Each FP32 operand is split into a BF16 high part and a BF16
+// BF16 x BF16 with FP32 accumulation; the warp's nodes that need the
+// network are packed into one or two 16-row tiles).  Each FP32 operand is split into a BF16 high part and a BF16
 // remainder, v = hi + lo, and a product is taken as hi*hi + hi*lo + lo*hi
 // (three MMAs), which keeps about 16 significant bits -- plain BF16 operands
 // (8 bits) put up to 0.03 dex of rounding error on the output, three times
@@ -21,8 +21,8 @@
 // in shared memory.
 //
 // Every lane of the warp must call surrogate_eval together (mma.sync is a
-// warp-collective instruction); lanes without a node feed any finite input
-// and ignore the result.
+// warp-collective instruction); lanes outside `need` get no row and ignore
+// the result, and lanes in it must feed finite inputs.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -77,6 +77,13 @@ __device__ __forceinline__ SurrogateSmem surrogate_view(const float* small, cons
 }
 
 __device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
+
+// Lane of the (q+1)-th set bit of mask (q < popc(mask)): PTX fns.
+__device__ __forceinline__ int nth_set_lane(unsigned mask, int q) {
+  unsigned r;
+  asm("fns.b32 %0, %1, 0, %2;" : "=r"(r) : "r"(mask), "r"(q + 1));
+  return (int)r;
+}
 
 __device__ __forceinline__ uint32_t bf16_bits(__nv_bfloat162 v) { return *reinterpret_cast<const uint32_t*>(&v); }
 
@@ -141,16 +148,22 @@ __device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0
                                                unsigned need = 0xffffffffu) {
   const unsigned FULLMASK = 0xffffffffu;
   const int g = lane >> 2, t = lane & 3;
-  // Row `lane` of the warp is row (lane & 7) of half (lane >> 3) & 1 of
-  // tile lane >> 4; its sum ends up in lane 4 (lane & 7) of that tile's pass.
+  // The lanes in `need` are packed into consecutive rows in lane order, so
+  // that ceil(count/16) tiles run.  A row's output depends on its own inputs
+  // only, so a lane's result does not depend on which row it lands in.
+  // The lane of rank q is row (q & 7) of half (q >> 3) & 1 of tile q >> 4;
+  // its sum ends up in lane 4 (q & 7) of that tile's pass.
+  const int count = __popc(need);
+  const int rank = __popc(need & ((1u << lane) - 1u));
   float out = 0.0f;
-  const int src = 4 * (lane & 7);
+  const int src = 4 * (rank & 7);
   // The tiles are not unrolled: one copy of the network code (the kernel
   // that calls it is otherwise instruction-fetch bound).
 #pragma unroll 1
-  for (int mt = 0; mt < 2; ++mt) {
-    if (((need >> (16 * mt)) & 0xffffu) == 0u) continue;
-    const int r0 = mt * 16 + g, r1 = r0 + 8;
+  for (int mt = 0; mt < (count + 15) >> 4; ++mt) {
+    // Rows past the last needing lane take lane 0's inputs (finite; ignored).
+    const int q0 = mt * 16 + g, q1 = q0 + 8;
+    const int r0 = q0 < count ? nth_set_lane(need, q0) : 0, r1 = q1 < count ? nth_set_lane(need, q1) : 0;
     const float u0 = __shfl_sync(FULLMASK, x0, r0), u1 = __shfl_sync(FULLMASK, x1, r0), u2 = __shfl_sync(FULLMASK, x2, r0);
     const float v0 = __shfl_sync(FULLMASK, x0, r1), v1 = __shfl_sync(FULLMASK, x1, r1), v2 = __shfl_sync(FULLMASK, x2, r1);
     // Layer 1 (FP32) straight into layer 2's A fragments: for k-step ks the
@@ -196,7 +209,7 @@ __device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0
     p1 += __shfl_xor_sync(FULLMASK, p1, 1);
     p1 += __shfl_xor_sync(FULLMASK, p1, 2);
     const float o0 = __shfl_sync(FULLMASK, p0, src), o1 = __shfl_sync(FULLMASK, p1, src);
-    if ((lane >> 4) == mt) out = ((lane >> 3) & 1) ? o1 : o0;
+    if ((rank >> 4) == mt) out = ((rank >> 3) & 1) ? o1 : o0;
   }
   return N.b4 + out;
 }
