@@ -142,6 +142,14 @@ __host__ __device__ inline size_t evolve_shared_bytes(int mode, int nT, int nZ, 
   return surrogate_offset(mode, nT, nZ) + surrogate_shared_bytes(mapCells);
 }
 
+// Decrement a progenitor counter with acquire-release semantics at GPU
+// scope; true for the decrement that takes it to zero.
+__device__ __forceinline__ bool last_progenitor(int32_t* counter) {
+  int32_t old;
+  asm volatile("atom.acq_rel.gpu.add.s32 %0, [%1], -1;" : "=r"(old) : "l"(counter) : "memory");
+  return old == 1;
+}
+
 // Cooling function (without the n_H^2 factor) and n_e/n_H of one
 // right-hand-side evaluation from the surrogate, for the node of this lane:
 // the network gives log10 Lambda at the central hot-gas density and n_e/n_H
@@ -385,6 +393,18 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
   // component in index order) and go on with the parent.
   auto complete_node = [&](int st) {
     for (;;) {
+      // The parent's fields are read-only during the evolution: read them
+      // with the parent index, before the decrement, so that the merge
+      // waits on no further lookup.
+      const int32_t par = F.parent[node];
+      int32_t c0 = 0, cn = 0, slot = -1, s0 = 0, sn = 0;
+      if (par >= 0) {
+        c0 = F.childFirst[par];
+        cn = F.childCount[par];
+        slot = F.snapInitial[par];
+        s0 = F.segFirst[par];
+        sn = F.segCount[par];
+      }
 #pragma unroll
       for (int v = 0; v < GAL_NY; ++v) F.state[v * F.n + node] = y[v];
       F.stepOut[node] = stepIn;
@@ -394,14 +414,15 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
         F.counters[F.n + node] = nRej;
         F.counters[2 * F.n + node] = nRhs;
       }
-      __threadfence();  // the state is visible before the parent's counter drops
-      const int32_t par = F.parent[node];
-      if (par < 0 || atomicSub(&F.pending[par], 1) != 1) {
+      // One acquire-release decrement of the parent's counter: its release
+      // half orders this lane's stores above before the decrement, and for
+      // the lane that takes the counter to zero its acquire half orders the
+      // other progenitors' stores (each released by their own decrement, in
+      // the counter's release sequence) before the merge's loads below.
+      if (par < 0 || !last_progenitor(&F.pending[par])) {
         phase = PH_NEED;
         return;
       }
-      __threadfence();  // every progenitor's state is visible after the last decrement
-      const int32_t c0 = F.childFirst[par], cn = F.childCount[par];
 #pragma unroll
       for (int v = 0; v < GAL_NY; ++v) y[v] = F.state[v * F.n + c0];
       for (int32_t j = 1; j < cn; ++j) {
@@ -411,13 +432,12 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       stepIn = F.stepOut[c0];
       node = par;
       nAcc = nRej = nRhs = 0;
-      const int32_t slot = F.snapInitial[node];
       if (slot >= 0) {
 #pragma unroll
         for (int v = 0; v < GAL_NY; ++v) F.snapshots[v * F.nSnap + slot] = y[v];
       }
-      seg = F.segFirst[node];
-      segEnd = seg + F.segCount[node];
+      seg = s0;
+      segEnd = s0 + sn;
       if (seg < segEnd) {
         start_segment();
         return;
