@@ -735,8 +735,9 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       double hh = 0.0;
       RateT hr = (RateT)0;
       const bool anyY = any(atY);
-#pragma unroll 1
-      for (int st = anyY ? 0 : 1; st <= 5; ++st) {
+      // One stage: its argument, the evaluation and the slope's slot; false
+      // when no lane of the warp steps (the attempt is over).
+      auto stage = [&](const int st) -> bool {
         if (st == 1) {
           // ---- the slopes at y are in: begin one attempted step (a pass of
           // gsl_odeiv2_evolve_apply's try_step) for every lane that steps.
@@ -755,7 +756,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
             }
           }
           stepping = phase == PH_STEP && !finished;
-          if (!any(stepping)) break;
+          if (!any(stepping)) return false;
           const double dt = t1 - t;
           finalStep = (dt >= 0.0 && h > dt) || (dt < 0.0 && h < dt);
           hh = finalStep ? dt : h;
@@ -821,6 +822,20 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
             for (int i = 0; i < GAL_NY; ++i) k6[i] = d[i];
             break;
         }
+        return true;
+      };
+      if constexpr (SURR) {
+        // One right-hand-side call site, for the network's code size.
+#pragma unroll 1
+        for (int st = anyY ? 0 : 1; st <= 5; ++st)
+          if (!stage(st)) break;
+      } else {
+        // Without the network the stages are unrolled: no stage switch, and
+        // the compiler schedules across stages.
+        if (anyY) stage(0);
+#pragma unroll
+        for (int st = 1; st <= 5; ++st)
+          if (!stage(st)) break;
       }
       if (stepping) {
         nRhs += 5;
