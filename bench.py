@@ -150,6 +150,23 @@ def algorithmic_flops_per_step(params, table, batch, weights_path, sample=512):
     return total / max(steps, 1)
 
 
+def reduce_over_ranks(dist, device, elapsed, work=None):
+    """Weak scaling over the ranks of one node: every rank evolves its own
+    halos or trees (no collective on the data path), so the job's time is the
+    slowest rank's (max) and its work the sum over ranks.  Returns
+    (elapsed, work) unchanged without a process group."""
+    if not dist:
+        return elapsed, work
+    import torch
+    t = torch.tensor([float(elapsed)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    if work is not None:
+        w = torch.tensor([int(work)], device=device, dtype=torch.int64)
+        dist.all_reduce(w, op=dist.ReduceOp.SUM)
+        work = int(w.item())
+    return float(t.item()), work
+
+
 def cpu_baseline(params, table, batch, seconds=10.0):
     """The oracle on every host core over repeats of the full batch; returns
     the baseline record and the final state of the first pass."""
@@ -287,16 +304,8 @@ def run_trees(args, params, table, net, gate, rank, dist, device):
             fe.evolve(sync=False)
         fe.sync()
         dt = (time.perf_counter() - tb) / reps
-        if dist:
-            tt = torch.tensor([dt], device=device)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            dt = float(tt.item())
         acc = fe.accepted_steps()
-        accepted_all = acc
-        if dist:
-            a = torch.tensor([acc], device=device, dtype=torch.int64)
-            dist.all_reduce(a, op=dist.ReduceOp.SUM)
-            accepted_all = int(a.item())
+        dt, accepted_all = reduce_over_ranks(dist, device, dt, acc)
         state, status = fe.results(snapshots=False)[:2]
         entry = {"value": accepted_all / dt, "s_per_evolution": dt, "accepted_steps": acc, "launch": list(ev.get_launch()),
                  "failed_nodes": int((status != 0).sum())}
@@ -518,14 +527,7 @@ def run_ours(args):
             dist.barrier()
         total_ms = sum(a.elapsed_time(b) for a, b, _, _ in evs)
         kernel_ms = statistics.mean(a.elapsed_time(b) for _, _, a, b in evs)
-        accepted_all = accepted
-        if dist:
-            tt = torch.tensor([total_ms], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            total_ms = float(tt.item())
-            acc = torch.tensor([accepted], device=dev, dtype=torch.int64)
-            dist.all_reduce(acc, op=dist.ReduceOp.SUM)
-            accepted_all = int(acc.item())
+        total_ms, accepted_all = reduce_over_ranks(dist, dev, total_ms, accepted)
         return {"value": accepted_all * args.steps / (total_ms * 1e-3), "ms_per_step": total_ms / args.steps,
                 "kernel_ms": kernel_ms, "accepted_per_pass": accepted, "launches": lib.gal_gpu_launch_count(ev.ctx) - launches0,
                 "wall_ms": wall * 1e3, "clocks": sampler.summary() if sampler else None}
@@ -639,11 +641,7 @@ def run_ours(args):
             raise RuntimeError("gal_gpu_evolve_batch failed")
         if i >= args.warmup:
             e2e_times.append(te)
-    e2e_total = sum(e2e_times)
-    if dist:
-        tt = torch.tensor([e2e_total], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_total = float(tt.item())
+    e2e_total, _ = reduce_over_ranks(dist, dev, sum(e2e_times))
     e2e_value = headline["value"] * headline["ms_per_step"] * args.steps * 1e-3 / e2e_total
     h2d = n * (_abi.NY + _abi.NP + 3) * 8
     d2h = n * (_abi.NY + 1) * 8 + n * 4 + n * 12
