@@ -694,14 +694,14 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       if (finished) finish(finalStatus);
     }
   } else {
-    // One right-hand-side call site per pass, in a loop over the stage
-    // index st = 0..5 that is the same for every lane of the warp: st = 0
-    // is f(y) for lanes that start a trial (dydt_in) or accepted a step in
-    // the previous pass (dydt_out, reused as the next dydt_in); st = 1..5
-    // are the stage slopes k2..k6 of an attempt.  Lanes attempt steps
-    // together, so the FP64 error norm and step control run once per
-    // attempt for the warp, and the right-hand side (with the network) is
-    // compiled once.
+    // The other forms (FP32 rates, and the network with either rates): one
+    // pass walks the stage index st = 0..5, the same for every lane of the
+    // warp: st = 0 is f(y) for lanes that start a trial (dydt_in) or
+    // accepted a step in the previous pass (dydt_out, reused as the next
+    // dydt_in); st = 1..5 are the stage slopes k2..k6 of an attempt.  Lanes attempt steps together, so the FP64 error norm and
+    // step control run once per attempt for the warp.  With the network the
+    // stages are a rolled loop around one right-hand-side call site (the
+    // network is compiled once); without it they are unrolled.
     bool needOut = false;
     for (;;) {
       // ---- refill lanes whose node has finished (warp-aggregated queue pop)
