@@ -166,6 +166,10 @@ __device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0
     const int r0 = q0 < count ? nth_set_lane(need, q0) : 0, r1 = q1 < count ? nth_set_lane(need, q1) : 0;
     const float u0 = __shfl_sync(FULLMASK, x0, r0), u1 = __shfl_sync(FULLMASK, x1, r0), u2 = __shfl_sync(FULLMASK, x2, r0);
     const float v0 = __shfl_sync(FULLMASK, x0, r1), v1 = __shfl_sync(FULLMASK, x1, r1), v2 = __shfl_sync(FULLMASK, x2, r1);
+    // Rows 8-15 of the tile (r1) carry a node only when more than 8 rows are
+    // in use; otherwise their element-wise work is skipped (warp-uniform)
+    // and their A rows are zero.  No row's output depends on another row.
+    const bool upper = count - mt * 16 > 8;
     // Layer 1 (FP32) straight into layer 2's A fragments: for k-step ks the
     // lane holds columns ks*16 + 2t, +1 (regs 0, 1) and ks*16 + 8 + 2t, +1
     // (regs 2, 3) of rows r0 (regs 0, 2) and r1 (regs 1, 3).
@@ -178,11 +182,24 @@ __device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0
         const float* wa = N.w1 + 3 * c;
         const float h00 = silu(fmaf(wa[2], u2, fmaf(wa[1], u1, fmaf(wa[0], u0, N.b1[c]))));
         const float h01 = silu(fmaf(wa[5], u2, fmaf(wa[4], u1, fmaf(wa[3], u0, N.b1[c + 1]))));
-        const float h10 = silu(fmaf(wa[2], v2, fmaf(wa[1], v1, fmaf(wa[0], v0, N.b1[c]))));
-        const float h11 = silu(fmaf(wa[5], v2, fmaf(wa[4], v1, fmaf(wa[3], v0, N.b1[c + 1]))));
         split_bf16(h00, h01, ahi[ks][2 * half], alo[ks][2 * half]);
-        split_bf16(h10, h11, ahi[ks][2 * half + 1], alo[ks][2 * half + 1]);
       }
+    }
+    if (upper) {
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks) {
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          const int c = ks * 16 + half * 8 + 2 * t;
+          const float* wa = N.w1 + 3 * c;
+          const float h10 = silu(fmaf(wa[2], v2, fmaf(wa[1], v1, fmaf(wa[0], v0, N.b1[c]))));
+          const float h11 = silu(fmaf(wa[5], v2, fmaf(wa[4], v1, fmaf(wa[3], v0, N.b1[c + 1]))));
+          split_bf16(h10, h11, ahi[ks][2 * half + 1], alo[ks][2 * half + 1]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks) ahi[ks][1] = alo[ks][1] = ahi[ks][3] = alo[ks][3] = 0u;
     }
     float acc[8][4];
     mlp_layer_tile(ahi, alo, N.w2hi, N.w2lo, N.b2, acc, g, t, lane);
@@ -190,9 +207,14 @@ __device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0
 #pragma unroll
     for (int ks = 0; ks < 4; ++ks) {
       split_bf16(silu(acc[2 * ks][0]), silu(acc[2 * ks][1]), ahi[ks][0], alo[ks][0]);
-      split_bf16(silu(acc[2 * ks][2]), silu(acc[2 * ks][3]), ahi[ks][1], alo[ks][1]);
       split_bf16(silu(acc[2 * ks + 1][0]), silu(acc[2 * ks + 1][1]), ahi[ks][2], alo[ks][2]);
-      split_bf16(silu(acc[2 * ks + 1][2]), silu(acc[2 * ks + 1][3]), ahi[ks][3], alo[ks][3]);
+    }
+    if (upper) {
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks) {
+        split_bf16(silu(acc[2 * ks][2]), silu(acc[2 * ks][3]), ahi[ks][1], alo[ks][1]);
+        split_bf16(silu(acc[2 * ks + 1][2]), silu(acc[2 * ks + 1][3]), ahi[ks][3], alo[ks][3]);
+      }
     }
     mlp_layer_tile(ahi, alo, N.w3hi, N.w3lo, N.b3, acc, g, t, lane);
     // Output layer (FP32): this lane's 16 columns of rows r0 and r1, then the
@@ -202,12 +224,18 @@ __device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0
     for (int nt = 0; nt < 8; ++nt) {
       const int col = nt * 8 + 2 * t;
       p0 = fmaf(N.w4[col], silu(acc[nt][0]), fmaf(N.w4[col + 1], silu(acc[nt][1]), p0));
-      p1 = fmaf(N.w4[col], silu(acc[nt][2]), fmaf(N.w4[col + 1], silu(acc[nt][3]), p1));
     }
     p0 += __shfl_xor_sync(FULLMASK, p0, 1);
     p0 += __shfl_xor_sync(FULLMASK, p0, 2);
-    p1 += __shfl_xor_sync(FULLMASK, p1, 1);
-    p1 += __shfl_xor_sync(FULLMASK, p1, 2);
+    if (upper) {
+#pragma unroll
+      for (int nt = 0; nt < 8; ++nt) {
+        const int col = nt * 8 + 2 * t;
+        p1 = fmaf(N.w4[col], silu(acc[nt][2]), fmaf(N.w4[col + 1], silu(acc[nt][3]), p1));
+      }
+      p1 += __shfl_xor_sync(FULLMASK, p1, 1);
+      p1 += __shfl_xor_sync(FULLMASK, p1, 2);
+    }
     const float o0 = __shfl_sync(FULLMASK, p0, src), o1 = __shfl_sync(FULLMASK, p1, src);
     if ((rank >> 4) == mt) out = ((rank >> 3) & 1) ? o1 : o0;
   }
