@@ -80,7 +80,7 @@ struct DeviceTables {
 struct SurrogateDev {
   const float* small;          // kSurrSmall FP32 values
   const __nv_bfloat16* planes; // W2 hi, W2 lo, W3 hi, W3 lo, each [64][kMlpStride]
-  const uint8_t* map;          // [mapT][mapZ] use-table flags
+  const uint8_t* map;          // [mapT][mapZ] use-table flags, then [mapT] row flags (surrogate_map_bytes)
   SurrogateInfo info;
   unsigned long long* stats;   // [2]: network and table evaluations
 };
@@ -128,6 +128,9 @@ __host__ __device__ inline size_t shared_bytes(int nT, int nZ) {
 __host__ __device__ inline size_t shared_bytes_fast(int nT, int nZ) {
   return (size_t)nZ * nT * sizeof(float2) + (size_t)((2 * nZ + 1) & ~1) * sizeof(float);
 }
+// The error map on the device: [mapT][mapZ] use-table flags, then one flag
+// per T row: 1 when at least one cell of the row is served by the network.
+__host__ __device__ inline int surrogate_map_bytes(int mapT, int mapZ) { return mapT * (mapZ + 1); }
 __host__ __device__ inline size_t surrogate_shared_bytes(int mapCells) {
   return (size_t)((kSurrSmall + 3) & ~3) * sizeof(float) + 4 * (size_t)kSurrPlane * sizeof(__nv_bfloat16) +
          (size_t)((mapCells + 15) & ~15);
@@ -150,6 +153,15 @@ __device__ __forceinline__ bool last_progenitor(int32_t* counter) {
   return old == 1;
 }
 
+// First error-map cell of the T row of a node at log10 T = lt, or -1 when
+// the network can serve none of its evaluations (cooling cut off, T outside
+// the training domain, or every cell of the row marked for the table).
+__device__ __forceinline__ int surrogate_net_row(const SurrogateInfo& I, const uint8_t* map, float lt, bool cooling) {
+  if (!cooling || !(lt >= I.lo[0] && lt <= I.hi[0])) return -1;
+  const int it = min(max((int)((lt - I.mapLoT) * I.mapInvDT), 0), I.mapT - 1);
+  return map[I.mapT * I.mapZ + it] ? it * I.mapZ : -1;
+}
+
 // Cooling function (without the n_H^2 factor) and n_e/n_H of one
 // right-hand-side evaluation from the surrogate, for the node of this lane:
 // the network gives log10 Lambda at the central hot-gas density and n_e/n_H
@@ -164,20 +176,30 @@ __device__ __forceinline__ CoolingValuesF surrogate_cooling(const Globals& G, co
                                                            uint32_t& nTab) {
   const float massHot = (float)y[GAL_Y_HOT_MASS];
   const float metals = (float)y[GAL_Y_HOT_METALS];
-  bool ok = active && massHot > 0.0f && c.coolingAllowed;
-  const float zf = ok ? (metals > massHot ? 1.0f : (metals <= 0.0f ? 0.0f : __fdividef(metals, massHot))) : 0.0f;
-  const float zs = zf * (float)(1.0 / k::metallicitySolar);
-  const float xH = fminf(fmaxf(zs * (float)(k::hydrogenByMassSolar - k::hydrogenByMassPrimordial) +
-                               (float)k::hydrogenByMassPrimordial, 0.7f), (float)k::hydrogenByMassPrimordial);
-  const float nH = massHot * (float)c.rho0PerMass * xH * (float)k::densityToHydrogenNumber;
+  // The node's T row (its cooling cut-off, T domain and whether any cell of
+  // the row uses the network) is fixed per node: c.netRow.  Then the Z
+  // domain and the map cell, and last the n_H domain, so that a lane bound
+  // for the table stops early.  The decision is the same as testing every
+  // condition.
   const float lt = c.log10T;
-  const float lz = zs > 0.0f ? __log10f(zs) : -1.0e30f;
-  const float ln = nH > 0.0f ? __log10f(nH) : -1.0e30f;
-  ok = ok && lt >= I.lo[0] && lt <= I.hi[0] && lz >= I.lo[1] && lz <= I.hi[1] && ln >= I.lo[2] && ln <= I.hi[2];
+  float zs = 0.0f, lz = -1.0e30f, ln = -1.0e30f;
+  bool ok = active && c.netRow >= 0 && massHot > 0.0f;
   if (ok) {
-    const int it = min(max((int)((lt - I.mapLoT) * I.mapInvDT), 0), I.mapT - 1);
-    const int iz = min(max((int)((lz - I.mapLoZ) * I.mapInvDZ), 0), I.mapZ - 1);
-    ok = map[it * I.mapZ + iz] == 0;
+    const float zf = metals > massHot ? 1.0f : (metals <= 0.0f ? 0.0f : __fdividef(metals, massHot));
+    zs = zf * (float)(1.0 / k::metallicitySolar);
+    lz = zs > 0.0f ? __log10f(zs) : -1.0e30f;
+    ok = lz >= I.lo[1] && lz <= I.hi[1];
+    if (ok) {
+      const int iz = min(max((int)((lz - I.mapLoZ) * I.mapInvDZ), 0), I.mapZ - 1);
+      ok = map[c.netRow + iz] == 0;
+    }
+    if (ok) {
+      const float xH = fminf(fmaxf(zs * (float)(k::hydrogenByMassSolar - k::hydrogenByMassPrimordial) +
+                                   (float)k::hydrogenByMassPrimordial, 0.7f), (float)k::hydrogenByMassPrimordial);
+      const float nH = massHot * (float)c.rho0PerMass * xH * (float)k::densityToHydrogenNumber;
+      ln = nH > 0.0f ? __log10f(nH) : -1.0e30f;
+      ok = ln >= I.lo[2] && ln <= I.hi[2];
+    }
   }
   CoolingValuesF cv{false, 0.0f, 0.0f};
   // The network runs only when some lane of the warp can use it.
@@ -270,7 +292,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
     for (int i = threadIdx.x; i < kSurrSmall; i += blockDim.x) small[i] = sd.small[i];
     for (int i = threadIdx.x; i < 4 * kSurrPlane / 2; i += blockDim.x)
       reinterpret_cast<uint32_t*>(planes)[i] = reinterpret_cast<const uint32_t*>(sd.planes)[i];
-    for (int i = threadIdx.x; i < sd.info.mapT * sd.info.mapZ; i += blockDim.x) map[i] = sd.map[i];
+    for (int i = threadIdx.x; i < surrogate_map_bytes(sd.info.mapT, sd.info.mapZ); i += blockDim.x) map[i] = sd.map[i];
     sSmall = small;
     sPlanes = planes;
     sMap = map;
@@ -314,6 +336,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
   uint32_t count = 0, nAcc = 0, nRej = 0, nRhs = 0, nNet = 0, nTab = 0;
   c.log10T = 0.0f;
   cf.log10T = 0.0f;
+  c.netRow = cf.netRow = -1;
 
   // One right-hand-side evaluation at xx for the lanes with `active`; with
   // the surrogate, every lane of the warp takes part in the network evaluation.
@@ -344,8 +367,10 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
     if constexpr (FAST) {
       node_setup_fast(G, sLnT, prm, cf);
       c.massHalo = prm[GAL_P_MASS];
+      if constexpr (SURR) cf.netRow = surrogate_net_row(sd.info, sMap, cf.log10T, cf.coolingAllowed);
     } else {
       node_setup(G, sLnT, prm, c);
+      if constexpr (SURR) c.netRow = surrogate_net_row(sd.info, sMap, c.log10T, c.coolingAllowed);
     }
   };
   // Absolute-tolerance scales of the current evolve call.

@@ -116,7 +116,8 @@ int ctx_mode(const gal_ctx* ctx) {
 }
 
 size_t ctx_shared_bytes(const gal_ctx* ctx, int mode) {
-  return evolve_shared_bytes(mode, ctx->globals.nT, ctx->globals.nZ, ctx->surrInfo.mapT * ctx->surrInfo.mapZ);
+  return evolve_shared_bytes(mode, ctx->globals.nT, ctx->globals.nZ,
+                             surrogate_map_bytes(ctx->surrInfo.mapT, ctx->surrInfo.mapZ));
 }
 
 // Block sizes each form is built for (evolve_*.cu).
@@ -466,11 +467,19 @@ int gal_gpu_set_surrogate(gal_ctx* ctx, const gal_surrogate* sg) {
   I.mapLoZ = sg->map_lo_z;
   I.mapInvDT = 1.0f / sg->map_dt;
   I.mapInvDZ = 1.0f / sg->map_dz;
-  if (evolve_shared_bytes(MODE_SURROGATE, ctx->globals.nT, ctx->globals.nZ, cells) > 227 * 1024)
+  // The map followed by its row flags (1: some cell of the row uses the network).
+  const int mapBytes = surrogate_map_bytes(sg->map_t, sg->map_z);
+  std::vector<uint8_t> map(sg->use_table, sg->use_table + cells);
+  for (int t = 0; t < sg->map_t; ++t) {
+    uint8_t any = 0;
+    for (int z = 0; z < sg->map_z; ++z) any |= sg->use_table[t * sg->map_z + z] == 0;
+    map.push_back(any);
+  }
+  if (evolve_shared_bytes(MODE_SURROGATE, ctx->globals.nT, ctx->globals.nZ, mapBytes) > 227 * 1024)
     return fail(ctx, GAL_ERR_TOO_LARGE, "gal_gpu_set_surrogate: shared memory footprint too large%s");
   if (cudaMalloc(&ctx->dSurrSmall, small.size() * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&ctx->dSurrPlanes, planes.size() * sizeof(__nv_bfloat16)) != cudaSuccess ||
-      cudaMalloc(&ctx->dSurrMap, cells) != cudaSuccess ||
+      cudaMalloc(&ctx->dSurrMap, mapBytes) != cudaSuccess ||
       cudaMalloc(&ctx->dSurrStats, 2 * sizeof(unsigned long long)) != cudaSuccess) {
     cudaGetLastError();
     free_surrogate(ctx);
@@ -478,7 +487,7 @@ int gal_gpu_set_surrogate(gal_ctx* ctx, const gal_surrogate* sg) {
   }
   if (cudaMemcpy(ctx->dSurrSmall, small.data(), small.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(ctx->dSurrPlanes, planes.data(), planes.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(ctx->dSurrMap, sg->use_table, cells, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->dSurrMap, map.data(), mapBytes, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemset(ctx->dSurrStats, 0, 2 * sizeof(unsigned long long)) != cudaSuccess) {
     free_surrogate(ctx);
     return fail(ctx, GAL_ERR_CUDA, "gal_gpu_set_surrogate: upload failed%s");

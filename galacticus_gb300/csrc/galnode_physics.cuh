@@ -169,6 +169,8 @@ struct NodeC {
   int iT;                     // temperature cell of T_vir
   int coolingAllowed;         // V_vir <= velocity cut-off
   float log10T;               // log10 T_vir (input of the cooling surrogate)
+  int netRow;                 // with the surrogate: first error-map cell of the node's T row, or -1
+                              // when no cell of that row is served by the network
   double sfrDisk, sfrSph;     // 1/tau_* of the disk and spheroid (0: none)
   double outDisk, outSph;     // outflow rate per unit SFR
   double outDiskMax, outSphMax; // 1/(t_dyn f_min) of the rate limit (<0: no limit)

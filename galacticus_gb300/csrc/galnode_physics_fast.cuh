@@ -36,6 +36,7 @@ struct NodeF {
   int iT;
   int coolingAllowed;
   float log10T;
+  int netRow;                // as NodeC::netRow
   float sfrDisk, sfrSph;
   float outDisk, outSph, outDiskMax, outSphMax;
   float aSph, invASph, rhoSphPerMass, radiusDisk;

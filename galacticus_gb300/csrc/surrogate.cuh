@@ -139,26 +139,100 @@ __device__ __forceinline__ void mlp_layer_tile(const uint32_t (&ahi)[4][4], cons
   }
 }
 
+// One 16-row tile of the network.  Lane group g = lane/4 holds rows g
+// (inputs u) and g + 8 (inputs v); `upper` (warp-uniform) says whether rows
+// 8-15 carry nodes -- otherwise their element-wise work is skipped and their
+// A rows are zero.  No row's output depends on another row.  On return
+// every lane of group g holds in p0 and p1 the normalised outputs of rows g
+// and g + 8 without the output bias.  Warp-collective.
+__device__ __forceinline__ void mlp_tile(const SurrogateSmem& N, float u0, float u1, float u2, float v0, float v1,
+                                         float v2, bool upper, int lane, float& p0, float& p1) {
+  const unsigned FULLMASK = 0xffffffffu;
+  const int g = lane >> 2, t = lane & 3;
+  // Layer 1 (FP32) straight into layer 2's A fragments: for k-step ks the
+  // lane holds columns ks*16 + 2t, +1 (regs 0, 1) and ks*16 + 8 + 2t, +1
+  // (regs 2, 3) of rows g (regs 0, 2) and g + 8 (regs 1, 3).
+  uint32_t ahi[4][4], alo[4][4];
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks) {
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int c = ks * 16 + half * 8 + 2 * t;
+      const float* wa = N.w1 + 3 * c;
+      const float h00 = silu(fmaf(wa[2], u2, fmaf(wa[1], u1, fmaf(wa[0], u0, N.b1[c]))));
+      const float h01 = silu(fmaf(wa[5], u2, fmaf(wa[4], u1, fmaf(wa[3], u0, N.b1[c + 1]))));
+      split_bf16(h00, h01, ahi[ks][2 * half], alo[ks][2 * half]);
+    }
+  }
+  if (upper) {
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int c = ks * 16 + half * 8 + 2 * t;
+        const float* wa = N.w1 + 3 * c;
+        const float h10 = silu(fmaf(wa[2], v2, fmaf(wa[1], v1, fmaf(wa[0], v0, N.b1[c]))));
+        const float h11 = silu(fmaf(wa[5], v2, fmaf(wa[4], v1, fmaf(wa[3], v0, N.b1[c + 1]))));
+        split_bf16(h10, h11, ahi[ks][2 * half + 1], alo[ks][2 * half + 1]);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) ahi[ks][1] = alo[ks][1] = ahi[ks][3] = alo[ks][3] = 0u;
+  }
+  float acc[8][4];
+  mlp_layer_tile(ahi, alo, N.w2hi, N.w2lo, N.b2, acc, g, t, lane);
+  // Layer 2's accumulators (n-tiles 2ks and 2ks+1) are layer 3's A fragments for k-step ks.
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks) {
+    split_bf16(silu(acc[2 * ks][0]), silu(acc[2 * ks][1]), ahi[ks][0], alo[ks][0]);
+    split_bf16(silu(acc[2 * ks + 1][0]), silu(acc[2 * ks + 1][1]), ahi[ks][2], alo[ks][2]);
+  }
+  if (upper) {
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+      split_bf16(silu(acc[2 * ks][2]), silu(acc[2 * ks][3]), ahi[ks][1], alo[ks][1]);
+      split_bf16(silu(acc[2 * ks + 1][2]), silu(acc[2 * ks + 1][3]), ahi[ks][3], alo[ks][3]);
+    }
+  }
+  mlp_layer_tile(ahi, alo, N.w3hi, N.w3lo, N.b3, acc, g, t, lane);
+  // Output layer (FP32): this lane's 16 columns of rows g and g + 8, then the
+  // sum over the four lanes of the row group.
+  p0 = 0.0f;
+  p1 = 0.0f;
+#pragma unroll
+  for (int nt = 0; nt < 8; ++nt) {
+    const int col = nt * 8 + 2 * t;
+    p0 = fmaf(N.w4[col], silu(acc[nt][0]), fmaf(N.w4[col + 1], silu(acc[nt][1]), p0));
+  }
+  p0 += __shfl_xor_sync(FULLMASK, p0, 1);
+  p0 += __shfl_xor_sync(FULLMASK, p0, 2);
+  if (upper) {
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+      const int col = nt * 8 + 2 * t;
+      p1 = fmaf(N.w4[col], silu(acc[nt][2]), fmaf(N.w4[col + 1], silu(acc[nt][3]), p1));
+    }
+    p1 += __shfl_xor_sync(FULLMASK, p1, 1);
+    p1 += __shfl_xor_sync(FULLMASK, p1, 2);
+  }
+}
+
 // Normalised output of the network for this lane's input (x0, x1, x2):
 // returns y_n.  `need` is the warp's ballot of lanes that use the result;
-// a 16-row tile (lanes 0-15 or 16-31) that no such lane falls in is skipped
-// (warp-uniform), which halves the cost when a warp integrates its last few
-// nodes.  Warp-collective.
+// they are packed into consecutive rows in lane order, so that
+// ceil(count/16) tiles run.  The lane of rank q is row (q & 7) of half
+// (q >> 3) & 1 of tile q >> 4; its sum ends up in lane 4 (q & 7) of that
+// tile's pass.  Warp-collective.
 __device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0, float x1, float x2, int lane,
                                                unsigned need = 0xffffffffu) {
   const unsigned FULLMASK = 0xffffffffu;
-  const int g = lane >> 2, t = lane & 3;
-  // The lanes in `need` are packed into consecutive rows in lane order, so
-  // that ceil(count/16) tiles run.  A row's output depends on its own inputs
-  // only, so a lane's result does not depend on which row it lands in.
-  // The lane of rank q is row (q & 7) of half (q >> 3) & 1 of tile q >> 4;
-  // its sum ends up in lane 4 (q & 7) of that tile's pass.
+  const int g = lane >> 2;
   const int count = __popc(need);
   const int rank = __popc(need & ((1u << lane) - 1u));
   float out = 0.0f;
   const int src = 4 * (rank & 7);
-  // The tiles are not unrolled: one copy of the network code (the kernel
-  // that calls it is otherwise instruction-fetch bound).
+  // The tiles are not unrolled: one copy of the network code.
 #pragma unroll 1
   for (int mt = 0; mt < (count + 15) >> 4; ++mt) {
     // Rows past the last needing lane take lane 0's inputs (finite; ignored).
@@ -166,76 +240,8 @@ __device__ __forceinline__ float surrogate_eval(const SurrogateSmem& N, float x0
     const int r0 = q0 < count ? nth_set_lane(need, q0) : 0, r1 = q1 < count ? nth_set_lane(need, q1) : 0;
     const float u0 = __shfl_sync(FULLMASK, x0, r0), u1 = __shfl_sync(FULLMASK, x1, r0), u2 = __shfl_sync(FULLMASK, x2, r0);
     const float v0 = __shfl_sync(FULLMASK, x0, r1), v1 = __shfl_sync(FULLMASK, x1, r1), v2 = __shfl_sync(FULLMASK, x2, r1);
-    // Rows 8-15 of the tile (r1) carry a node only when more than 8 rows are
-    // in use; otherwise their element-wise work is skipped (warp-uniform)
-    // and their A rows are zero.  No row's output depends on another row.
-    const bool upper = count - mt * 16 > 8;
-    // Layer 1 (FP32) straight into layer 2's A fragments: for k-step ks the
-    // lane holds columns ks*16 + 2t, +1 (regs 0, 1) and ks*16 + 8 + 2t, +1
-    // (regs 2, 3) of rows r0 (regs 0, 2) and r1 (regs 1, 3).
-    uint32_t ahi[4][4], alo[4][4];
-#pragma unroll
-    for (int ks = 0; ks < 4; ++ks) {
-#pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        const int c = ks * 16 + half * 8 + 2 * t;
-        const float* wa = N.w1 + 3 * c;
-        const float h00 = silu(fmaf(wa[2], u2, fmaf(wa[1], u1, fmaf(wa[0], u0, N.b1[c]))));
-        const float h01 = silu(fmaf(wa[5], u2, fmaf(wa[4], u1, fmaf(wa[3], u0, N.b1[c + 1]))));
-        split_bf16(h00, h01, ahi[ks][2 * half], alo[ks][2 * half]);
-      }
-    }
-    if (upper) {
-#pragma unroll
-      for (int ks = 0; ks < 4; ++ks) {
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-          const int c = ks * 16 + half * 8 + 2 * t;
-          const float* wa = N.w1 + 3 * c;
-          const float h10 = silu(fmaf(wa[2], v2, fmaf(wa[1], v1, fmaf(wa[0], v0, N.b1[c]))));
-          const float h11 = silu(fmaf(wa[5], v2, fmaf(wa[4], v1, fmaf(wa[3], v0, N.b1[c + 1]))));
-          split_bf16(h10, h11, ahi[ks][2 * half + 1], alo[ks][2 * half + 1]);
-        }
-      }
-    } else {
-#pragma unroll
-      for (int ks = 0; ks < 4; ++ks) ahi[ks][1] = alo[ks][1] = ahi[ks][3] = alo[ks][3] = 0u;
-    }
-    float acc[8][4];
-    mlp_layer_tile(ahi, alo, N.w2hi, N.w2lo, N.b2, acc, g, t, lane);
-    // Layer 2's accumulators (n-tiles 2ks and 2ks+1) are layer 3's A fragments for k-step ks.
-#pragma unroll
-    for (int ks = 0; ks < 4; ++ks) {
-      split_bf16(silu(acc[2 * ks][0]), silu(acc[2 * ks][1]), ahi[ks][0], alo[ks][0]);
-      split_bf16(silu(acc[2 * ks + 1][0]), silu(acc[2 * ks + 1][1]), ahi[ks][2], alo[ks][2]);
-    }
-    if (upper) {
-#pragma unroll
-      for (int ks = 0; ks < 4; ++ks) {
-        split_bf16(silu(acc[2 * ks][2]), silu(acc[2 * ks][3]), ahi[ks][1], alo[ks][1]);
-        split_bf16(silu(acc[2 * ks + 1][2]), silu(acc[2 * ks + 1][3]), ahi[ks][3], alo[ks][3]);
-      }
-    }
-    mlp_layer_tile(ahi, alo, N.w3hi, N.w3lo, N.b3, acc, g, t, lane);
-    // Output layer (FP32): this lane's 16 columns of rows r0 and r1, then the
-    // sum over the four lanes of the row group.
-    float p0 = 0.0f, p1 = 0.0f;
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-      const int col = nt * 8 + 2 * t;
-      p0 = fmaf(N.w4[col], silu(acc[nt][0]), fmaf(N.w4[col + 1], silu(acc[nt][1]), p0));
-    }
-    p0 += __shfl_xor_sync(FULLMASK, p0, 1);
-    p0 += __shfl_xor_sync(FULLMASK, p0, 2);
-    if (upper) {
-#pragma unroll
-      for (int nt = 0; nt < 8; ++nt) {
-        const int col = nt * 8 + 2 * t;
-        p1 = fmaf(N.w4[col], silu(acc[nt][2]), fmaf(N.w4[col + 1], silu(acc[nt][3]), p1));
-      }
-      p1 += __shfl_xor_sync(FULLMASK, p1, 1);
-      p1 += __shfl_xor_sync(FULLMASK, p1, 2);
-    }
+    float p0, p1;
+    mlp_tile(N, u0, u1, u2, v0, v1, v2, count - mt * 16 > 8, lane, p0, p1);
     const float o0 = __shfl_sync(FULLMASK, p0, src), o1 = __shfl_sync(FULLMASK, p1, src);
     if ((rank >> 4) == mt) out = ((rank >> 3) & 1) ? o1 : o0;
   }

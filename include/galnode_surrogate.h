@@ -77,7 +77,7 @@ int gal_surrogate_predict(const float* params, const float* x, int64_t n, float*
 int gal_gpu_set_surrogate(gal_ctx* ctx, const gal_surrogate* s);
 
 /* Cooling-function evaluations by the surrogate and by the table fallback
- * since the surrogate was installed (counted per warp-level call). */
+ * since the surrogate was installed (one per node and right-hand side). */
 int gal_gpu_surrogate_stats(const gal_ctx* ctx, uint64_t* network, uint64_t* table);
 
 #ifdef __cplusplus
