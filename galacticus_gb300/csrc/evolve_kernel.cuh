@@ -334,9 +334,13 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
   double t = 0.0, t0 = 0.0, t1 = 0.0, h = 0.0, stepIn = -1.0;
   int trial = 0;
   uint32_t count = 0, nAcc = 0, nRej = 0, nRhs = 0, nNet = 0, nTab = 0;
+  // Lanes that never take a node still hold in-range table coordinates.
   c.log10T = 0.0f;
   cf.log10T = 0.0f;
   c.netRow = cf.netRow = -1;
+  c.iT = cf.iT = 0;
+  c.hT = 0.0;
+  cf.hT = 0.0f;
 
   // One right-hand-side evaluation at xx for the lanes with `active`; with
   // the surrogate, every lane of the warp takes part in the network evaluation.
