@@ -8,8 +8,9 @@
 //
 // Layers 2 and 3 (64 -> 64) run on the tensor cores (mma.sync m16n8k16,
 // BF16 x BF16 with FP32 accumulation; the warp's nodes that need the
-// network are packed into one or two 16-row tiles).  Each FP32 operand is split into a BF16 high part and a BF16
-// remainder, v = hi + lo, and a product is taken as hi*hi + hi*lo + lo*hi
+// network are packed into one or two 16-row tiles).  Each FP32 operand is
+// split into a BF16 high part and a BF16 remainder, v = hi + lo, and a
+// product is taken as hi*hi + hi*lo + lo*hi
 // (three MMAs), which keeps about 16 significant bits -- plain BF16 operands
 // (8 bits) put up to 0.03 dex of rounding error on the output, three times
 // the fallback tolerance.  The activations never leave registers: layer 1
