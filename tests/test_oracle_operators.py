@@ -1,0 +1,159 @@
+"""The oracle's right-hand side, one node operator at a time, against the
+reference's formulas restated here independently (physics mask with a single
+operator enabled; the constants are the reference's GSL MKSA values).
+
+  reincorporation  haloDynamicalTime: dM_out/dt = -m M_out / t_dyn
+                   (hot_halo/outflow_reincorporation/halo_dynamical_time.F90:113-128)
+  star formation   timescale + dynamicalTime + instantaneous populations
+                   (star_formation/rates/disks/timescale.F90:109-130,
+                   star_formation/timescales/dynamical_time.F90:121-189,
+                   stellar_populations/properties/instantaneous.F90:133-219)
+  feedback         powerLaw under rateLimit (stellar_feedback/outflows/power_law/
+                   _class.F90:118-164, rate_limit.F90)
+  cooling          whiteFrenk1991: M_hot / t_dyn once the cooling radius reaches the
+                   outer radius (cooling/cooling_rate/White-Frenk.F90:132-185), nothing
+                   above the velocity cut-off
+  black holes      Bondi-Hoyle-Lyttleton accretion from the hot halo, capped by the hot
+                   gas and the Eddington rate (accretion/Bondi_Hoyle_Lyttleton.F90:34-78,
+                   black_holes/fundamentals.F90:123-138, accretion_rates/standard.F90:221-440)
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from galacticus_gb300 import _abi, workloads
+
+# GSL MKSA constants as the reference uses them (numerical/constants).
+MEGAPARSEC = 3.08567758135e22
+GIGAYEAR = 3.15581497635456e16
+MPC_PER_KMS_TO_GYR = MEGAPARSEC / 1.0e3 / GIGAYEAR
+G_SI, M_H, SIGMA_T, C_LIGHT = 6.673e-11, 1.0078250322 * 1.660538782e-27, 6.65245893699e-29, 2.99792458e8
+
+
+def node(mass=1e12, rvir=0.2, vvir=150.0, spin=0.04, mdot=0.0):
+    p = np.zeros(_abi.NP)
+    p[_abi.P_MASS], p[_abi.P_MASS_RATE], p[_abi.P_RADIUS_VIRIAL], p[_abi.P_VELOCITY_VIRIAL], p[_abi.P_SPIN] = \
+        mass, mdot, rvir, vvir, spin
+    return p
+
+
+def only(mask):
+    params = workloads.isolated_params()
+    params.physics = mask
+    return params
+
+
+def test_reincorporation(oracle_mod, table):
+    params = only(_abi.PHYS_REINCORPORATION)
+    prm = node()
+    y = np.zeros(_abi.NY)
+    y[_abi.Y_OUTFLOWED_MASS], y[_abi.Y_OUTFLOWED_METALS] = 3e9, 4e7
+    d = oracle_mod.rhs(params, table, prm, y)
+    tdyn = prm[_abi.P_RADIUS_VIRIAL] / prm[_abi.P_VELOCITY_VIRIAL] * MPC_PER_KMS_TO_GYR
+    rate = params.reincorporation_multiplier * y[_abi.Y_OUTFLOWED_MASS] / tdyn
+    assert d[_abi.Y_OUTFLOWED_MASS] == pytest.approx(-rate, rel=1e-13)
+    assert d[_abi.Y_HOT_MASS] == pytest.approx(rate, rel=1e-13)
+    assert d[_abi.Y_HOT_METALS] == pytest.approx(rate * 4e7 / 3e9, rel=1e-13)
+    others = [i for i in range(_abi.NY) if i not in (_abi.Y_OUTFLOWED_MASS, _abi.Y_OUTFLOWED_METALS,
+                                                       _abi.Y_HOT_MASS, _abi.Y_HOT_METALS)]
+    assert np.all(d[others] == 0.0)
+
+
+def disk_timescale(params, prm):
+    sf = params.sf_disk
+    radius = params.radius_factor_disk * prm[_abi.P_SPIN] * prm[_abi.P_RADIUS_VIRIAL]
+    v = prm[_abi.P_VELOCITY_VIRIAL]
+    return max(MPC_PER_KMS_TO_GYR * radius / v * (v / 200.0) ** sf.exponent_velocity / sf.efficiency,
+               sf.timescale_minimum), radius
+
+
+def test_disk_star_formation(oracle_mod, table):
+    params = only(_abi.PHYS_STAR_FORMATION_DISK)
+    prm = node()
+    y = np.zeros(_abi.NY)
+    y[_abi.Y_DISK_GAS], y[_abi.Y_DISK_GAS_METALS] = 5e9, 5e7
+    d = oracle_mod.rhs(params, table, prm, y)
+    tau, _ = disk_timescale(params, prm)
+    sfr = y[_abi.Y_DISK_GAS] / tau
+    stars = (1.0 - params.recycled_fraction) * sfr
+    z = y[_abi.Y_DISK_GAS_METALS] / y[_abi.Y_DISK_GAS]
+    assert d[_abi.Y_DISK_STARS] == pytest.approx(stars, rel=1e-12)
+    assert d[_abi.Y_DISK_GAS] == pytest.approx(-stars, rel=1e-12)
+    assert d[_abi.Y_DISK_STARS_METALS] == pytest.approx(z * stars, rel=1e-12)
+    assert d[_abi.Y_DISK_GAS_METALS] == pytest.approx(-z * stars + params.metal_yield * sfr, rel=1e-12)
+
+
+@pytest.mark.parametrize("vvir", [40.0, 300.0])
+def test_disk_feedback_with_rate_limit(oracle_mod, table, vvir):
+    params = only(_abi.PHYS_STAR_FORMATION_DISK | _abi.PHYS_FEEDBACK_DISK)
+    prm = node(vvir=vvir)
+    y = np.zeros(_abi.NY)
+    y[_abi.Y_DISK_GAS] = 5e9
+    d_sf = oracle_mod.rhs(only(_abi.PHYS_STAR_FORMATION_DISK), table, prm, y)
+    d = oracle_mod.rhs(params, table, prm, y)
+    tau, radius = disk_timescale(params, prm)
+    sfr = y[_abi.Y_DISK_GAS] / tau
+    o = params.outflow_disk
+    outflow = (o.velocity_characteristic / vvir) ** o.exponent * sfr
+    limit = y[_abi.Y_DISK_GAS] / (MPC_PER_KMS_TO_GYR * radius / vvir) / o.timescale_fractional_minimum
+    expected = min(outflow, limit)
+    assert d[_abi.Y_OUTFLOWED_MASS] == pytest.approx(expected, rel=1e-12)
+    assert d[_abi.Y_DISK_GAS] - d_sf[_abi.Y_DISK_GAS] == pytest.approx(-expected, rel=1e-12)
+
+
+def test_rapid_cooling_and_the_velocity_cutoff(oracle_mod, table):
+    params = only(_abi.PHYS_COOLING)
+    # A dense, cool hot halo: the cooling radius reaches the virial radius.
+    prm = node(mass=1e10, rvir=0.02, vvir=50.0)
+    y = np.zeros(_abi.NY)
+    y[_abi.Y_HOT_MASS], y[_abi.Y_HOT_METALS] = 1.5e9, 1.5e9 * 0.0188
+    rcool = oracle_mod.cooling_radius(params, table, prm, y[_abi.Y_HOT_MASS], y[_abi.Y_HOT_METALS])
+    assert rcool >= prm[_abi.P_RADIUS_VIRIAL]
+    d = oracle_mod.rhs(params, table, prm, y)
+    tdyn = prm[_abi.P_RADIUS_VIRIAL] / prm[_abi.P_VELOCITY_VIRIAL] * MPC_PER_KMS_TO_GYR
+    rate = y[_abi.Y_HOT_MASS] / tdyn
+    assert d[_abi.Y_HOT_MASS] == pytest.approx(-rate, rel=1e-12)
+    assert d[_abi.Y_DISK_GAS] == pytest.approx(rate, rel=1e-12)
+    assert d[_abi.Y_DISK_GAS_METALS] == pytest.approx(rate * 0.0188, rel=1e-12)
+    # Above the cut-off velocity nothing cools.
+    params.cooling_velocity_cutoff = 40.0
+    assert np.all(oracle_mod.rhs(params, table, prm, y) == 0.0)
+
+
+@pytest.mark.parametrize("enhancement,binding", [(None, "bondi"), (1.0e6, "eddington")])
+def test_hot_mode_black_hole_accretion(oracle_mod, table, enhancement, binding):
+    """Bondi-Hoyle-Lyttleton accretion from the hot halo at the accretion
+    radius G M_BH / c_s^2 (Bondi_Hoyle_Lyttleton.F90:34-59), under the
+    hot-gas and Eddington caps; with a large enhancement the Eddington rate
+    binds."""
+    params = only(_abi.PHYS_BLACK_HOLE_ACCRETION)
+    if enhancement is not None:
+        params.bh_enhancement_hot_halo = enhancement
+    prm = node()
+    rvir, v = prm[_abi.P_RADIUS_VIRIAL], prm[_abi.P_VELOCITY_VIRIAL]
+    y = np.zeros(_abi.NY)
+    y[_abi.Y_HOT_MASS], y[_abi.Y_BLACK_HOLE] = 1e11, 1e9
+    # Hot mode throughout: the cooling radius is inside 0.9 r_vir.
+    assert oracle_mod.cooling_radius(params, table, prm, y[_abi.Y_HOT_MASS], 0.0) < 0.9 * rvir
+    d = oracle_mod.rhs(params, table, prm, y)
+    amu, kB = 1.660538782e-27, 1.3806504e-23
+    mu = 1.0 / (2.0 * 0.7514 / 1.0078250322 + 3.0 * 0.2486 / 4.0026032545)
+    temperature = 0.5 * amu * mu * (1e3 * v) ** 2 / kB
+    cs = math.sqrt(5.0 * kB * temperature / 3.0 / mu / amu) / 1e3
+    g_internal = G_SI * 1.98892e30 / 1e6 / MEGAPARSEC
+    r_acc = min(g_internal * y[_abi.Y_BLACK_HOLE] / cs ** 2, rvir)
+    rc = params.core_radius_fraction * rvir
+    x = rvir / rc
+    rho = y[_abi.Y_HOT_MASS] / (4.0 * math.pi * rc ** 3) / (x - math.atan(x)) / (1.0 + (r_acc / rc) ** 2)
+    bhl = 1e3 * GIGAYEAR / MEGAPARSEC * 4.0 * math.pi
+    bondi = params.bh_enhancement_hot_halo * bhl * r_acc ** 2 * rho * cs
+    hot_cap = y[_abi.Y_HOT_MASS] / (rvir / cs * MPC_PER_KMS_TO_GYR)
+    eddington = y[_abi.Y_BLACK_HOLE] * 4.0 * math.pi * G_SI * M_H * GIGAYEAR / SIGMA_T / C_LIGHT \
+        / params.bh_efficiency_radiative
+    accreted = min(bondi, hot_cap, eddington)
+    assert accreted == (bondi if binding == "bondi" else eddington)
+    kept = 1.0 - params.bh_efficiency_radiative - params.bh_efficiency_jet
+    assert d[_abi.Y_BLACK_HOLE] == pytest.approx(kept * accreted, rel=1e-12)
+    assert d[_abi.Y_HOT_MASS] == pytest.approx(-accreted, rel=1e-12)
