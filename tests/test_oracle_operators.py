@@ -11,8 +11,11 @@ operator enabled; the constants are the reference's GSL MKSA values).
   feedback         powerLaw under rateLimit (stellar_feedback/outflows/power_law/
                    _class.F90:118-164, rate_limit.F90)
   cooling          whiteFrenk1991: M_hot / t_dyn once the cooling radius reaches the
-                   outer radius (cooling/cooling_rate/White-Frenk.F90:132-185), nothing
-                   above the velocity cut-off
+                   outer radius, the infall of the cooling radius below it
+                   (cooling/cooling_rate/White-Frenk.F90:132-185,
+                   cooling_radius/simple.F90:229-311), nothing above the velocity cut-off
+  gas accretion    Omega_b / Omega_m of the halo's growth (accretion/halo/simple.F90:281-319)
+  spheroids        star formation and feedback with the spheroid's parameters
   black holes      Bondi-Hoyle-Lyttleton accretion from the hot halo, capped by the hot
                    gas and the Eddington rate (accretion/Bondi_Hoyle_Lyttleton.F90:34-78,
                    black_holes/fundamentals.F90:123-138, accretion_rates/standard.F90:221-440)
@@ -157,3 +160,66 @@ def test_hot_mode_black_hole_accretion(oracle_mod, table, enhancement, binding):
     kept = 1.0 - params.bh_efficiency_radiative - params.bh_efficiency_jet
     assert d[_abi.Y_BLACK_HOLE] == pytest.approx(kept * accreted, rel=1e-12)
     assert d[_abi.Y_HOT_MASS] == pytest.approx(-accreted, rel=1e-12)
+
+
+def test_slow_cooling_infall_rate(oracle_mod, table):
+    """Below the outer radius the cooling rate is the infall of the cooling
+    radius, 4 pi r^2 rho(r) dr/dt (White-Frenk.F90:132-185), with the
+    growth rate of cooling_radius/simple.F90:229-311 for an isothermal
+    beta = 2/3 profile and CIE cooling (d ln t_cool / d ln rho = -1):
+    dr/dt = r / t_dyn / (2 x^2 / (1 + x^2)), x = r / r_core."""
+    params = only(_abi.PHYS_COOLING)
+    prm = node()
+    rvir = prm[_abi.P_RADIUS_VIRIAL]
+    y = np.zeros(_abi.NY)
+    y[_abi.Y_HOT_MASS], y[_abi.Y_HOT_METALS] = 8e10, 8e10 * 0.003
+    r = oracle_mod.cooling_radius(params, table, prm, y[_abi.Y_HOT_MASS], y[_abi.Y_HOT_METALS])
+    assert 0.0 < r < rvir
+    d = oracle_mod.rhs(params, table, prm, y)
+    tdyn = rvir / prm[_abi.P_VELOCITY_VIRIAL] * MPC_PER_KMS_TO_GYR
+    rc = params.core_radius_fraction * rvir
+    xo, x = rvir / rc, r / rc
+    rho = y[_abi.Y_HOT_MASS] / (4.0 * math.pi * rc ** 3) / (xo - math.atan(xo)) / (1.0 + x * x)
+    rate = 4.0 * math.pi * r * r * rho * r / tdyn / (2.0 * x * x / (1.0 + x * x))
+    assert d[_abi.Y_HOT_MASS] == pytest.approx(-rate, rel=1e-12)
+    assert d[_abi.Y_DISK_GAS] == pytest.approx(rate, rel=1e-12)
+    assert d[_abi.Y_DISK_GAS_METALS] == pytest.approx(rate * 0.003, rel=1e-12)
+
+
+def test_cgm_accretion(oracle_mod, table):
+    """Hot gas accretes the universal baryon fraction of the halo's growth,
+    metal-free (circumgalactic_medium/accretion.F90:517-593,
+    accretion/halo/simple.F90:281-319, failed fraction 0)."""
+    params = only(_abi.PHYS_CGM_ACCRETION)
+    d = oracle_mod.rhs(params, table, node(mdot=3e11), np.zeros(_abi.NY))
+    assert d[_abi.Y_HOT_MASS] == pytest.approx(params.omega_baryon / params.omega_matter * 3e11, rel=1e-14)
+    assert np.count_nonzero(d) == 1
+    assert np.all(oracle_mod.rhs(params, table, node(mdot=-1e11), np.zeros(_abi.NY)) == 0.0)
+
+
+@pytest.mark.parametrize("gas", [5e9, 5e-7])
+def test_spheroid_star_formation_and_feedback(oracle_mod, table, gas):
+    """The spheroid's own timescale and outflow parameters; below 1e-6 Msun
+    of gas nothing forms (star_formation/spheroids.F90:152-)."""
+    params = only(_abi.PHYS_STAR_FORMATION_SPHEROID | _abi.PHYS_FEEDBACK_SPHEROID)
+    prm = node()
+    y = np.zeros(_abi.NY)
+    y[_abi.Y_SPHEROID_GAS], y[_abi.Y_SPHEROID_GAS_METALS] = gas, gas * 0.01
+    d = oracle_mod.rhs(params, table, prm, y)
+    if gas < 1e-6:
+        assert np.all(d == 0.0)
+        return
+    sf, o = params.sf_spheroid, params.outflow_spheroid
+    radius = params.radius_factor_spheroid * prm[_abi.P_SPIN] * prm[_abi.P_RADIUS_VIRIAL]
+    v = prm[_abi.P_VELOCITY_VIRIAL]
+    tau = max(MPC_PER_KMS_TO_GYR * radius / v * (v / 200.0) ** sf.exponent_velocity / sf.efficiency,
+              sf.timescale_minimum)
+    sfr = gas / tau
+    stars = (1.0 - params.recycled_fraction) * sfr
+    outflow = min((o.velocity_characteristic / v) ** o.exponent * sfr,
+                  gas / (MPC_PER_KMS_TO_GYR * radius / v) / o.timescale_fractional_minimum)
+    assert d[_abi.Y_SPHEROID_STARS] == pytest.approx(stars, rel=1e-12)
+    assert d[_abi.Y_SPHEROID_GAS] == pytest.approx(-stars - outflow, rel=1e-12)
+    assert d[_abi.Y_OUTFLOWED_MASS] == pytest.approx(outflow, rel=1e-12)
+    assert d[_abi.Y_SPHEROID_GAS_METALS] == pytest.approx(
+        -0.01 * stars + params.metal_yield * sfr - 0.01 * outflow, rel=1e-12)
