@@ -223,3 +223,40 @@ def test_spheroid_star_formation_and_feedback(oracle_mod, table, gas):
     assert d[_abi.Y_OUTFLOWED_MASS] == pytest.approx(outflow, rel=1e-12)
     assert d[_abi.Y_SPHEROID_GAS_METALS] == pytest.approx(
         -0.01 * stars + params.metal_yield * sfr - 0.01 * outflow, rel=1e-12)
+
+
+def test_cooling_radius_from_the_cooling_time(oracle_mod, table):
+    """coolingRadiusSimple: the radius where the cooling time equals the
+    time available (coolingTimeAvailableWhiteFrenk1991 with ageFactor 0:
+    the halo dynamical time).  The cooling time is (dof/2) k T n_tot /
+    Lambda with n_tot = n_H / f_H + n_e (cooling_time/simple.F90:128-179;
+    abundances.F90:781-883 for the hydrogen mass and number fractions); with
+    CIE cooling it scales as 1/rho, so r = r_core sqrt(t_avail/t_cool(0) - 1).
+    The table is interpolated here by the Python restatement."""
+    from galacticus_gb300.cie_tables import _interp_ln
+    params = workloads.isolated_params()
+    prm = node()
+    rvir, v = prm[_abi.P_RADIUS_VIRIAL], prm[_abi.P_VELOCITY_VIRIAL]
+    mass_hot, z = 8e10, 0.003
+    amu, kB, m_h = 1.660538782e-27, 1.3806504e-23, 1.0078250322 * 1.660538782e-27
+    mu = 1.0 / (2.0 * 0.7514 / 1.0078250322 + 3.0 * 0.2486 / 4.0026032545)
+    temperature = 0.5 * amu * mu * (1e3 * v) ** 2 / kB
+    rc = params.core_radius_fraction * rvir
+    xo = rvir / rc
+    rho0 = mass_hot / (4.0 * math.pi * rc ** 3) / (xo - math.atan(xo))
+    x_h = min(max(z / 0.0188 * (0.7070 - 0.7514) + 0.7514, 0.7), 0.7514)
+    y_he = min(z / 0.0188 * (0.2740 - 0.2486) + 0.2486, 0.2486)
+    f_h = (x_h / 1.0078250322) / (x_h / 1.0078250322 + y_he / 4.0026032545)
+    n_h = rho0 * x_h * 1.98892e30 / m_h / 1e6 / MEGAPARSEC ** 3
+    z_solar = z / 0.0188
+    lam = table.interpolate_cooling(n_h, temperature, z_solar)
+    n_e = _interp_ln(np.log(table.electron_density), np.log(table.temperature), table.metallicity,
+                     np.log(temperature), z_solar) * n_h
+    t_cool = params.cooling_degrees_of_freedom / 2.0 * kB * temperature * (n_h / f_h + n_e) / 1e-7 / lam / GIGAYEAR
+    t_avail = rvir / v * MPC_PER_KMS_TO_GYR
+    expected = min(max(rc * math.sqrt(max(t_avail / t_cool - 1.0, 0.0)), 0.0), rvir)
+    assert 0.0 < expected < rvir
+    closed = oracle_mod.cooling_radius(params, table, prm, mass_hot, mass_hot * z, brent=False)
+    brent = oracle_mod.cooling_radius(params, table, prm, mass_hot, mass_hot * z, brent=True)
+    assert closed == pytest.approx(expected, rel=1e-12)
+    assert brent == pytest.approx(expected, rel=1e-6)
