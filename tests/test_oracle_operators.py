@@ -17,7 +17,8 @@ operator enabled; the constants are the reference's GSL MKSA values).
   gas accretion    Omega_b / Omega_m of the halo's growth (accretion/halo/simple.F90:281-319)
   spheroids        star formation and feedback with the spheroid's parameters
   black holes      Bondi-Hoyle-Lyttleton accretion from the hot halo, capped by the hot
-                   gas and the Eddington rate (accretion/Bondi_Hoyle_Lyttleton.F90:34-78,
+                   gas and the Eddington rate, and from the spheroid gas with the Jeans
+                   length (accretion/Bondi_Hoyle_Lyttleton.F90:34-78,
                    black_holes/fundamentals.F90:123-138, accretion_rates/standard.F90:221-440)
 """
 
@@ -260,3 +261,43 @@ def test_cooling_radius_from_the_cooling_time(oracle_mod, table):
     brent = oracle_mod.cooling_radius(params, table, prm, mass_hot, mass_hot * z, brent=True)
     assert closed == pytest.approx(expected, rel=1e-12)
     assert brent == pytest.approx(expected, rel=1e-6)
+
+
+@pytest.mark.parametrize("mass_bh,jeans_branch", [(1e7, False), (1e4, True)])
+def test_spheroid_black_hole_accretion(oracle_mod, table, mass_bh, jeans_branch):
+    """Bondi-Hoyle-Lyttleton accretion from the spheroid gas at the
+    spheroid temperature (accretion_rates/standard.F90:262-300): the
+    Hernquist gas density at the accretion radius G M / c_s^2, or at the
+    Jeans length c_s / sqrt(G rho) (limited to the spheroid radius) when that
+    is larger (thermodynamics/ideal_gases.F90:34-69,
+    accretion/Bondi_Hoyle_Lyttleton.F90:34-78)."""
+    params = only(_abi.PHYS_BLACK_HOLE_ACCRETION)
+    prm = node()
+    y = np.zeros(_abi.NY)
+    y[_abi.Y_SPHEROID_GAS], y[_abi.Y_SPHEROID_GAS_METALS], y[_abi.Y_BLACK_HOLE] = 1e9, 1e7, mass_bh
+    d = oracle_mod.rhs(params, table, prm, y)
+    amu, kB = 1.660538782e-27, 1.3806504e-23
+    mu = 1.0 / (2.0 * 0.7514 / 1.0078250322 + 3.0 * 0.2486 / 4.0026032545)
+    cs = math.sqrt(5.0 * kB * params.bh_temperature_spheroid / 3.0 / mu / amu) / 1e3
+    g_internal = G_SI * 1.98892e30 / 1e6 / MEGAPARSEC
+    a = params.radius_factor_spheroid * prm[_abi.P_SPIN] * prm[_abi.P_RADIUS_VIRIAL]
+
+    def hernquist(r):
+        x = r / a
+        return y[_abi.Y_SPHEROID_GAS] / (2.0 * math.pi * a ** 3) / (x * (1.0 + x) ** 3)
+
+    r_acc = g_internal * mass_bh / cs ** 2
+    rho = hernquist(r_acc)
+    assert rho > 1.0
+    jeans = min(cs / math.sqrt(g_internal) / math.sqrt(rho), a)
+    assert (jeans > r_acc) == jeans_branch
+    if jeans > r_acc:
+        rho = hernquist(jeans)
+    rate = params.bh_enhancement_spheroid * 1e3 * GIGAYEAR / MEGAPARSEC * 4.0 * math.pi * (g_internal * mass_bh) ** 2 \
+        * rho / cs ** 3
+    eddington = mass_bh * 4.0 * math.pi * G_SI * M_H * GIGAYEAR / SIGMA_T / C_LIGHT / params.bh_efficiency_radiative
+    rate = min(rate, eddington)
+    kept = 1.0 - params.bh_efficiency_radiative - params.bh_efficiency_jet
+    assert d[_abi.Y_BLACK_HOLE] == pytest.approx(kept * rate, rel=1e-12)
+    assert d[_abi.Y_SPHEROID_GAS] == pytest.approx(-rate, rel=1e-12)
+    assert d[_abi.Y_SPHEROID_GAS_METALS] == pytest.approx(-rate * 1e7 / 1e9, rel=1e-12)
