@@ -48,7 +48,9 @@ N_NODES = 65536
 WORKLOAD = "isolated-halo step: 65,536 halos/GPU, M 1e10-1e14 Msun, dt 0.01-1 Gyr, rel tol 1e-3, P-std physics"
 TREES_WORKLOAD = ("uneven trees: {} PCH trees (seed 3), roots dN/dlnM ~ M^-0.9 on 1e10-1e14 Msun, resolution "
                   "1e8 Msun, z=8->0 with 20 outputs, rel tol 1e-3")
-GATES = (0.01, 0.005, 0.003, 0.002)  # error-map tolerances tried for the surrogate form (dex)
+# Error-map gates tried for the surrogate form (dex), loose to tight; the
+# table alone comes after them.
+GATES = (0.01, 0.003, 0.001, 0.0003, 0.0001)
 MLP_FLOPS = 2 * (3 * 64 + 64 * 64 + 64 * 64 + 64)  # per network evaluation
 # dram__bytes_read.sum + dram__bytes_write.sum of the headline kernel (the
 # surrogate form on this workload) from one ncu --set full capture, per launch.
@@ -65,12 +67,13 @@ def parse():
     ap.add_argument("--form", choices=["compare", "plain", "fast", "surrogate", "trees-plain", "trees-fast",
                                        "trees-surrogate"], default="compare",
                     help="compare: the headline run; otherwise time one form alone (for profiling)")
-    ap.add_argument("--gate", type=float, default=0.003, help="error-map tolerance of --form surrogate (dex)")
+    ap.add_argument("--gate", type=float, default=0.003,
+                    help="error-map tolerance of --form surrogate and --workload scale (dex; 0: the table alone)")
     ap.add_argument("--trees", type=int, default=4096, help="trees of the uneven-trees workload (0: skip it)")
     ap.add_argument("--tree-steps", type=int, default=2, help="timed evolutions of the whole forest per form")
     ap.add_argument("--workload", choices=["isolated", "scale"], default="isolated",
                     help="scale: the full chosen form on a forest at scale (one JSON line of its own)")
-    ap.add_argument("--trees-scale", type=int, default=65536, help="trees of the scale workload")
+    ap.add_argument("--trees-scale", type=int, default=65536, help="trees of the scale workload (0: skip it)")
     ap.add_argument("--halo", type=int, default=-1,
                     help="with a single --form: evolve only this halo of the batch (profiling the batch's tail)")
     return ap.parse_args()
@@ -225,6 +228,28 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def oracle_mod():
+    from oracle import oracle
+    return oracle
+
+
+def lambda_sensitivity(params, table, batch, ref, dexes=(1e-4, 3e-4, 1e-3, 3e-3, 1e-2)):
+    """What a systematic error in Lambda does to the per-halo bar: the
+    oracle rerun with every cooling rate scaled by 10^dex, and the share of
+    halos above 1e6 Msun whose stellar and cold-gas masses stay within 1e-3
+    (a network used in a halo's cells shifts its Lambda by about its
+    deployed error there)."""
+    from oracle import compare, oracle
+    out = {}
+    for dex in dexes:
+        m = oracle.evolve_batch(params, compare.perturbed_table(table, dex), batch.state, batch.param, batch.t_start,
+                                batch.t_end, batch.step, threads=os.cpu_count() or 1)[0]
+        errs = compare.relative_mass_errors(m, ref)
+        out[str(dex)] = {name: {"share_within_1e-3": float(np.mean(rel[big] <= 1e-3)),
+                                "p99": float(np.percentile(rel[big], 99))} for name, (rel, big) in errs.items()}
+    return out
+
+
 def mass_errors(gpu, ref):
     """Final stellar (disk + spheroid stars) and cold-gas (disk + spheroid
     gas) masses against the FP64 oracle: relative error of the population
@@ -282,7 +307,7 @@ def run_trees(args, params, table, net, gate, rank, dist, device):
     results = {}
     for name, rates in (("plain", "fp64"), ("fast_no_network", "fp32"), ("surrogate", "fp32")):
         ev = MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision=rates)
-        if name == "surrogate":
+        if name == "surrogate" and gate is not None:
             net.build_error_map(table, tolerance=gate)
             net.install(ev)
         fe = forest.ForestEvolver(ev, f, state0, times)
@@ -294,7 +319,7 @@ def run_trees(args, params, table, net, gate, rank, dist, device):
         elif name == "fast_no_network":
             ev.set_launch(128, 2)
         fe.evolve()
-        s0 = surrogate.stats(ev) if name == "surrogate" else (0, 0)
+        s0 = surrogate.stats(ev) if name == "surrogate" and gate is not None else (0, 0)
         reps = max(1, args.tree_steps)
         if dist:
             dist.barrier()
@@ -310,7 +335,7 @@ def run_trees(args, params, table, net, gate, rank, dist, device):
         entry = {"value": accepted_all / dt, "s_per_evolution": dt, "accepted_steps": acc, "launch": list(ev.get_launch()),
                  "failed_nodes": int((status != 0).sum())}
         if name == "surrogate":
-            s1 = surrogate.stats(ev)
+            s1 = surrogate.stats(ev) if gate is not None else (0, 0)
             entry["network_share"] = (s1[0] - s0[0]) / max(1, (s1[0] - s0[0]) + (s1[1] - s0[1]))
             entry["gate_dex"] = gate
         results[name] = state
@@ -331,39 +356,39 @@ def run_trees(args, params, table, net, gate, rank, dist, device):
     return out
 
 
-def run_scale(args):
-    """The full chosen form at scale: 65,536 PCH trees (seed 5), z=10->0 with
-    50 outputs, the surrogate form with the table fallback against the plain
-    GPU form and the CPU oracle (one evolution of each, after a warm-up)."""
-    import torch
+def scale_record(args, params, table, net, gate):
+    """The full chosen form at scale (65,536 PCH trees, seed 5, roots
+    dN/dlnM ~ M^-0.9 on 1e10-1e14 Msun, resolution 1e8 Msun, z=10->0 with
+    50 outputs, rel tol 1e-3): one warm-up and one timed evolution of the
+    plain GPU form and of the surrogate form at `gate` (None: the table
+    alone), the surrogate's fallback rate, final-mass errors of the roots
+    against the plain GPU form, and against the CPU oracle on a sample of
+    the trees (every 128th tree, evolved on all host cores; its time is the
+    CPU baseline)."""
     from galacticus_gb300 import _abi, forest, surrogate, workloads
-    from galacticus_gb300.cie_tables import CieTable
     from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
     from oracle import oracle
-    torch.cuda.set_device(0)
-    params = workloads.isolated_params()
-    table = CieTable()
     t0 = time.perf_counter()
     f = forest.build(params, n_trees=args.trees_scale, seed=5, redshift_max=10.0)
     build_s = time.perf_counter() - t0
     state0 = forest.initial_state(params, f)
     times = forest.output_times(params, n=50, redshift_max=10.0)
-    net = surrogate.train(table)
-    out = {"workload": f"scale: {args.trees_scale} PCH trees (seed 5), roots dN/dlnM ~ M^-0.9 on 1e10-1e14 Msun, resolution "
-                       f"1e8 Msun, z=10->0 with 50 outputs, rel tol 1e-3", "metric": METRIC, "unit": UNIT,
+    out = {"workload": f"scale: {args.trees_scale} PCH trees (seed 5), roots dN/dlnM ~ M^-0.9 on 1e10-1e14 Msun, "
+                       f"resolution 1e8 Msun, z=10->0 with 50 outputs, rel tol 1e-3", "metric": METRIC, "unit": UNIT,
            "nodes": f.n, "leaves": int((f.child_count == 0).sum()), "max_tree_nodes": int(np.bincount(f.tree).max()),
-           "build_s": build_s, "forms": {}}
-    states = {}
+           "build_s": build_s, "timing": "host clock around one graph launch and its completion, after one warm-up",
+           "forms": {}}
+    states, counts = {}, {}
     for name, rates in (("plain", "fp64"), ("surrogate", "fp32")):
         ev = MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision=rates)
         ev.set_launch(128, 1 if rates == "fp64" else 2)
-        if name == "surrogate":
-            net.build_error_map(table, tolerance=args.gate)
+        if name == "surrogate" and gate is not None:
+            net.build_error_map(table, tolerance=gate)
             net.install(ev)
         fe = forest.ForestEvolver(ev, f, state0, times)
         out["snapshots"] = fe.snapshot_count()
         fe.evolve()
-        s0 = surrogate.stats(ev) if name == "surrogate" else (0, 0)
+        s0 = surrogate.stats(ev) if name == "surrogate" and gate is not None else (0, 0)
         tb = time.perf_counter()
         fe.evolve()
         dt = time.perf_counter() - tb
@@ -371,21 +396,28 @@ def run_scale(args):
         entry = {"value": float(counters[0].sum()) / dt, "s_per_evolution": dt, "accepted_steps": int(counters[0].sum()),
                  "rhs_evaluations": int(counters[2].sum()), "failed_nodes": int((status != 0).sum())}
         if name == "surrogate":
-            s1 = surrogate.stats(ev)
+            s1 = surrogate.stats(ev) if gate is not None else (0, 0)
             served = s1[0] - s0[0]
-            entry["gate_dex"] = args.gate
+            entry["gate_dex"] = gate
             entry["fallback_rate"] = 1.0 - served / max(1, served + (s1[1] - s0[1]))
         states[name] = state
+        counts[name] = counters
         out["forms"][name] = entry
         fe.close()
         ev.close()
+    # The CPU oracle on every 128th tree (trees are independent: each one's
+    # GPU result is its result alone).
+    sample = np.arange(0, f.n_trees, 128)
+    sub, idx = f.subset(sample)
     tb = time.perf_counter()
-    ref = oracle.evolve_forest(params, table, f, state0, times, threads=os.cpu_count() or 1, brent=True)[0]
+    ref = oracle.evolve_forest(params, table, sub, forest.initial_state(params, sub), times,
+                               threads=os.cpu_count() or 1, brent=True)[0]
     cpu_s = time.perf_counter() - tb
-    out["cpu_baseline"] = {"value": out["forms"]["plain"]["accepted_steps"] / cpu_s, "unit": UNIT,
-                           "cores": os.cpu_count() or 1, "kind": "port", "sample": f"one evolution of the whole forest ({cpu_s:.1f} s)"}
-    out["forms"]["plain"]["mass_error_vs_cpu"] = forest_mass_errors(states["plain"], ref, f)
-    out["forms"]["surrogate"]["mass_error_vs_cpu"] = forest_mass_errors(states["surrogate"], ref, f)
+    acc_sample = int(counts["plain"][0][idx].sum())
+    out["cpu_baseline"] = {"value": acc_sample / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                           "sample": f"{len(sample)} of the trees ({sub.n} nodes), one evolution ({cpu_s:.1f} s)"}
+    for name in states:
+        out["forms"][name]["mass_error_vs_cpu_sample"] = forest_mass_errors(states[name][:, idx], ref, sub)
     out["forms"]["surrogate"]["mass_error_vs_plain_gpu"] = forest_mass_errors(states["surrogate"], states["plain"], f)
     out["speedup_surrogate_vs_plain"] = out["forms"]["surrogate"]["value"] / out["forms"]["plain"]["value"]
     # Rooflines: the reference's FP64 work per RHS evaluation (counted by the
@@ -418,7 +450,19 @@ def run_scale(args):
                              "hbm": {"achieved_gbs": nbytes / entry["s_per_evolution"] / 1e9, "peak_gbs": peaks.get("hbm_gbs"),
                                      "frac": (nbytes / entry["s_per_evolution"] / 1e9 / peaks["hbm_gbs"]) if peaks.get("hbm_gbs") else None}}
     out["flops_per_rhs"] = f_rhs
-    print(json.dumps(out), flush=True)
+    return out
+
+
+def run_scale(args):
+    """--workload scale: the scale record alone (the surrogate at --gate)."""
+    import torch
+    from galacticus_gb300 import surrogate, workloads
+    from galacticus_gb300.cie_tables import CieTable
+    torch.cuda.set_device(0)
+    params = workloads.isolated_params()
+    table = CieTable()
+    net = surrogate.train(table)
+    print(json.dumps(scale_record(args, params, table, net, args.gate if args.gate > 0 else None)), flush=True)
 
 
 def run_ours(args):
@@ -501,14 +545,15 @@ def run_ours(args):
             raise RuntimeError("node evolution failed")
         return state.cpu().numpy()
 
-    def timed(ev, clocks=None):
-        """W warm-up passes, then K passes bracketed by barrier + synchronize."""
+    def timed(ev, clocks=None, passes=None):
+        """W warm-up passes, then K passes (or `passes`) bracketed by barrier + synchronize."""
+        steps = passes or args.steps
         for _ in range(max(args.warmup, 3)):
             one_step(ev)
         torch.cuda.synchronize()
         assert int((status != 0).sum()) == 0, "node evolution failed during warm-up"
         accepted = int(counters[0].sum())
-        evs = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(4)) for _ in range(args.steps)]
+        evs = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(4)) for _ in range(steps)]
         launches0 = lib.gal_gpu_launch_count(ev.ctx)
         if dist:
             dist.barrier()
@@ -527,8 +572,11 @@ def run_ours(args):
             dist.barrier()
         total_ms = sum(a.elapsed_time(b) for a, b, _, _ in evs)
         kernel_ms = statistics.mean(a.elapsed_time(b) for _, _, a, b in evs)
-        total_ms, accepted_all = reduce_over_ranks(dist, dev, total_ms, accepted)
-        return {"value": accepted_all * args.steps / (total_ms * 1e-3), "ms_per_step": total_ms / args.steps,
+        if passes is None:
+            total_ms, accepted_all = reduce_over_ranks(dist, dev, total_ms, accepted)
+        else:
+            accepted_all = accepted  # a rank-0 side measurement
+        return {"value": accepted_all * steps / (total_ms * 1e-3), "ms_per_step": total_ms / steps,
                 "kernel_ms": kernel_ms, "accepted_per_pass": accepted, "launches": lib.gal_gpu_launch_count(ev.ctx) - launches0,
                 "wall_ms": wall * 1e3, "clocks": sampler.summary() if sampler else None}
 
@@ -582,44 +630,71 @@ def run_ours(args):
     if rank == 0:
         cpu, ref = cpu_baseline(params, table, batch)
 
-    # Error-map gate of the surrogate form: the loosest of GATES whose total
-    # stellar and cold-gas errors stay within 1e-3 (decided on rank 0).
-    gate_results = {}
-    chosen = GATES[-1]
-    for gate in GATES:
+    # Error-map gate of the surrogate form, chosen by the per-halo bar: the
+    # loosest of GATES at which 99.5% of the well-conditioned halos keep their
+    # final stellar and cold-gas masses within 1e-3 of the FP64 oracle (halos
+    # whose oracle masses themselves move by more than 1e-3 when the
+    # tolerance changes by 10% or Lambda by 1e-4 dex are exempt).  None: no
+    # gate with the network meets the bar and the form runs on the table.
+    # Decided on rank 0.
+    from oracle import compare
+    movement = sensitivity_lambda = None
+    if rank == 0:
+        movement, _ = compare.conditioning(oracle_mod(), params, table, batch, ref, threads=os.cpu_count() or 1)
+        sensitivity_lambda = lambda_sensitivity(params, table, batch, ref)
+
+    totals = {}
+
+    def run_gate(gate):
+        ev = forms["surrogate"]
+        if gate is None:
+            net.uninstall(ev)
+            out = final_state(ev)
+            totals[gate] = mass_errors(out, ref)
+            return out, 0.0
         net.build_error_map(table, tolerance=gate)
-        net.install(forms["surrogate"])
-        out = final_state(forms["surrogate"])
-        if rank == 0:
-            err = mass_errors(out, ref)
-            gate_results[gate] = {"errors": err, "table_cells": float(net.use_table.mean())}
-            if err["max_total"] <= 1e-3:
-                chosen = gate
-                break
+        net.install(ev)
+        a = surrogate.stats(ev)
+        out = final_state(ev)
+        b = surrogate.stats(ev)
+        totals[gate] = mass_errors(out, ref)
+        return out, (b[0] - a[0]) / max(1, (b[0] - a[0]) + (b[1] - a[1]))
+
+    gate_results = {}
+    chosen = None
+    if rank == 0:
+        chosen, gate_results = compare.select_gate(run_gate, ref, movement, GATES + (None,))
+        for gate, rec in gate_results.items():
+            if gate is not None:
+                net.build_error_map(table, tolerance=gate)
+                net.install(forms["surrogate"])
+                rec["table_cells"] = float(net.use_table.mean())
+            else:
+                net.uninstall(forms["surrogate"])
+                rec["table_cells"] = 1.0
+            rec["value"] = timed(forms["surrogate"], passes=10)["value"]
     if dist:
-        g = torch.tensor([chosen], device=dev, dtype=torch.float64)
+        g = torch.tensor([-1.0 if chosen is None else chosen], device=dev, dtype=torch.float64)
         dist.broadcast(g, 0)
-        chosen = float(g.item())
-    spec = {}
-    if chosen != GATES[0]:
-        net.build_error_map(table, tolerance=GATES[0])
+        chosen = None if float(g.item()) < 0 else float(g.item())
+    if chosen is None:
+        net.uninstall(forms["surrogate"])
+    else:
+        net.build_error_map(table, tolerance=chosen)
         net.install(forms["surrogate"])
-        spec = timed(forms["surrogate"])
-        spec.update(gate_results.get(GATES[0], {}))
-        spec["gate_dex"] = GATES[0]
-        spec["network_share"] = None
-    net.build_error_map(table, tolerance=chosen)
-    net.install(forms["surrogate"])
-    s0 = surrogate.stats(forms["surrogate"])
+    s0 = surrogate.stats(forms["surrogate"]) if chosen is not None else (0, 0)
     headline = timed(forms["surrogate"], clocks=True)
-    s1 = surrogate.stats(forms["surrogate"])
+    s1 = surrogate.stats(forms["surrogate"]) if chosen is not None else (0, 0)
     network_share = (s1[0] - s0[0]) / max(1, (s1[0] - s0[0]) + (s1[1] - s0[1]))
     others = {name: timed(forms[name]) for name in ("plain", "fast")}
     if rank == 0:
         for name in ("plain", "fast"):
-            others[name]["mass_error"] = mass_errors(final_state(forms[name]), ref)
+            st = final_state(forms[name])
+            others[name]["mass_error"] = mass_errors(st, ref)
+            others[name]["bar"] = compare.bar_shares(st, ref, movement)
 
     trees = run_trees(args, params, table, net, chosen, rank, dist, dev) if args.trees > 0 else None
+    scale = scale_record(args, params, table, net, chosen) if rank == 0 and args.trees_scale > 0 else None
 
     # End-to-end through the public host API (pinned host buffers, copies in the timed region).
     ev = forms["surrogate"]
@@ -662,33 +737,44 @@ def run_ours(args):
         bytes_launch = n * ((_abi.NY + _abi.NP + 3) * 8 + (_abi.NY + 1) * 8 + 4 + 12)
         net_evals = (s1[0] - s0[0]) / max(1, args.steps)  # network evaluations (one per node and RHS) per pass
         mlp_tflops = net_evals * MLP_FLOPS / (k_ms * 1e-3) / 1e12
-        err = gate_results[chosen]["errors"]
+        err = totals[chosen]
+        bar = gate_results[chosen]
+        form = ("batched surrogate (fp32 rates + MLP cooling, table fallback)" if chosen is not None else
+                "batched fp32-rate form with the surrogate gated off: no error-map gate with the network meets the "
+                "per-halo bar, so every cooling evaluation uses the table")
         line = {
             "metric": METRIC, "value": headline["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": headline["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64 state, error norm and step control; f32 rates; MLP on bf16 tensor cores (split hi/lo operands, f32 accumulate)",
+            "dtype": "f64 state, error norm and step control; f32 rates" +
+                     ("; MLP on bf16 tensor cores (split hi/lo operands, f32 accumulate)" if chosen is not None else ""),
             "data": "synthetic (seeded Philox halos; reference datasets absent)",
-            "config": {"workload": WORKLOAD, "nodes_per_gpu": n, "form": "batched surrogate (fp32 rates + MLP cooling, table fallback)",
+            "config": {"workload": WORKLOAD, "nodes_per_gpu": n, "form": form,
                        "gate_dex": chosen, "l2": "flushed between timed iterations (256 MB memset outside the kernel event pair)",
                        "launch": list(forms["surrogate"].get_launch()), "accepted_steps_per_pass": acc},
             "speedup_vs_plain": headline["value"] / others["plain"]["value"],
             "mass_error": err,
+            "per_halo_bar": {"criterion": "stellar and cold-gas mass within 1e-3 of the FP64 oracle for >= 99.5% of "
+                                          "the well-conditioned halos above 1e6 Msun (exempt: oracle masses that move "
+                                          "by > 1e-3 under rel tol x0.9/x1.1 or Lambda x10^(+-1e-4))",
+                             "headline": bar, "network_meets_bar": chosen is not None,
+                             "lambda_sensitivity": sensitivity_lambda},
             "forms": {
                 "surrogate": {"value": headline["value"], "ms_per_step": headline["ms_per_step"], "gate_dex": chosen,
-                              "table_cells": gate_results[chosen]["table_cells"], "network_share": network_share,
-                              "mass_error": err},
-                "plain": {k: others["plain"][k] for k in ("value", "ms_per_step", "mass_error")},
-                "fast_no_network": {k: others["fast"][k] for k in ("value", "ms_per_step", "mass_error")},
+                              "table_cells": bar["table_cells"], "network_share": network_share,
+                              "mass_error": err, "bar": bar},
+                "plain": {k: others["plain"][k] for k in ("value", "ms_per_step", "mass_error", "bar")},
+                "fast_no_network": {k: others["fast"][k] for k in ("value", "ms_per_step", "mass_error", "bar")},
             },
             "surrogate": {"train_s": train_s, "val_rms_dex": net.rms_dex, "samples": 2_000_000, "epochs": 20,
-                          "gates_tried": {str(k): v for k, v in gate_results.items()}},
+                          "map_cells_dex": list(net.map_step),
+                          "gates_tried": {str(k): dict(v, totals=totals[k]) for k, v in gate_results.items()}},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(headline["launches"]),
             "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": flops_peak.value / 1e12, "unit": "TFLOP/s",
                          "frac": achieved / flops_peak.value, "traffic": HEADLINE_DRAM_BYTES,
                          "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
-                         "basis": "the reference's FP64 work per node-timestep (counted by the oracle) over the surrogate-form "
+                         "basis": "the reference's FP64 work per node-timestep (counted by the oracle) over the headline "
                                   "kernel time: an FP64-equivalent rate, since this form runs the rates on the FP32 pipe "
                                   "and keeps FP64 for the state, error norm and step control",
                          "peak_source": "measured by gal_calibrate_fp64 (DFMA loop on all SMs); MEASURED_PEAKS.json has no FP64 figure",
@@ -696,8 +782,7 @@ def run_ours(args):
                          "tensor": {"achieved": mlp_tflops, "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
                                     "frac": mlp_tflops / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
                                     "basis": "the MLP's flops (16,896 per evaluation) times the network evaluations "
-                                             "per pass (one per node and RHS that used it), over the kernel time; the "
-                                             "tensor cores execute three split-BF16 products per flop and whole 16-row tiles"},
+                                             "per pass (one per node and RHS that used it), over the kernel time"},
                          "hbm": {"achieved": bytes_launch / (k_ms * 1e-3) / 1e9, "peak": peaks.get("hbm_gbs"),
                                  "unit": "GB/s", "bytes_per_launch": bytes_launch}},
             "wall_ms_timed_region": headline["wall_ms"],
@@ -706,8 +791,8 @@ def run_ours(args):
         }
         if trees:
             line["trees"] = trees
-        if spec:
-            line["forms"]["surrogate_gate_0.01"] = {k: spec.get(k) for k in ("value", "ms_per_step", "errors", "table_cells")}
+        if scale:
+            line["scale"] = scale
         print(json.dumps(line), flush=True)
     for ev in forms.values():
         ev.close()

@@ -557,6 +557,39 @@ __global__ void noalloc_prepare_tables(double2* tab, double* lnT, double* lnZ, i
   }
 }
 
+// The grid-spacing constants gal_gpu_init derives (evenly spaced rows in
+// ln Z and ln T: the cell is found by arithmetic), computed from the raw
+// grids one logarithm at a time so that nothing is allocated; then the FP32
+// copies.  Same Globals as a context built from the same table.
+void noalloc_uniform_grids(Globals& g, const double* temperature, const double* metallicity, int nT, int nZ) {
+  auto lnZ = [&](int j) { return metallicity[j] > 0.0 ? std::log(metallicity[j]) : -999.0; };
+  const int first = g.firstZero ? 1 : 0;
+  g.zFirstLog = first;
+  g.lnZFirst = lnZ(first);
+  g.zUniform = 0;
+  if (nZ - first >= 2) {
+    const double d = (lnZ(nZ - 1) - lnZ(first)) / (nZ - 1 - first);
+    bool even = true;
+    for (int j = first; j + 1 < nZ && even; ++j) even = std::fabs(lnZ(j + 1) - lnZ(j) - d) <= 1.0e-9 * std::fabs(d);
+    if (even) {
+      g.invDlnZ = 1.0 / d;
+      g.zUniform = 1;
+    }
+  }
+  fill_fast_constants(g);
+  g.tUniform = 0;
+  const double lnT0 = std::log(temperature[0]);
+  const double d = (std::log(temperature[nT - 1]) - lnT0) / (nT - 1);
+  bool even = true;
+  for (int i = 0; i + 1 < nT && even; ++i)
+    even = std::fabs(std::log(temperature[i + 1]) - std::log(temperature[i]) - d) <= 1.0e-9 * std::fabs(d);
+  if (even) {
+    g.f.lnTFirst = (float)lnT0;
+    g.f.invDlnT = (float)(1.0 / d);
+    g.tUniform = 1;
+  }
+}
+
 }  // namespace
 
 extern "C" int gal_gpu_evolve_batch_noalloc(const gal_params* p, const gal_cie_table* t, int64_t n, double* state,
@@ -570,10 +603,14 @@ extern "C" int gal_gpu_evolve_batch_noalloc(const gal_params* p, const gal_cie_t
   if (!(p->ode_tolerance_absolute > 0.0 || p->ode_tolerance_relative > 0.0) || p->ode_tolerance_absolute < 0.0 ||
       p->ode_tolerance_relative < 0.0 || p->trial_count_maximum < 1 || p->trial_count_maximum > 30)
     return fail(nullptr, GAL_ERR_ARGUMENT, "gal_gpu_evolve_batch_noalloc: invalid tolerances or trial count%s");
+  if ((unsigned long long)n * GAL_NY > (1ull << 62))
+    return fail(nullptr, GAL_ERR_TOO_LARGE, "gal_gpu_evolve_batch_noalloc: batch too large%s");
   const int nT = t->n_temperature, nZ = t->n_metallicity;
   if (nT < 2 || nZ < 2 || !t->temperature || !t->metallicity || !t->cooling_rate || !t->electron_density)
     return fail(nullptr, GAL_ERR_TABLE, "gal_gpu_evolve_batch_noalloc: CIE table needs at least 2x2 entries%s");
-  if (noalloc_bytes(nT, nZ) > kNoAllocScratchBytes)
+  // The cell count first, in 64-bit arithmetic, so that the int sizes below
+  // cannot overflow for an absurd table.
+  if ((uint64_t)nT * (uint64_t)nZ > kNoAllocScratchBytes / sizeof(double2) || noalloc_bytes(nT, nZ) > kNoAllocScratchBytes)
     return fail(nullptr, GAL_ERR_TOO_LARGE,
                 "gal_gpu_evolve_batch_noalloc: CIE table too large for the fixed 128 KiB scratch "
                 "(16 (n_metallicity*n_temperature + 128) + 8 (n_temperature + 2 n_metallicity + 64) + 256 bytes must not exceed 131072)%s");
@@ -630,7 +667,7 @@ extern "C" int gal_gpu_evolve_batch_noalloc(const gal_params* p, const gal_cie_t
   g.bhRadiusSpheroidCoef = k::gravitationalConstantInternal / (cs * cs);
   g.coolingCoef = p->cooling_degrees_of_freedom / 2.0 * k::boltzmannsConstant / k::ergs / k::gigaYear / k::densityToHydrogenNumber;
   g.accretionFraction = p->omega_baryon / p->omega_matter;
-  fill_fast_constants(g);
+  noalloc_uniform_grids(g, t->temperature, t->metallicity, nT, nZ);
 
   cudaStream_t st = (cudaStream_t)stream;
   int sms = 0;

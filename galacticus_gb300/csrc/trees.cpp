@@ -184,33 +184,39 @@ struct GrowthTable {
   }
 };
 
-struct Builder {
+// Branching rates of the PCH algorithm for a branch of mass M2 at w.  The
+// modifier G = G0 (sigma1/sigma2)^gamma1 (w/sigma2)^gamma2 factors into a
+// part that depends on M2 alone and (w/sigma2)^gamma2, so the split rate R,
+// the sub-resolution accretion rate F and the distribution of the split's
+// mass ratio q are integrated once per mass on a grid in ln M2 (RateTable)
+// and scaled by (w/sigma2)^gamma2 along each branch.
+struct Rates {
   const SigmaTable& sig;
   gal_pch_params pch;
-  double mRes, wMax;
+  double mRes;
+  static constexpr int kNq = 96;  // trapezoid points in ln q (1e-5 of the analytic rate)
 
-  // G = G0 (sigma1/sigma2)^gamma1 (w/sigma2)^gamma2
-  double modifier(double s1, double s2, double w) const {
-    return pch.g0 * std::pow(s1 / s2, pch.gamma1) * std::pow(w / s2, pch.gamma2);
-  }
+  // G without its w factor: G0 (sigma1/sigma2)^gamma1.
+  double modifier_mass(double s1, double s2) const { return pch.g0 * std::pow(s1 / s2, pch.gamma1); }
 
-  // Split rate R (per unit w) of a branch (M2, w) with its cumulative
-  // distribution over ln q on nq points from ln q_res to ln 1/2.
-  double split_rate(double M2, double w, std::vector<double>& lnq, std::vector<double>& cdf) const {
-    const int nq = 48;
+  // R / (w/sigma2)^gamma2 with its cumulative distribution over ln q on kNq
+  // points from ln(mRes/M2) to ln 1/2:
+  //   R = int q dN/dq dln q,  q dN/dq = (1/sqrt(2 pi)) |dS1/dln M1| q^-1 (S1 - S2)^-3/2 G.
+  double split_rate(double M2, double* lnq, double* cdf) const {
     const double qRes = mRes / M2;
-    lnq.resize(nq);
-    cdf.resize(nq);
     if (qRes >= 0.5) {
-      std::fill(cdf.begin(), cdf.end(), 0.0);
+      for (int i = 0; i < kNq; ++i) {
+        lnq[i] = std::log(0.5);
+        cdf[i] = 0.0;
+      }
       return 0.0;
     }
     double lns2, sl2;
     sig.at(M2, lns2, sl2);
     const double S2 = std::exp(2.0 * lns2), s2 = std::sqrt(S2);
-    const double a = std::log(qRes), b = std::log(0.5), d = (b - a) / (nq - 1);
+    const double a = std::log(qRes), b = std::log(0.5), d = (b - a) / (kNq - 1);
     double prev = 0.0;
-    for (int i = 0; i < nq; ++i) {
+    for (int i = 0; i < kNq; ++i) {
       lnq[i] = a + i * d;
       const double q = std::exp(lnq[i]);
       double lns1, sl1;
@@ -218,16 +224,18 @@ struct Builder {
       const double S1 = std::exp(2.0 * lns1);
       const double dS1 = 2.0 * S1 * std::fabs(sl1);  // |dS1/dln M1|
       const double diff = S1 - S2;
-      // q dN/dq (the integrand in ln q)
-      const double f = diff > 0.0 ? dS1 / q * std::pow(diff, -1.5) * modifier(std::sqrt(S1), s2, w) / std::sqrt(2.0 * kPi) : 0.0;
+      const double f = diff > 0.0 ? dS1 / q * std::pow(diff, -1.5) * modifier_mass(std::sqrt(S1), s2) / std::sqrt(2.0 * kPi) : 0.0;
       cdf[i] = i == 0 ? 0.0 : cdf[i - 1] + 0.5 * (prev + f) * d;
       prev = f;
     }
-    return cdf[nq - 1];
+    return cdf[kNq - 1];
   }
 
-  // Sub-resolution mass-loss rate F (per unit w).
-  double accretion_rate(double M2, double w) const {
+  // F / (w/sigma2)^gamma2:
+  //   F = (1/sqrt(2 pi)) int_{S_res}^inf (S1 - S2)^-3/2 G dS1 = (2/sqrt(2 pi)) int_0^{u_res} G du,
+  // u = (S1 - S2)^-1/2, by the midpoint rule in v with u = u_res v^(1/(1-gamma1)),
+  // which is exact for gamma1 = 0.
+  double accretion_rate(double M2) const {
     const double S2 = sig.sigma2(M2), s2 = std::sqrt(S2);
     const double Sres = sig.sigma2(mRes);
     if (!(Sres > S2)) return 0.0;
@@ -240,11 +248,54 @@ struct Builder {
       const double u = uRes * std::pow(v, p);
       const double dudv = uRes * p * std::pow(v, p - 1.0);
       const double s1 = std::sqrt(S2 + 1.0 / (u * u));
-      acc += modifier(s1, s2, w) * dudv;
+      acc += modifier_mass(s1, s2) * dudv;
     }
     return 2.0 / std::sqrt(2.0 * kPi) * acc / nv;
   }
 
+  // (w/sigma2)^gamma2, the w-dependent factor of G.
+  double modifier_w(double w, double s2) const { return std::pow(w / s2, pch.gamma2); }
+};
+
+// Rates on a grid in ln M2 (kPerDecade rows per decade from the resolution
+// up): R and F interpolated linearly in ln M2, q drawn from the nearest row.
+struct RateTable {
+  static constexpr int kPerDecade = 256;
+  double lnMin = 0.0, dlnM = 1.0, lnMRes = 0.0;
+  int rows = 0;
+  std::vector<double> R, F, lnq, cdf;  // R, F [rows]; lnq, cdf [rows][kNq] (cdf normalised to 1)
+
+  void build(const Rates& r, double massMax) {
+    lnMRes = std::log(r.mRes);
+    lnMin = lnMRes;
+    dlnM = std::log(10.0) / kPerDecade;
+    rows = std::max(2, (int)std::ceil((std::log(massMax) - lnMin) / dlnM) + 2);
+    R.resize(rows);
+    F.resize(rows);
+    lnq.resize((size_t)rows * Rates::kNq);
+    cdf.resize((size_t)rows * Rates::kNq);
+    for (int j = 0; j < rows; ++j) {
+      const double M = std::exp(lnMin + j * dlnM);
+      double* q = &lnq[(size_t)j * Rates::kNq];
+      double* c = &cdf[(size_t)j * Rates::kNq];
+      R[j] = r.split_rate(M, q, c);
+      F[j] = r.accretion_rate(M);
+      if (R[j] > 0.0)
+        for (int i = 0; i < Rates::kNq; ++i) c[i] /= R[j];
+    }
+  }
+  // Row coordinate of mass M (clamped to the grid).
+  double coord(double M) const {
+    double x = (std::log(M) - lnMin) / dlnM;
+    return std::min(std::max(x, 0.0), rows - 1.000001);
+  }
+};
+
+struct Builder {
+  const SigmaTable& sig;
+  gal_pch_params pch;
+  double mRes, wMax;
+  const RateTable& rt;
   struct Node {
     double mass, w;
     int32_t parent, childFirst, childCount;
@@ -255,8 +306,8 @@ struct Builder {
     nodes.clear();
     nodes.push_back(Node{rootMass, rootW, -1, 0, 0});
     std::vector<int32_t> stack{0};
-    std::vector<double> lnq, cdf;
     std::uniform_real_distribution<double> U(0.0, 1.0);
+    constexpr int nq = Rates::kNq;
     while (!stack.empty()) {
       const int32_t i = stack.back();
       stack.pop_back();
@@ -265,9 +316,15 @@ struct Builder {
       bool split = false;
       int guard = 0;
       while (w < wMax && m >= mRes && ++guard < 100000) {
-        const double R = split_rate(m, w, lnq, cdf);
-        const double F = accretion_rate(m, w);
-        const double S2 = sig.sigma2(m), Sh = sig.sigma2(0.5 * m);
+        const double x = rt.coord(m);
+        const int j = (int)x;
+        const double fx = x - j;
+        double lns2, sl2;
+        sig.at(m, lns2, sl2);
+        const double S2 = std::exp(2.0 * lns2), Sh = sig.sigma2(0.5 * m);
+        const double wf = std::pow(w / std::sqrt(S2), pch.gamma2);
+        const double R = m <= 2.0 * mRes ? 0.0 : wf * (rt.R[j] + fx * (rt.R[j + 1] - rt.R[j]));
+        const double F = wf * (rt.F[j] + fx * (rt.F[j + 1] - rt.F[j]));
         double dw = pch.accuracy_second * std::sqrt(2.0 * std::max(Sh - S2, 0.0));
         if (R > 0.0) dw = std::min(dw, pch.accuracy_first / R);
         if (F > 0.0) dw = std::min(dw, pch.accuracy_first / F);
@@ -281,10 +338,15 @@ struct Builder {
         mPrev = m;
         wPrev = w;
         if (R > 0.0 && U(rng) < R * dw) {
-          // Split: q from the tabulated distribution in ln q.
-          const double target = U(rng) * cdf.back();
-          const int k = (int)(std::upper_bound(cdf.begin(), cdf.end(), target) - cdf.begin());
-          const int k1 = std::min(std::max(k, 1), (int)cdf.size() - 1);
+          // Split: q from the tabulated distribution in ln q of the nearest
+          // row with a resolved split (its q range is that row's).
+          int row = fx < 0.5 ? j : j + 1;
+          if (!(rt.R[row] > 0.0)) row = j + 1;
+          const double* cdf = &rt.cdf[(size_t)row * nq];
+          const double* lnq = &rt.lnq[(size_t)row * nq];
+          const double target = U(rng);
+          const int k = (int)(std::upper_bound(cdf, cdf + nq, target) - cdf);
+          const int k1 = std::min(std::max(k, 1), nq - 1);
           const double f = (target - cdf[k1 - 1]) / std::max(cdf[k1] - cdf[k1 - 1], 1e-300);
           const double q = std::exp(lnq[k1 - 1] + f * (lnq[k1] - lnq[k1 - 1]));
           const double m1 = q * m;
@@ -367,6 +429,28 @@ double gal_pch_sigma(const gal_params* p, const gal_pch_params* pch, double mass
   return std::sqrt(s.sigma2(mass));
 }
 
+int gal_pch_branching_rates(const gal_pch_params* pch, double alpha, double sigma_parent, double mass_parent,
+                            double mass_resolution, double w, double* rate, double* accretion) {
+  if (!pch || !rate || !accretion || !(sigma_parent > 0.0) || !(mass_parent > 0.0) || !(mass_resolution > 0.0) ||
+      !(mass_resolution < mass_parent) || !(w > 0.0))
+    return GAL_ERR_ARGUMENT;
+  // sigma(M) = sigma_parent (M / mass_parent)^alpha on the builder's grid:
+  // linear interpolation of ln sigma in ln M is exact for a power law.
+  SigmaTable sig;
+  const int n = 400;
+  sig.lnMin = std::log(mass_resolution) - 8.0;
+  sig.dlnM = (std::log(mass_parent) + 8.0 - sig.lnMin) / (n - 1);
+  sig.lnSigma.resize(n);
+  sig.slope.assign(n, alpha);
+  for (int i = 0; i < n; ++i) sig.lnSigma[i] = std::log(sigma_parent) + alpha * (sig.lnMin + i * sig.dlnM - std::log(mass_parent));
+  const Rates r{sig, *pch, mass_resolution};
+  std::vector<double> lnq(Rates::kNq), cdf(Rates::kNq);
+  const double wf = r.modifier_w(w, sigma_parent);
+  *rate = wf * r.split_rate(mass_parent, lnq.data(), cdf.data());
+  *accretion = wf * r.accretion_rate(mass_parent);
+  return GAL_OK;
+}
+
 int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec, gal_forest** out) {
   if (!out) return GAL_ERR_ARGUMENT;
   *out = nullptr;
@@ -379,7 +463,9 @@ int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_f
   sig.build(c, *pch);
   GrowthTable gt;
   gt.build(c);
-  const Builder B{sig, *pch, spec->mass_resolution, gt.w_of_z(spec->redshift_max)};
+  RateTable rt;
+  rt.build(Rates{sig, *pch, spec->mass_resolution}, spec->root_mass_max);
+  const Builder B{sig, *pch, spec->mass_resolution, gt.w_of_z(spec->redshift_max), rt};
   const int64_t nTrees = spec->n_trees;
   std::vector<std::vector<Builder::Node>> trees((size_t)nTrees);
   std::vector<std::vector<double>> spins((size_t)nTrees);

@@ -49,6 +49,9 @@ def _declare(lib):
     lib.gal_redshift.restype = ctypes.c_double
     lib.gal_pch_sigma.argtypes = [pp, ctypes.POINTER(PchParams), ctypes.c_double]
     lib.gal_pch_sigma.restype = ctypes.c_double
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.gal_pch_branching_rates.argtypes = [ctypes.POINTER(PchParams)] + [ctypes.c_double] * 5 + [dp, dp]
+    lib.gal_pch_branching_rates.restype = ctypes.c_int
     lib.gal_gpu_forest_create.argtypes = [vp, ctypes.c_int64] + [vp] * 7 + [ctypes.c_int32, vp, ctypes.POINTER(vp)]
     lib.gal_gpu_forest_create.restype = ctypes.c_int
     for name in ("gal_gpu_forest_evolve", "gal_gpu_forest_sync"):
@@ -86,6 +89,26 @@ class Forest:
     def n(self):
         return len(self.parent)
 
+    @property
+    def n_trees(self):
+        return int(self.tree.max()) + 1 if self.n else 0
+
+    def subset(self, trees):
+        """The forest made of the given trees (ids of `tree`), node order
+        kept, indices remapped and the trees renumbered 0.. in increasing
+        order of their ids.  Returns (forest, [n_sub] original node index)."""
+        keep = np.isin(self.tree, np.asarray(trees))
+        idx = np.flatnonzero(keep)
+        new = np.full(self.n, -1, np.int64)
+        new[idx] = np.arange(len(idx))
+        parent = self.parent[idx]
+        parent = np.where(parent >= 0, new[np.maximum(parent, 0)], -1).astype(np.int32)
+        count = self.child_count[idx].copy()
+        first = np.where(count > 0, new[self.child_first[idx]], 0).astype(np.int32)
+        _, renum = np.unique(self.tree[idx], return_inverse=True)
+        return Forest(renum.astype(np.int32), parent, first, count, self.time[idx].copy(), self.mass[idx].copy(),
+                      self.spin[idx].copy()), idx
+
 
 def pch_params():
     lib = _declare(_abi.load_library())
@@ -109,6 +132,18 @@ def build(params, n_trees, seed=3, root_mass_min=1e10, root_mass_max=1e14, root_
     lib.gal_forest_get(handle, *[_vp(a) for a in arrays])
     lib.gal_forest_free(handle)
     return Forest(*arrays)
+
+
+def branching_rates(pch, alpha, sigma_parent, mass_parent, mass_resolution, w=1.686):
+    """(split rate, sub-resolution accretion rate) per unit w of the
+    builder, for sigma(M) = sigma_parent (M/mass_parent)^alpha."""
+    lib = _declare(_abi.load_library())
+    r, a = ctypes.c_double(), ctypes.c_double()
+    rc = lib.gal_pch_branching_rates(ctypes.byref(pch), alpha, sigma_parent, mass_parent, mass_resolution, w,
+                                     ctypes.byref(r), ctypes.byref(a))
+    if rc:
+        raise RuntimeError(f"gal_pch_branching_rates failed ({rc})")
+    return r.value, a.value
 
 
 def output_times(params, n=20, redshift_max=8.0):

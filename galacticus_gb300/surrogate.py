@@ -131,7 +131,7 @@ class CoolingSurrogate:
     y_scale: float
     tolerance: float = 0.01
     map_lo: tuple = (4.0, -4.0)
-    map_step: tuple = (0.1, 0.25)
+    map_step: tuple = (0.05, 0.125)
     use_table: np.ndarray = field(default=None)
     history: np.ndarray = field(default=None)
     rms_dex: float = float("nan")
@@ -179,6 +179,13 @@ class CoolingSurrogate:
             buf = ctypes.create_string_buffer(512)
             lib.gal_gpu_last_error(evolver.ctx, buf, 512)
             raise RuntimeError(f"gal_gpu_set_surrogate failed: {buf.value.decode()}")
+
+    def uninstall(self, evolver):
+        """Remove the surrogate from the context: the table alone again."""
+        lib = _declare(evolver.lib)
+        rc = lib.gal_gpu_set_surrogate(evolver.ctx, None)
+        if rc:
+            raise RuntimeError(f"gal_gpu_set_surrogate(NULL) failed ({rc})")
 
     def build_error_map(self, table, tolerance=None, per_cell=64, seed=7):
         """Mark the (log10 T, log10 Z) cells where the deployed network misses

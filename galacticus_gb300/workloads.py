@@ -117,6 +117,35 @@ def isolated_halos(n=65536, seed=2, cosmology=None, spin=SPIN_DEFAULT):
     return Batch(state, param, t0, t0 + dt, np.full(n, -1.0))
 
 
+def galaxy_halos(n=8192, seed=12, cosmology=None, spin=SPIN_DEFAULT):
+    """Isolated halos that already hold a galaxy: the halos, hot gas, times
+    and timesteps of isolated_halos(), plus a gaseous and stellar disk and
+    spheroid with metals, and a central black hole of 1e4-1e9 Msun.  Masses
+    (as fractions f of the halo's baryons (Omega_b/Omega_m) M):
+    disk gas and stars log-uniform f in 1e-3-0.1, spheroid gas log-uniform f
+    in 1e-4-0.1, spheroid stars log-uniform f in 1e-3-0.3, gas metallicities
+    log-uniform 1e-3-0.03 (mass fraction), stellar disk metallicity 0.01; the
+    black-hole mass log-uniform.  This batch runs every operator of the node
+    (spheroid star formation, feedback and Bondi-Hoyle accretion from the
+    spheroid gas on both sides of the Jeans-length condition) from the
+    first step."""
+    batch = isolated_halos(n=n, seed=seed, cosmology=cosmology, spin=spin)
+    cosmo = cosmology or Cosmology()
+    rng = np.random.Generator(np.random.Philox(key=seed + 1000))
+    u = rng.random((8, n))
+    baryons = cosmo.omega_baryon / cosmo.omega_matter * batch.param[_abi.P_MASS]
+    s = batch.state
+    s[_abi.Y_DISK_GAS] = baryons * 10.0 ** (-3.0 + 2.0 * u[0])
+    s[_abi.Y_DISK_GAS_METALS] = s[_abi.Y_DISK_GAS] * 10.0 ** (-3.0 + np.log10(30.0) * u[1])
+    s[_abi.Y_DISK_STARS] = baryons * 10.0 ** (-3.0 + 2.0 * u[2])
+    s[_abi.Y_DISK_STARS_METALS] = 0.01 * s[_abi.Y_DISK_STARS]
+    s[_abi.Y_SPHEROID_GAS] = baryons * 10.0 ** (-4.0 + 3.0 * u[3])
+    s[_abi.Y_SPHEROID_GAS_METALS] = s[_abi.Y_SPHEROID_GAS] * 10.0 ** (-3.0 + np.log10(30.0) * u[4])
+    s[_abi.Y_SPHEROID_STARS] = baryons * 10.0 ** (-3.0 + np.log10(300.0) * u[5])
+    s[_abi.Y_BLACK_HOLE] = 10.0 ** (4.0 + 5.0 * u[6])
+    return batch
+
+
 def isolated_params(tolerance_relative=1.0e-3):
     """P-std parameters with the batched-isolated-step tolerances."""
     p = _abi.default_params()

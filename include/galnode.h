@@ -245,8 +245,11 @@ int gal_gpu_evolve_batch_device(gal_ctx* ctx, int64_t n, double* state, const do
  * nothing is allocated, on the device or the host: the kernel's scratch (the
  * work-queue head plus the log-converted CIE tables) is one fixed 128 KiB
  * static device array in this library, held by every GPU that loads it until
- * the process exits.  Tables needing more than that (16 B per table cell +
- * 8 B per grid point + 256 B) are rejected with GAL_ERR_TOO_LARGE.  The
+ * the process exits.  Tables needing more than that are rejected with
+ * GAL_ERR_TOO_LARGE: a table takes 16 B per cell, 8 B per temperature and
+ * 16 B per metallicity, plus 2,816 B that do not depend on it (the 2 KiB
+ * short-log and 512 B exponential tables of the FP64 functions and the
+ * 256 B queue head); the reference's 24 x 261 grid takes 105,512 B.  The
  * first call on a device looks up the array's device address; make that
  * first call before any stream capture.  Every call restages the table and
  * resets the queue head in the shared array, so calls that overlap on the

@@ -82,6 +82,17 @@ double gal_cosmic_time(const gal_params* p, double z);
 double gal_redshift(const gal_params* p, double t);
 /* sigma(M) of the builder's power spectrum at z = 0 (for tests). */
 double gal_pch_sigma(const gal_params* p, const gal_pch_params* pch, double mass);
+/* The builder's branching rates, per unit of the critical overdensity w,
+ * for a branch of mass_parent at w when sigma(M) is the power law
+ * sigma_parent (M/mass_parent)^alpha: rate = the probability rate of a
+ * split into a progenitor above mass_resolution, accretion = the rate of
+ * the mass fraction lost below it.  The reference's
+ * mergerTreeBranchingProbabilityParkinsonColeHelly%probability and
+ * %fractionSubresolution (merger_trees/branching_probability/
+ * Parkinson_Cole_Helly.F90:265-634); for tests against the reference's
+ * branching-rate known answers (source/tests/merger_tree_branching.F90). */
+int gal_pch_branching_rates(const gal_pch_params* pch, double alpha, double sigma_parent, double mass_parent,
+                            double mass_resolution, double w, double* rate, double* accretion);
 
 /* -------------------------------------------------------------- evolution */
 

@@ -41,3 +41,114 @@ def parity_ratio(gpu, ref, state0, param, params, factor=10.0):
 def parity_bound(ref, state0, param, params, factor=10.0):
     """The allowed |gpu - ref| of parity_ratio: factor times the tolerance."""
     return factor * (params.ode_tolerance_relative * np.abs(ref) + params.ode_tolerance_absolute * scales(state0, param))
+
+
+# ---- per-halo final-mass criterion ----------------------------------------
+# The target of the surrogate form: final stellar (disk + spheroid stars)
+# and cold-gas (disk + spheroid gas) masses within 1e-3 relative of the FP64
+# oracle, halo by halo, over halos whose oracle mass is above 1e6 Msun.
+
+MASS_MINIMUM = 1.0e6
+MASS_BAR = 1.0e-3
+SUMS = (("stellar", (_abi.Y_DISK_STARS, _abi.Y_SPHEROID_STARS)),
+        ("cold_gas", (_abi.Y_DISK_GAS, _abi.Y_SPHEROID_GAS)))
+
+
+def mass_sums(state):
+    """{name: [n] stellar / cold-gas mass} of a [NY][n] state."""
+    return {name: state[a] + state[b] for name, (a, b) in SUMS}
+
+
+def relative_mass_errors(gpu, ref):
+    """{name: ([n] |gpu/ref - 1|, [n] mask ref > 1e6 Msun)}."""
+    g, r = mass_sums(gpu), mass_sums(ref)
+    out = {}
+    for name in g:
+        big = r[name] > MASS_MINIMUM
+        rel = np.zeros_like(r[name])
+        rel[big] = np.abs(g[name][big] / r[name][big] - 1.0)
+        out[name] = (rel, big)
+    return out
+
+
+def mass_movement(ref, moved):
+    """[n] largest relative change of the stellar or cold-gas mass between
+    the oracle's answer and each of the `moved` answers (halos below 1e6 Msun
+    count as not moving)."""
+    r = mass_sums(ref)
+    worst = np.zeros(ref.shape[1])
+    for m in moved:
+        s = mass_sums(m)
+        for name in r:
+            big = r[name] > MASS_MINIMUM
+            d = np.zeros_like(worst)
+            d[big] = np.abs(s[name][big] / r[name][big] - 1.0)
+            worst = np.maximum(worst, d)
+    return worst
+
+
+def perturbed_table(table, dex):
+    """The CIE table with every cooling rate multiplied by 10^dex."""
+    from galacticus_gb300.cie_tables import CieTable
+    return CieTable(table.temperature, table.metallicity, table.cooling_rate * 10.0 ** dex, table.electron_density)
+
+
+def conditioning(oracle_mod, params, table, batch, ref, lambda_dex=1.0e-4, threads=0):
+    """How well the oracle's own stellar and cold-gas masses are determined,
+    per halo: the largest relative change under (a) the relative tolerance
+    x0.9 and x1.1 (the integration) and (b) the cooling function scaled by
+    10^(+-lambda_dex) (Lambda known to 1e-4 dex, a tenth of the tightest
+    error gate).  Returns ([n] movement, [NY][n] worst absolute change of
+    every property under (a) and (b))."""
+    from galacticus_gb300 import workloads
+    moved = []
+    for factor in (0.9, 1.1):
+        q = workloads.isolated_params(tolerance_relative=params.ode_tolerance_relative * factor)
+        moved.append(oracle_mod.evolve_batch(q, table, batch.state, batch.param, batch.t_start, batch.t_end,
+                                             batch.step, threads=threads)[0])
+    for dex in (lambda_dex, -lambda_dex):
+        moved.append(oracle_mod.evolve_batch(params, perturbed_table(table, dex), batch.state, batch.param,
+                                             batch.t_start, batch.t_end, batch.step, threads=threads)[0])
+    sensitivity = np.max([np.abs(m - ref) for m in moved], axis=0)
+    return mass_movement(ref, moved), sensitivity
+
+
+def bar_shares(gpu, ref, movement):
+    """Per-halo shares within the 1e-3 bar: over all halos above 1e6 Msun
+    ("all"), and over those whose oracle masses move by less than the bar
+    under conditioning() ("conditioned").  {name: {...}} plus the worst
+    errors."""
+    errs = relative_mass_errors(gpu, ref)
+    good = movement <= MASS_BAR
+    out = {}
+    for name, (rel, big) in errs.items():
+        out[name] = {"all": float(np.mean(rel[big] <= MASS_BAR)),
+                     "conditioned": float(np.mean(rel[big & good] <= MASS_BAR)),
+                     "p99": float(np.percentile(rel[big], 99)), "max": float(rel[big].max()),
+                     "max_conditioned": float(rel[big & good].max())}
+    out["ill_conditioned"] = float(np.mean(~good))
+    out["min_conditioned"] = min(out[n]["conditioned"] for n, _ in SUMS)
+    out["min_all"] = min(out[n]["all"] for n, _ in SUMS)
+    return out
+
+
+def select_gate(run, ref, movement, gates, share=0.995):
+    """Pick the loosest error-map gate of the cooling surrogate whose final
+    stellar and cold-gas masses meet the 1e-3 bar halo by halo: at least
+    `share` of the well-conditioned halos above 1e6 Msun within 1e-3 of the
+    oracle, for both masses.  `gates` run from loose to tight; a gate of
+    None is the table alone (the network never used).  run(gate) returns
+    (final state, network share of the cooling evaluations).  Every gate is
+    run (the records show the trade-off).  Returns (chosen gate, {gate:
+    record}); None when only the table meets the bar."""
+    results = {}
+    chosen = None
+    for gate in gates:
+        state, net_share = run(gate)
+        rec = bar_shares(state, ref, movement)
+        rec["network_share"] = net_share
+        rec["meets_bar"] = rec["min_conditioned"] >= share
+        results[gate] = rec
+        if rec["meets_bar"] and chosen is None:
+            chosen = gate
+    return chosen, results

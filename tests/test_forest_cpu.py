@@ -30,6 +30,39 @@ def test_sigma_normalisation(params):
     assert lib.gal_pch_sigma(ctypes.byref(params), ctypes.byref(pch), 1e10) > s
 
 
+@pytest.mark.parametrize("w", [1.686, 4.0])
+def test_branching_rates_match_reference_known_answers(w):
+    """The builder's branching rates against the reference's known answers
+    (source/tests/merger_tree_branching.F90:76-78, 185-191, 224-234,
+    390-399): for sigma(M) proportional to M^(-1/3) (an n = -1 power
+    spectrum with a sharp k-space filter) and the unmodified rates (G0 = 1,
+    gamma1 = gamma2 = 0), a 1e12 Msun branch with resolution 1e11 Msun
+    splits at 2.498324530964044/sigma and loses mass below the resolution
+    at 0.4181139013841312/sigma per unit of the critical overdensity, at
+    any w; tolerances as the reference's (1e-4 and 2e-3)."""
+    pch = forest.pch_params()
+    pch.g0, pch.gamma1, pch.gamma2 = 1.0, 0.0, 0.0
+    for sigma in (0.7, 2.3):
+        rate, accretion = forest.branching_rates(pch, -1.0 / 3.0, sigma, 1e12, 1e11, w=w)
+        assert rate == pytest.approx(2.498324530964044 / sigma, rel=1e-4)
+        assert accretion == pytest.approx(0.4181139013841312 / sigma, rel=2e-3)
+
+
+def test_branching_rates_modifier():
+    """With the PCH modifier G0 (sigma1/sigma2)^gamma1 (w/sigma2)^gamma2
+    (Parkinson_Cole_Helly.F90:265-634), the w dependence is the factor
+    (w/sigma2)^gamma2, and G0 scales both rates."""
+    pch = forest.pch_params()
+    pch.g0, pch.gamma1, pch.gamma2 = 0.57, 0.38, -0.01
+    r1, a1 = forest.branching_rates(pch, -0.25, 1.5, 1e12, 1e10, w=1.0)
+    r2, a2 = forest.branching_rates(pch, -0.25, 1.5, 1e12, 1e10, w=3.0)
+    assert r2 / r1 == pytest.approx(3.0 ** -0.01, rel=1e-12)
+    assert a2 / a1 == pytest.approx(3.0 ** -0.01, rel=1e-12)
+    pch.g0 = 1.14
+    r3, a3 = forest.branching_rates(pch, -0.25, 1.5, 1e12, 1e10, w=1.0)
+    assert r3 / r1 == pytest.approx(2.0, rel=1e-12) and a3 / a1 == pytest.approx(2.0, rel=1e-12)
+
+
 def test_tree_invariants(small_forest, params):
     f = small_forest
     roots = np.flatnonzero(f.parent < 0)

@@ -50,29 +50,37 @@ def test_error_map_bounds_the_deployed_error(trained, table):
 
 
 @pytest.mark.parametrize("rates", ["fp64", "fp32"])
-def test_evolution_with_surrogate(trained, table, oracle_mod, rates):
-    """The surrogate forms against the FP64 oracle on the isolated-halo step,
-    and what the network gains: the share of cooling evaluations it serves
-    and its error against the untrained network it started from."""
+def test_evolution_with_surrogate_against_the_table(trained, table, oracle_mod, rates):
+    """The surrogate forms at the configuration's gate (0.01 dex) against
+    the same rates with the table (the method without the network), both
+    against the FP64 oracle on the isolated-halo step: the network takes
+    most cooling evaluations off the table, and the price is accuracy --
+    per halo, the table form keeps more halos' stellar and cold-gas masses
+    within 1e-3 of the oracle than the surrogate form does (the per-halo
+    bar itself is held in test_surrogate_bar.py)."""
     from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
+    from oracle import compare
     params = workloads.isolated_params()
     batch = workloads.isolated_halos(n=8192, seed=2)
-    ev = MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision=rates)
-    trained.install(ev)
-    g = batch.copy()
-    status = ev.evolve(g.state, g.param, g.t_start, g.t_end, g.step, return_status=True)
-    network, tab = surrogate.stats(ev)
-    ev.close()
-    assert np.all(status == 0)
-    assert network > 0.5 * (network + tab), f"network served {network} of {network + tab}"
     ref, _, ref_status, _ = oracle_mod.evolve_batch(params, table, batch.state, batch.param, batch.t_start, batch.t_end,
                                                     batch.step)
-    for idx in (_abi.Y_DISK_STARS, _abi.Y_DISK_GAS):
-        big = ref[idx] > 1e6
-        rel = np.abs(g.state[idx][big] / ref[idx][big] - 1.0)
-        assert np.median(rel) < 1e-3, f"median rel error {np.median(rel):.2e}"
-    # The gain of training: the untrained network misses the table by far more.
-    untrained = surrogate.CoolingSurrogate(surrogate.init_params(4), trained.in_mean, trained.in_scale, trained.y_mean,
-                                           trained.y_scale)
-    x, y = surrogate.cooling_samples(table, 20000, seed=23)
-    assert np.abs(untrained.predict(x) - y).mean() > 50 * np.abs(trained.predict(x) - y).mean()
+    out = {}
+    for name in ("table", "network"):
+        ev = MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision=rates)
+        if name == "network":
+            trained.build_error_map(table, tolerance=0.01)
+            trained.install(ev)
+        g = batch.copy()
+        status = ev.evolve(g.state, g.param, g.t_start, g.t_end, g.step, return_status=True)
+        if name == "network":
+            network, tab = surrogate.stats(ev)
+        ev.close()
+        assert np.all(status == 0)
+        out[name] = compare.bar_shares(g.state, ref, np.zeros(batch.n))
+    assert network > 0.5 * (network + tab), f"network served {network} of {network + tab}"
+    assert out["table"]["min_all"] >= 0.995
+    assert out["network"]["min_all"] < out["table"]["min_all"]
+    # Still a close approximation: the median halo within 1e-3.
+    errs = compare.relative_mass_errors(g.state, ref)
+    for name, (rel, big) in errs.items():
+        assert np.median(rel[big]) < 1e-3, f"{name}: median rel error {np.median(rel[big]):.2e}"
