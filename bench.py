@@ -17,9 +17,11 @@ their final-mass errors.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-N > 1 runs one process per GPU under torch.distributed.run; every rank
-evolves its own batch (independent halos, no collective on the data path;
-weak scaling) and rank 0 prints the JSON line with the max-over-ranks time.
+N > 1 runs one process per GPU under torch.distributed.run with no
+collective on the data path (weak scaling): every rank evolves its own batch
+of independent halos, and the uneven-trees forest (4,096 trees per rank) is
+one forest split over the ranks by longest processing time first on node
+counts; rank 0 prints the JSON line with the max-over-ranks time.
 
 `--impl reference` times the reference algorithm on the host CPU.  The
 Fortran reference cannot be built in this environment (no gfortran, GSL,
@@ -170,6 +172,18 @@ def reduce_over_ranks(dist, device, elapsed, work=None):
     return float(t.item()), work
 
 
+def gather_ranks(dist, device, values):
+    """Every rank's list of numbers, in rank order (rank 0 reports them);
+    [values] without a process group."""
+    if not dist:
+        return [list(values)]
+    import torch
+    mine = torch.tensor([float(v) for v in values], device=device, dtype=torch.float64)
+    every = [torch.zeros_like(mine) for _ in range(dist.get_world_size())]
+    dist.all_gather(every, mine)
+    return [e.tolist() for e in every]
+
+
 def cpu_baseline(params, table, batch, seconds=10.0):
     """The oracle on every host core over repeats of the full batch; returns
     the baseline record and the final state of the first pass."""
@@ -295,13 +309,18 @@ def run_trees(args, params, table, net, gate, rank, dist, device):
     import torch
     from galacticus_gb300 import forest, surrogate
     from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
+    world = dist.get_world_size() if dist else 1
     t0 = time.perf_counter()
-    f = forest.build(params, n_trees=args.trees, seed=3 + rank)
+    # One forest of `trees` per rank (seed 3), split over the ranks by
+    # longest processing time first on node counts (weak scaling).
+    f_all = forest.build(params, n_trees=args.trees * world, seed=3)
+    f, _ = forest.partition(f_all, rank, world)
     build_s = time.perf_counter() - t0
     state0 = forest.initial_state(params, f)
     times = forest.output_times(params)
-    out = {"workload": TREES_WORKLOAD.format(args.trees), "nodes": f.n, "leaves": int((f.child_count == 0).sum()),
+    out = {"workload": TREES_WORKLOAD.format(args.trees * world), "nodes": f.n, "leaves": int((f.child_count == 0).sum()),
            "max_tree_nodes": int(np.bincount(f.tree).max()), "build_s": build_s,
+           "split": f"{world} rank(s), trees assigned longest processing time first by node count",
            "graph": "one CUDA graph per evolution: counter reset, leaf-queue reset, one persistent kernel",
            "timing": "host clock around the graph launch and its completion event, after 1 warm-up evolution", "forms": {}}
     results = {}
@@ -330,10 +349,14 @@ def run_trees(args, params, table, net, gate, rank, dist, device):
         fe.sync()
         dt = (time.perf_counter() - tb) / reps
         acc = fe.accepted_steps()
+        per_rank = gather_ranks(dist, device, [dt, acc, f.n])
         dt, accepted_all = reduce_over_ranks(dist, device, dt, acc)
         state, status = fe.results(snapshots=False)[:2]
         entry = {"value": accepted_all / dt, "s_per_evolution": dt, "accepted_steps": acc, "launch": list(ev.get_launch()),
                  "failed_nodes": int((status != 0).sum())}
+        if world > 1:
+            entry["per_rank"] = [{"s_per_evolution": r[0], "accepted_steps": int(r[1]), "nodes": int(r[2])}
+                                 for r in per_rank]
         if name == "surrogate":
             s1 = surrogate.stats(ev) if gate is not None else (0, 0)
             entry["network_share"] = (s1[0] - s0[0]) / max(1, (s1[0] - s0[0]) + (s1[1] - s0[1]))
@@ -588,7 +611,7 @@ def run_ours(args):
         if name == "surrogate":
             net.build_error_map(table, tolerance=args.gate)
             net.install(ev)
-        f = forest_mod.build(params, n_trees=args.trees, seed=3 + rank)
+        f, _ = forest_mod.partition(forest_mod.build(params, n_trees=args.trees * world, seed=3), rank, world)
         fe = forest_mod.ForestEvolver(ev, f, forest_mod.initial_state(params, f), forest_mod.output_times(params))
         for _ in range(args.warmup):
             fe.evolve()

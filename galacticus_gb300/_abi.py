@@ -30,6 +30,10 @@ STATUS_SUCCESS = 0
 STATUS_UNDERFLOW = 15
 STATUS_XCPU = 1025
 STATUS_NOT_FINITE = 2001
+STATUS_INTERRUPTED = 9
+
+COMPONENT_DISK, COMPONENT_SPHEROID, COMPONENT_BLACK_HOLE, COMPONENT_ALL = 1, 2, 4, 7
+INTERRUPT_CREATE_DISK, INTERRUPT_CREATE_SPHEROID, INTERRUPT_CREATE_BLACK_HOLE = 1, 2, 4
 RATES_FP64 = 0
 RATES_FP32 = 1
 
@@ -89,6 +93,7 @@ class Params(ctypes.Structure):
         ("bh_hot_mode_only", ctypes.c_int32), ("pad", ctypes.c_int32),
         ("bh_efficiency_radiative", ctypes.c_double),
         ("bh_efficiency_jet", ctypes.c_double),
+        ("timestep_relative", ctypes.c_double), ("timestep_absolute", ctypes.c_double),
     ]
 
 
@@ -133,6 +138,7 @@ def default_params():
     p.bh_hot_mode_only = 1
     p.bh_efficiency_radiative = 1.0 - (8.0 / 9.0) ** 0.5
     p.bh_efficiency_jet = 0.0
+    p.timestep_relative, p.timestep_absolute = 0.1, 1.0
     return p
 
 
@@ -168,6 +174,10 @@ def load_library(path=LIB_PATH):
     lib.gal_gpu_evolve_batch.restype = ctypes.c_int
     lib.gal_gpu_evolve_batch_device.argtypes = [vp, ctypes.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]
     lib.gal_gpu_evolve_batch_device.restype = ctypes.c_int
+    lib.gal_gpu_evolve_batch_interrupt.argtypes = [vp, ctypes.c_int64, dp, dp, dp, dp, dp, ip, ip, up, dp, ip]
+    lib.gal_gpu_evolve_batch_interrupt.restype = ctypes.c_int
+    lib.gal_gpu_evolve_batch_interrupt_device.argtypes = [vp, ctypes.c_int64] + [vp] * 11
+    lib.gal_gpu_evolve_batch_interrupt_device.restype = ctypes.c_int
     lib.gal_gpu_set_launch.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
     lib.gal_gpu_set_launch.restype = ctypes.c_int
     lib.gal_gpu_get_launch.argtypes = [vp, ip, ip]

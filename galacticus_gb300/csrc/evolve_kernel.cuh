@@ -46,6 +46,8 @@ constexpr double c1 = 37.0 / 378.0, c3 = 250.0 / 621.0, c4 = 125.0 / 594.0, c6 =
 constexpr double e1 = 37.0 / 378.0 - 2825.0 / 27648.0, e3 = 250.0 / 621.0 - 18575.0 / 48384.0,
                  e4 = 125.0 / 594.0 - 13525.0 / 55296.0, e5 = -277.0 / 14336.0, e6 = 512.0 / 1771.0 - 0.25;
 constexpr double order = 5.0;  // order GSL's rkck reports to the step controller
+// Stage abscissae (used only by the interrupt form, where evaluation times matter).
+constexpr double a2 = 1.0 / 5.0, a3 = 3.0 / 10.0, a4 = 3.0 / 5.0, a5 = 1.0, a6 = 7.0 / 8.0;
 }  // namespace ck
 
 enum EvolveMode : int { MODE_PLAIN = 0, MODE_SURROGATE = 1, MODE_FAST = 2, MODE_FAST_SURROGATE = 3 };
@@ -62,6 +64,11 @@ struct Batch {
   int32_t* status;
   uint32_t* counters;
   unsigned long long* queue;  // work-queue head (device scratch, zeroed before launch)
+  // Interrupt form only (gal_gpu_evolve_batch_interrupt): the GAL_COMPONENT_*
+  // mask of each node, and the time reached and interrupt task.
+  const int32_t* components;
+  double* tReached;
+  int32_t* task;
 };
 
 // Device tables: the FP64 forms read gTab/gLnT/gLnZ/gFastLog/gFastExp, the
@@ -243,10 +250,11 @@ __device__ __forceinline__ CoolingValuesF surrogate_cooling(const Globals& G, co
   return cv;
 }
 
-template <int THREADS, int MODE, bool FOREST>
+template <int THREADS, int MODE, bool FOREST, bool INTR = false>
 __global__ void __launch_bounds__(THREADS, 1)
 evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant__ DeviceTables T,
               const __grid_constant__ SurrogateDev sd, const __grid_constant__ ForestDev F) {
+  static_assert(!INTR || (MODE == MODE_PLAIN && !FOREST), "interrupts: batches in the plain form only");
   constexpr bool SURR = (MODE & MODE_SURROGATE) != 0;
   constexpr bool FAST = (MODE & MODE_FAST) != 0;
   using RateT = typename std::conditional<FAST, float, double>::type;
@@ -534,6 +542,10 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       if (b.counters) {
         b.counters[node] = 0; b.counters[n + node] = 0; b.counters[2 * n + node] = 0;
       }
+      if constexpr (INTR) {
+        b.tReached[node] = t1;
+        b.task[node] = 0;
+      }
       phase = PH_NEED;
     }
   };
@@ -572,7 +584,206 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
     }
   };
 
-  if constexpr (MODE == MODE_PLAIN) {
+  if constexpr (INTR) {
+    // The plain form with interrupts (the reference's standardODEs,
+    // node_evolver/standard.F90:895-945, with odeSolver%solve's
+    // re-targeting, numerical/ODE_solver/solver.F90:608-620): an evaluation
+    // that gives a rate to a component the node does not have returns zero
+    // derivatives and, when it is the earliest so far, records its time and
+    // task and abandons the attempt (GSL_EBADFUNC: the state stays at the
+    // step's start); the integration then ends at that time, every
+    // evaluation at or after it returning zero derivatives.  As GSL's rkck,
+    // each attempt evaluates f(t+h, y_new), which can interrupt too and is
+    // the next step's slope on acceptance.  The interrupt persists over the
+    // trials of the call; a restarted trial integrates to the interrupt time.
+    double kOut[GAL_NY];
+    double tInt = 0.0, target = 0.0;
+    bool found = false;
+    int32_t task = 0;
+    uint32_t comps = 0;
+    // One evaluation at time ts; true when it sets the earliest interrupt.
+    auto evalI = [&](const double* xx, double* d, double ts) -> bool {
+      if (found && ts >= tInt) {
+#pragma unroll
+        for (int i = 0; i < GAL_NY; ++i) d[i] = 0.0;
+        return false;
+      }
+      rhs(G, S, c, xx, d);
+      ++nRhs;
+      const int32_t req = interrupt_request(comps, d);
+      if (req) {
+#pragma unroll
+        for (int i = 0; i < GAL_NY; ++i) d[i] = 0.0;
+        if (!found || ts < tInt) {
+          found = true;
+          tInt = ts;
+          task = req;
+          return true;
+        }
+      }
+      return false;
+    };
+    for (;;) {
+      // ---- refill lanes whose node has finished (warp-aggregated queue pop)
+      const unsigned need = __ballot_sync(FULL, phase == PH_NEED);
+      if (need) {
+        const int leader = __ffs(need) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(queueHead, (unsigned long long)__popc(need));
+        base = __shfl_sync(FULL, base, leader);
+        if (phase == PH_NEED) {
+          take(base + __popc(need & ((1u << lane) - 1u)));
+          if (phase != PH_DONE) {
+            found = false;
+            task = 0;
+            comps = (uint32_t)b.components[node];
+          }
+        }
+      }
+      if (__all_sync(FULL, phase == PH_DONE)) break;
+
+      if (phase == PH_TRIAL && t0 == t1) zero_interval();
+      bool finished = false;
+      int finalStatus = GAL_STATUS_SUCCESS;
+      if (phase == PH_TRIAL) {
+        // odeSolverSolve from t0 toward the end (or the interrupt found by
+        // an earlier trial); the slope at the start is evaluated first.
+        target = found ? fmin(tInt, t1) : t1;
+        const double stepSize = G.p.reuse_step_size ? stepIn / (double)(1u << trial) : -1.0;
+        h = target - t0;
+        if (stepSize > 0.0) h = fmin(stepSize, h);
+        if (trial > 0) restore_start();
+        t = t0;
+        count = 0;
+        phase = PH_STEP;
+        if (target - t > 0.0 && evalI(y, k1, t)) target = tInt;
+        if (!(target - t > 0.0)) finished = true;
+      }
+      if (phase == PH_STEP && !finished) {
+        // ---- one attempted step (rkck with dydt_out, inside evolve_apply)
+        const double dt = target - t;
+        const bool finalStep = (dt >= 0.0 && h > dt) || (dt < 0.0 && h < dt);
+        const double hh = finalStep ? dt : h;
+        bool abandon;
+#pragma unroll
+        for (int i = 0; i < GAL_NY; ++i) x[i] = y[i] + ck::b21 * hh * k1[i];
+        abandon = evalI(x, k2, t + ck::a2 * hh);
+        if (!abandon) {
+#pragma unroll
+          for (int i = 0; i < GAL_NY; ++i) x[i] = y[i] + hh * (ck::b31 * k1[i] + ck::b32 * k2[i]);
+          abandon = evalI(x, k3, t + ck::a3 * hh);
+        }
+        if (!abandon) {
+#pragma unroll
+          for (int i = 0; i < GAL_NY; ++i) x[i] = y[i] + hh * (ck::b41 * k1[i] + ck::b42 * k2[i] + ck::b43 * k3[i]);
+          abandon = evalI(x, k4, t + ck::a4 * hh);
+        }
+        if (!abandon) {
+#pragma unroll
+          for (int i = 0; i < GAL_NY; ++i)
+            x[i] = y[i] + hh * (ck::b51 * k1[i] + ck::b52 * k2[i] + ck::b53 * k3[i] + ck::b54 * k4[i]);
+          abandon = evalI(x, k5, t + ck::a5 * hh);
+        }
+        if (!abandon) {
+#pragma unroll
+          for (int i = 0; i < GAL_NY; ++i)
+            x[i] = y[i] + hh * (ck::b61 * k1[i] + ck::b62 * k2[i] + ck::b63 * k3[i] + ck::b64 * k4[i] + ck::b65 * k5[i]);
+          abandon = evalI(x, k6, t + ck::a6 * hh);
+        }
+        if (!abandon) {
+#pragma unroll
+          for (int i = 0; i < GAL_NY; ++i) x[i] = y[i] + hh * (ck::c1 * k1[i] + ck::c3 * k3[i] + ck::c4 * k4[i] + ck::c6 * k6[i]);
+          abandon = evalI(x, kOut, t + hh);
+        }
+        if (abandon) {
+          // The attempt is abandoned: the integration now ends at the interrupt.
+          target = tInt;
+          if (!(target - t > 0.0)) finished = true;
+        } else {
+          double errMax = 0.0, dMax = 1.0;
+#pragma unroll
+          for (int i = 0; i < GAL_NY; ++i) {
+            const double err = fabs(hh * (ck::e1 * k1[i] + ck::e3 * k3[i] + ck::e4 * k4[i] + ck::e5 * k5[i] + ck::e6 * k6[i]));
+            const double D0 = fabs(epsRel * fabs(x[i]) + epsAbs * s[i]);
+            if (err * dMax > errMax * D0 || !(err == err)) {
+              errMax = err;
+              dMax = D0;
+            }
+          }
+          const double rmax = dmax(fast_div(errMax, dMax), 2.2250738585072014e-308);
+          ++count;
+          const double tNew = finalStep ? target : t + hh;
+          double hNew = hh;
+          bool decrease = false;
+          if (rmax > 1.1) {
+            double r = rmax > 1845.28125 ? 0.2 : 0.9 * inv_root<5>(rmax);
+            if (r < 0.2) r = 0.2;
+            hNew = r * hh;
+            decrease = true;
+          } else if (rmax < 0.5) {
+            double r = rmax < 3.8394e-5 ? 4.9 : 0.9 * inv_root<6>(rmax);
+            if (r > 4.9) r = 4.9;
+            if (r < 1.0) r = 1.0;
+            hNew = r * hh;
+          }
+          if (decrease) {
+            const double tNext = tNew + hNew;
+            if (fabs(hNew) < fabs(hh) && tNext != tNew) {
+              h = hNew;
+              ++nRej;
+              if (budget && count >= budget) { finished = true; finalStatus = GAL_STATUS_XCPU; }
+            } else {
+              ++trial;
+              if (trial >= G.p.trial_count_maximum) { finished = true; finalStatus = GAL_STATUS_UNDERFLOW; }
+              else phase = PH_TRIAL;
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < GAL_NY; ++i) {
+              y[i] = x[i];
+              k1[i] = kOut[i];
+            }
+            t = tNew;
+            h = hNew;
+            ++nAcc;
+            post_step(y);
+            if (!(target - t > 0.0 || target - t < 0.0)) {
+              finished = true;
+              bool finite = true;
+#pragma unroll
+              for (int i = 0; i < GAL_NY; ++i) finite = finite && isfinite(y[i]);
+              finalStatus = finite ? GAL_STATUS_SUCCESS : GAL_STATUS_NOT_FINITE;
+            } else if (budget && count >= budget) {
+              finished = true;
+              finalStatus = GAL_STATUS_XCPU;
+            }
+          }
+        }
+      }
+      if (finished) {
+        // evolve's results: an interrupted node reports the interrupt time
+        // and task and node%timeStep = -1 (standard.F90:729-737).
+        if (finalStatus == GAL_STATUS_SUCCESS) {
+#pragma unroll
+          for (int v = 0; v < GAL_NY; ++v) b.state[v * n + node] = y[v];
+          b.step[node] = found ? -1.0 : h;
+          b.tReached[node] = found ? tInt : t1;
+          b.task[node] = found ? task : 0;
+          b.status[node] = found ? GAL_STATUS_INTERRUPTED : GAL_STATUS_SUCCESS;
+        } else {
+          b.tReached[node] = t1;
+          b.task[node] = 0;
+          b.status[node] = finalStatus;
+        }
+        if (b.counters) {
+          b.counters[node] = nAcc;
+          b.counters[n + node] = nRej;
+          b.counters[2 * n + node] = nRhs;
+        }
+        phase = PH_NEED;
+      }
+    }
+  } else if constexpr (MODE == MODE_PLAIN) {
     // The FP64 parity form: every right-hand side inlined at its stage, the
     // stage arguments computed by the whole warp at once.
     for (;;) {
@@ -996,12 +1207,13 @@ struct LaunchArgs {
   cudaStream_t stream;
 };
 
-template <int THREADS, int MODE, bool FOREST = false>
+template <int THREADS, int MODE, bool FOREST = false, bool INTR = false>
 cudaError_t launch_evolve(const LaunchArgs& a) {
-  cudaError_t e =
-      cudaFuncSetAttribute(evolve_kernel<THREADS, MODE, FOREST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a.shm);
+  cudaError_t e = cudaFuncSetAttribute(evolve_kernel<THREADS, MODE, FOREST, INTR>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a.shm);
   if (e != cudaSuccess) return e;
-  evolve_kernel<THREADS, MODE, FOREST><<<(unsigned)a.blocks, THREADS, a.shm, a.stream>>>(a.G, a.b, a.tables, a.sd, a.forest);
+  evolve_kernel<THREADS, MODE, FOREST, INTR><<<(unsigned)a.blocks, THREADS, a.shm, a.stream>>>(a.G, a.b, a.tables, a.sd,
+                                                                                               a.forest);
   return cudaGetLastError();
 }
 
@@ -1009,6 +1221,8 @@ cudaError_t launch_evolve(const LaunchArgs& a) {
 // evolve_fast_surrogate.cu); cudaErrorInvalidConfiguration for a block size
 // the form is not built for.
 cudaError_t evolve_launch_plain(int threads, const LaunchArgs& a);
+// The plain form with interrupts (128 threads per block).
+cudaError_t evolve_launch_plain_interrupt(const LaunchArgs& a);
 cudaError_t evolve_launch_surrogate(int threads, const LaunchArgs& a);
 cudaError_t evolve_launch_fast(int threads, const LaunchArgs& a);
 cudaError_t evolve_launch_fast_surrogate(int threads, const LaunchArgs& a);

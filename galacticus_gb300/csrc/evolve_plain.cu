@@ -14,4 +14,6 @@ cudaError_t evolve_launch_plain(int threads, const LaunchArgs& a) {
   }
 }
 
+cudaError_t evolve_launch_plain_interrupt(const LaunchArgs& a) { return launch_evolve<128, MODE_PLAIN, false, true>(a); }
+
 }  // namespace gal

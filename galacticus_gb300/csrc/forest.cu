@@ -42,6 +42,16 @@ struct HostCosmology {
     const double x = std::sinh(1.5 * hubbleGyr * std::sqrt(ol) * t);
     return 1.0 / std::pow(x / std::sqrt(ol / om), 2.0 / 3.0) - 1.0;
   }
+  // The longest evolve call from time t: min(relative / H(t), absolute)
+  // (mergerTreeEvolveTimestepSimple, timesteps/simple.F90:124-161), H the
+  // expansion rate of cosmologyFunctionsMatterLambda in 1/Gyr.
+  double step_limit(double t, double relative, double absolute) const {
+    if (!(relative > 0.0)) return absolute;
+    const double hubbleGyr = h0 / (kMpc / 1.0e3 / kGyr);
+    const double zp = 1.0 + redshift(t);
+    const double rate = hubbleGyr * std::sqrt(om * zp * zp * zp + ol);
+    return std::min(relative / rate, absolute);
+  }
   void virial(double M, double z, double& r, double& v) const {
     const double zp = (1.0 + z) * (1.0 + z) * (1.0 + z);
     const double omz = om * zp / (om * zp + ol);
@@ -234,8 +244,11 @@ int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const 
     int32_t k = 0;
     while (k < nOut && !(tOut[k] > t0)) ++k;
     while (a < t1) {
-      const bool atOutput = k < nOut && tOut[k] < t1;
-      const double b = atOutput ? tOut[k] : t1;
+      // The call ends at the first of: the next output time, the parent's
+      // time and the timestep limit.
+      const double limit = a + cos.step_limit(a, p.timestep_relative, p.timestep_absolute);
+      const bool atOutput = k < nOut && tOut[k] < t1 && !(limit < tOut[k]);
+      const double b = atOutput ? tOut[k] : std::min(limit, t1);
       const double M = mass[i] + (massEnd - mass[i]) * (a - t0) / (t1 - t0);
       double r, v;
       cos.virial(M, cos.redshift(a), r, v);

@@ -215,6 +215,8 @@ void gal_params_default(gal_params* p) {
   p->bh_hot_mode_only = 1;
   p->bh_efficiency_radiative = 1.0 - std::sqrt(8.0 / 9.0);
   p->bh_efficiency_jet = 0.0;
+  p->timestep_relative = 0.1;
+  p->timestep_absolute = 1.0;
 }
 
 int gal_gpu_last_error(const gal_ctx* ctx, char* buf, int len) {
@@ -233,6 +235,8 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
     return fail(nullptr, GAL_ERR_ARGUMENT, "at least one of absolute and relative tolerance must be greater than zero%s");
   if (p->trial_count_maximum < 1 || p->trial_count_maximum > 30)
     return fail(nullptr, GAL_ERR_ARGUMENT, "trial_count_maximum must be in 1..30%s");
+  if (!(p->timestep_absolute > 0.0) || !(p->timestep_relative == p->timestep_relative))
+    return fail(nullptr, GAL_ERR_ARGUMENT, "timestep_absolute must be positive%s");
   const int nT = t->n_temperature, nZ = t->n_metallicity;
   if (nT < 2 || nZ < 2 || !t->temperature || !t->metallicity || !t->cooling_rate || !t->electron_density)
     return fail(nullptr, GAL_ERR_TABLE, "CIE table: at least 2x2 entries and all arrays are required%s");
@@ -430,6 +434,89 @@ int gal_gpu_evolve_batch(gal_ctx* ctx, int64_t n, double* state, const double* p
   CUDA_TRY(ctx, cudaMemcpyAsync(state, dState, (size_t)n * GAL_NY * sizeof(double), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(ctx, cudaMemcpyAsync(step, dStep, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(ctx, cudaMemcpyAsync(status, dStatus, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  if (counters)
+    CUDA_TRY(ctx, cudaMemcpyAsync(counters, dCounters, (size_t)n * 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  return GAL_OK;
+}
+
+int gal_gpu_evolve_batch_interrupt_device(gal_ctx* ctx, int64_t n, double* state, const double* param,
+                                          const double* tStart, const double* tEnd, double* step,
+                                          const int32_t* components, int32_t* status, uint32_t* counters,
+                                          double* tReached, int32_t* task, void* stream) {
+  if (!ctx) return fail(nullptr, GAL_ERR_ARGUMENT, "NULL context%s");
+  if (n < 0) return fail(ctx, GAL_ERR_ARGUMENT, "negative node count%s");
+  if (n == 0) return GAL_OK;
+  if (!state || !param || !tStart || !tEnd || !step || !components || !status || !tReached || !task)
+    return fail(ctx, GAL_ERR_ARGUMENT, "NULL array%s");
+  if ((unsigned long long)n * GAL_NY > (1ull << 62)) return fail(ctx, GAL_ERR_TOO_LARGE, "batch too large%s");
+  if (ctx_mode(ctx) != MODE_PLAIN)
+    return fail(ctx, GAL_ERR_ARGUMENT, "interrupts are available in the FP64-rate form without a surrogate%s");
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  CUDA_TRY(ctx, cudaMemsetAsync(ctx->dQueue, 0, sizeof(unsigned long long), st));
+  int threads, blocksPerSm;
+  effective_shape(ctx, MODE_PLAIN, threads, blocksPerSm);
+  LaunchArgs a{};
+  a.G = ctx->globals;
+  a.b = Batch{n, state, param, tStart, tEnd, step, status, counters, ctx->dQueue, components, tReached, task};
+  a.tables = DeviceTables{ctx->dTab, ctx->dLnT, ctx->dLnZ, ctx->dFastLog, ctx->dFastExp, ctx->dTabF, ctx->dLnZF};
+  a.shm = ctx_shared_bytes(ctx, MODE_PLAIN);
+  const int64_t warps = (n + 31) / 32;
+  a.blocks = std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->smCount * blocksPerSm, (warps * 32 + 127) / 128));
+  a.stream = st;
+  CUDA_TRY(ctx, evolve_launch_plain_interrupt(a));
+  ++ctx->launches;
+  return GAL_OK;
+}
+
+int gal_gpu_evolve_batch_interrupt(gal_ctx* ctx, int64_t n, double* state, const double* param, const double* tStart,
+                                   const double* tEnd, double* step, const int32_t* components, int32_t* status,
+                                   uint32_t* counters, double* tReached, int32_t* task) {
+  if (!ctx) return fail(nullptr, GAL_ERR_ARGUMENT, "NULL context%s");
+  if (n < 0) return fail(ctx, GAL_ERR_ARGUMENT, "negative node count%s");
+  if (n == 0) return GAL_OK;
+  if (!state || !param || !tStart || !tEnd || !step || !components || !status || !tReached || !task)
+    return fail(ctx, GAL_ERR_ARGUMENT, "NULL array%s");
+  if (ctx_mode(ctx) != MODE_PLAIN)
+    return fail(ctx, GAL_ERR_ARGUMENT, "interrupts are available in the FP64-rate form without a surrogate%s");
+  // One device buffer: state, param, t0, t1, step, t_reached (FP64), then
+  // components, status, task, counters.
+  const size_t nd = (size_t)n * (GAL_NY + GAL_NP + 4);
+  const size_t bytes = nd * sizeof(double) + (size_t)n * 3 * sizeof(int32_t) + (size_t)n * 3 * sizeof(uint32_t) + 256;
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  if (bytes > ctx->bufBytes) {
+    cudaFree(ctx->dBuf);
+    ctx->dBuf = nullptr;
+    ctx->bufBytes = 0;
+    CUDA_TRY(ctx, cudaMalloc(&ctx->dBuf, bytes));
+    ctx->bufBytes = bytes;
+  }
+  double* dState = (double*)ctx->dBuf;
+  double* dParam = dState + (size_t)n * GAL_NY;
+  double* dT0 = dParam + (size_t)n * GAL_NP;
+  double* dT1 = dT0 + n;
+  double* dStep = dT1 + n;
+  double* dReached = dStep + n;
+  int32_t* dComponents = (int32_t*)(dReached + n);
+  int32_t* dStatus = dComponents + n;
+  int32_t* dTask = dStatus + n;
+  uint32_t* dCounters = (uint32_t*)(dTask + n);
+  cudaStream_t st = ctx->stream;
+  CUDA_TRY(ctx, cudaMemcpyAsync(dState, state, (size_t)n * GAL_NY * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(dParam, param, (size_t)n * GAL_NP * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(dT0, tStart, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(dT1, tEnd, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(dStep, step, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(dComponents, components, (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  int rc = gal_gpu_evolve_batch_interrupt_device(ctx, n, dState, dParam, dT0, dT1, dStep, dComponents, dStatus,
+                                                 counters ? dCounters : nullptr, dReached, dTask, (void*)st);
+  if (rc) return rc;
+  CUDA_TRY(ctx, cudaMemcpyAsync(state, dState, (size_t)n * GAL_NY * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(step, dStep, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(status, dStatus, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(tReached, dReached, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(task, dTask, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   if (counters)
     CUDA_TRY(ctx, cudaMemcpyAsync(counters, dCounters, (size_t)n * 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(ctx, cudaStreamSynchronize(st));

@@ -530,6 +530,22 @@ __device__ __forceinline__ void rhs(const Globals& G, const Smem& S, const NodeC
   }
 }
 
+// The components to create for one evaluation of an interrupt-form
+// integration: those missing from `components` (GAL_COMPONENT_*) that
+// receive a non-zero rate in one of their properties (a null component's
+// rate function interrupts to create the component).
+__device__ __forceinline__ int32_t interrupt_request(uint32_t components, const double* d) {
+  int32_t task = 0;
+  if (!(components & GAL_COMPONENT_DISK) && (d[GAL_Y_DISK_GAS] != 0.0 || d[GAL_Y_DISK_GAS_METALS] != 0.0 ||
+                                             d[GAL_Y_DISK_STARS] != 0.0 || d[GAL_Y_DISK_STARS_METALS] != 0.0))
+    task |= GAL_INTERRUPT_CREATE_DISK;
+  if (!(components & GAL_COMPONENT_SPHEROID) &&
+      (d[GAL_Y_SPHEROID_GAS] != 0.0 || d[GAL_Y_SPHEROID_GAS_METALS] != 0.0 || d[GAL_Y_SPHEROID_STARS] != 0.0))
+    task |= GAL_INTERRUPT_CREATE_SPHEROID;
+  if (!(components & GAL_COMPONENT_BLACK_HOLE) && d[GAL_Y_BLACK_HOLE] != 0.0) task |= GAL_INTERRUPT_CREATE_BLACK_HOLE;
+  return task;
+}
+
 // Post-step clamps of the standard components (hot_halo/standard/_class.F90:
 // 455-530, disk/standard/_class.F90:473-677, spheroid/standard/_class.F90:
 // 464-636); all return GSL_Continue, so the evolver is not reset.  Returns

@@ -115,3 +115,33 @@ class MergerTreeNodeEvolverStandard:
         if counters:
             out.append(cnt)
         return tuple(out) if len(out) > 1 else (out[0] if out else None)
+
+    def evolve_interruptible(self, state, param, time_start, time_end, step, components, counters=False):
+        """Evolve a batch in place with interrupts: the reference's
+        ``evolve(..., interrupted, functionInterrupt, ...)``.  ``components``
+        holds each node's GAL_COMPONENT_* mask; a node that gives a rate to a
+        component it does not have stops at that time.  Returns (status,
+        t_reached, task[, counters]): status GAL_STATUS_INTERRUPTED (9) with
+        the time reached and the GAL_INTERRUPT_* task of the components to
+        create, GAL_STATUS_SUCCESS at time_end, or a failure code."""
+        state = np.asarray(state)
+        if state.dtype != np.float64 or not state.flags.c_contiguous:
+            raise ValueError("state must be a C-contiguous float64 array")
+        n = state.shape[1]
+        param = np.ascontiguousarray(param, dtype=np.float64)
+        t0 = np.ascontiguousarray(time_start, dtype=np.float64)
+        t1 = np.ascontiguousarray(time_end, dtype=np.float64)
+        comps = np.ascontiguousarray(components, dtype=np.int32)
+        if (param.shape != (_abi.NP, n) or t0.shape != (n,) or t1.shape != (n,) or comps.shape != (n,)
+                or step.dtype != np.float64 or step.shape != (n,)):
+            raise ValueError("array shapes do not match the node count")
+        status = np.zeros(n, dtype=np.int32)
+        reached = np.zeros(n)
+        task = np.zeros(n, dtype=np.int32)
+        cnt = np.zeros((3, n), dtype=np.uint32) if counters else None
+        ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        rc = self.lib.gal_gpu_evolve_batch_interrupt(
+            self.ctx, n, _dp(state), _dp(param), _dp(t0), _dp(t1), _dp(step), ip(comps), ip(status),
+            cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)) if counters else None, _dp(reached), ip(task))
+        _check(self.lib, self.ctx, rc)
+        return (status, reached, task, cnt) if counters else (status, reached, task)

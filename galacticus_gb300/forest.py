@@ -110,6 +110,30 @@ class Forest:
                       self.spin[idx].copy()), idx
 
 
+def lpt_assignment(forest, n_ranks):
+    """Trees to ranks by longest processing time first, node count as the
+    cost (the reference's work sharing hands out forests largest first,
+    tasks/evolve_forests/work_share/_class.F90:37): trees in decreasing
+    node count (ties by tree id) each go to the rank with the fewest nodes
+    so far (ties to the lowest rank).  Returns one sorted array of tree ids
+    per rank."""
+    counts = np.bincount(forest.tree, minlength=forest.n_trees)
+    order = np.lexsort((np.arange(len(counts)), -counts))
+    load = np.zeros(n_ranks, dtype=np.int64)
+    owner = np.empty(len(counts), dtype=np.int64)
+    for t in order:
+        r = int(np.argmin(load))
+        owner[t] = r
+        load[r] += counts[t]
+    return [np.flatnonzero(owner == r) for r in range(n_ranks)]
+
+
+def partition(forest, rank, n_ranks):
+    """This rank's share of one forest (lpt_assignment): (sub-forest, [n]
+    original node indices)."""
+    return forest.subset(lpt_assignment(forest, n_ranks)[rank])
+
+
 def pch_params():
     lib = _declare(_abi.load_library())
     p = PchParams()

@@ -146,6 +146,28 @@ def galaxy_halos(n=8192, seed=12, cosmology=None, spin=SPIN_DEFAULT):
     return batch
 
 
+def disk_creation_halos(n=8192, seed=21, cosmology=None, spin=SPIN_DEFAULT):
+    """Halos without a disk whose hot gas starts to cool during the step:
+    the halos, times and timesteps of isolated_halos(), hot gas log-uniform
+    in 1e-3-0.3 of the halo's baryons (Omega_b/Omega_m) M with metallicity
+    log-uniform 1e-4-0.02, and halo growth at 0.05-0.5 M per Gyr, whose
+    accreted gas raises the cooling rate.  Returns (batch, components): the
+    GAL_COMPONENT_* masks say every halo has a spheroid and a black hole and
+    no disk, so that cooling into the disk interrupts the integration (at
+    the start, part way through the step, or never)."""
+    batch = isolated_halos(n=n, seed=seed, cosmology=cosmology, spin=spin)
+    cosmo = cosmology or Cosmology()
+    rng = np.random.Generator(np.random.Philox(key=seed + 2000))
+    u = rng.random((3, n))
+    mass = batch.param[_abi.P_MASS]
+    hot = cosmo.omega_baryon / cosmo.omega_matter * mass * 10.0 ** (-3.0 + 2.5 * u[0])
+    batch.state[_abi.Y_HOT_MASS] = hot
+    batch.state[_abi.Y_HOT_METALS] = hot * 10.0 ** (-4.0 + np.log10(200.0) * u[1])
+    batch.param[_abi.P_MASS_RATE] = mass * (0.05 + 0.45 * u[2])
+    components = np.full(n, _abi.COMPONENT_SPHEROID | _abi.COMPONENT_BLACK_HOLE, dtype=np.int32)
+    return batch, components
+
+
 def isolated_params(tolerance_relative=1.0e-3):
     """P-std parameters with the batched-isolated-step tolerances."""
     p = _abi.default_params()

@@ -69,7 +69,29 @@ enum {
   GAL_STATUS_SUCCESS = 0,     /* errorStatusSuccess                            */
   GAL_STATUS_UNDERFLOW = 15,  /* errorStatusUnderflow: all ODE trials failed   */
   GAL_STATUS_XCPU = 1025,     /* errorStatusXCPU: per-node step budget used up */
-  GAL_STATUS_NOT_FINITE = 2001 /* a state value became NaN or infinite       */
+  GAL_STATUS_NOT_FINITE = 2001, /* a state value became NaN or infinite      */
+  GAL_STATUS_INTERRUPTED = 9   /* odeSolverInterrupt (= GSL_EBADFUNC): the
+                                  evolution stopped early for an interrupt
+                                  task (gal_gpu_evolve_batch_interrupt)       */
+};
+
+/* ---- components and interrupt tasks (gal_gpu_evolve_batch_interrupt) -----
+ * components[i] says which optional components node i has.  As in the
+ * reference, where a rate into a component the node does not have makes
+ * that component's null-class rate function interrupt the integration so
+ * that the host creates it, an evaluation that gives a non-zero rate to a
+ * property of a missing component interrupts; the task is the bit mask of
+ * the components to create. */
+enum {
+  GAL_COMPONENT_DISK = 1,
+  GAL_COMPONENT_SPHEROID = 2,
+  GAL_COMPONENT_BLACK_HOLE = 4,
+  GAL_COMPONENT_ALL = 7
+};
+enum {
+  GAL_INTERRUPT_CREATE_DISK = 1,
+  GAL_INTERRUPT_CREATE_SPHEROID = 2,
+  GAL_INTERRUPT_CREATE_BLACK_HOLE = 4
 };
 
 /* ---- library error codes ------------------------------------------------- */
@@ -172,6 +194,12 @@ typedef struct gal_params {
   int32_t pad;
   double bh_efficiency_radiative;  /* 1 - E_ISCO(spin 0) = 1 - sqrt(8/9)     */
   double bh_efficiency_jet;        /* 0                                      */
+  /* mergerTreeEvolveTimestepSimple (merger_trees/evolve/timesteps/simple.F90:
+   * 71-80, 124-161): in a forest, one evolve call advances a node by at most
+   * min(timestep_relative / H(t), timestep_absolute), H the expansion rate
+   * at the call's start (timestep_relative <= 0: the absolute limit alone). */
+  double timestep_relative;        /* timeStepRelative (0.1)                 */
+  double timestep_absolute;        /* timeStepAbsolute, Gyr (1)              */
 } gal_params;
 
 /* Cooling-function and electron-density tables in the layout of the
@@ -234,6 +262,32 @@ int gal_gpu_evolve_batch(gal_ctx* ctx, int64_t n, double* state, const double* p
 int gal_gpu_evolve_batch_device(gal_ctx* ctx, int64_t n, double* state, const double* param,
                                 const double* t_start, const double* t_end, double* step,
                                 int32_t* status, uint32_t* counters, void* stream);
+
+/* Evolution with interrupts: mergerTreeNodeEvolver%evolve with its
+ * `interrupted` and `functionInterrupt` outputs (node_evolver/_class.F90:
+ * 41-57; standard.F90:385-406, 575-578, 729-737, 895-945; the solver's
+ * re-targeting numerical/ODE_solver/solver.F90:608-620).  Arrays as in
+ * gal_gpu_evolve_batch, plus
+ *   components [n]  in   GAL_COMPONENT_* mask of the components node i has
+ *   t_reached  [n]  out  the time node i reached: t_end[i], or the time of
+ *                        its earliest interrupt
+ *   task       [n]  out  GAL_INTERRUPT_* mask of that interrupt (0: none)
+ * An interrupted node has status GAL_STATUS_INTERRUPTED, its state at
+ * t_reached[i] and step[i] = -1 (node%timeStepSet(-1)); the caller creates
+ * the components named by the task and evolves it again from t_reached.
+ * Every evaluation at or after an interrupt time returns zero derivatives,
+ * and the step function evaluates f(t+h, y_new) on every attempt, as GSL's
+ * rkck does, since that evaluation can interrupt too.  FP64 rates only
+ * (GAL_ERR_ARGUMENT in the FP32-rate form or with a surrogate installed);
+ * 128 threads per block. */
+int gal_gpu_evolve_batch_interrupt(gal_ctx* ctx, int64_t n, double* state, const double* param, const double* t_start,
+                                   const double* t_end, double* step, const int32_t* components, int32_t* status,
+                                   uint32_t* counters, double* t_reached, int32_t* task);
+/* As gal_gpu_evolve_batch_interrupt on device arrays, enqueued on `stream`. */
+int gal_gpu_evolve_batch_interrupt_device(gal_ctx* ctx, int64_t n, double* state, const double* param,
+                                          const double* t_start, const double* t_end, double* step,
+                                          const int32_t* components, int32_t* status, uint32_t* counters,
+                                          double* t_reached, int32_t* task, void* stream);
 
 /* Evolution for callers that cannot let a library allocate device memory,
  * e.g. a host code whose pool allocator owns all device memory, or one that

@@ -28,8 +28,12 @@
  * index order.  A primary progenitor's halo mass grows linearly to its
  * parent's over the interval; its hot halo accretes (Omega_b/Omega_m) times
  * the parent's mass not brought in by its progenitors.  The interval is cut
- * at every output time inside it (each piece is one evolve call, with the
- * step size carried over), and the state at each output time is recorded.
+ * into evolve calls at every output time inside it and wherever a call would
+ * be longer than the timestep limit min(timestep_relative / H(t),
+ * timestep_absolute) of gal_params (merger_trees/evolve/timesteps/
+ * simple.F90:124-161); each call recomputes the halo's mass, virial radius
+ * and velocity at its start, carries the step size over, and the state at
+ * each output time is recorded.
  */
 #ifndef GALNODE_FOREST_H
 #define GALNODE_FOREST_H

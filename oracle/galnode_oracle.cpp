@@ -725,6 +725,33 @@ const double e1 = 37.0 / 378.0 - 2825.0 / 27648.0, e3 = 250.0 / 621.0 - 18575.0 
 const unsigned order = 5;  // order reported by GSL's rkck stepper to the controller
 }  // namespace ck
 
+// sc2_control_hadjust (external/gslODEInitVal2/cscal2.c:93-169) with
+// a_y=1, a_dydt=0 (numerical/ODE_solver/solver.F90:365-366) and no
+// non-negativity constraints (enforceNonNegativity=false by default).
+template <class R>
+static int control_hadjust(int dim, const R* y, const R* yerr, double epsAbs, double epsRel, const double* scale, R& h) {
+  const R hOld = h;
+  R rmax = R(DBL_MIN);
+  for (int i = 0; i < dim; ++i) {
+    R D0 = R(epsRel) * xabs(y[i]) + R(epsAbs) * R(scale[i]);
+    R r = xabs(yerr[i]) / xabs(D0);
+    rmax = xmax(r, rmax);
+  }
+  if (rmax > R(1.1)) {
+    R r = R(0.9) / xpow(rmax, R(1.0 / (double)ck::order));
+    if (r < R(0.2)) r = R(0.2);
+    h = r * hOld;
+    return HADJ_DEC;
+  } else if (rmax < R(0.5)) {
+    R r = R(0.9) / xpow(rmax, R(1.0 / ((double)ck::order + 1.0)));
+    if (r > R(4.9)) r = R(4.9);
+    if (r < R(1.0)) r = R(1.0);
+    h = r * hOld;
+    return HADJ_INC;
+  }
+  return HADJ_NIL;
+}
+
 template <class R, class F>
 struct Solver {
   int dim;
@@ -764,31 +791,8 @@ struct Solver {
       yerr[i] = h * (R(ck::e1) * k1[i] + R(ck::e3) * k3[i] + R(ck::e4) * k4[i] + R(ck::e5) * k5[i] + R(ck::e6) * k6[i]);
   }
 
-  // sc2_control_hadjust (external/gslODEInitVal2/cscal2.c:93-169) with
-  // a_y=1, a_dydt=0 (numerical/ODE_solver/solver.F90:365-366) and no
-  // non-negativity constraints (enforceNonNegativity=false by default).
-  int hadjust(const R* y, R& h) {
-    const R hOld = h;
-    R rmax = R(DBL_MIN);
-    for (int i = 0; i < dim; ++i) {
-      R D0 = R(epsRel) * xabs(y[i]) + R(epsAbs) * R(scale[i]);
-      R r = xabs(yerr[i]) / xabs(D0);
-      rmax = xmax(r, rmax);
-    }
-    if (rmax > R(1.1)) {
-      R r = R(0.9) / xpow(rmax, R(1.0 / (double)ck::order));
-      if (r < R(0.2)) r = R(0.2);
-      h = r * hOld;
-      return HADJ_DEC;
-    } else if (rmax < R(0.5)) {
-      R r = R(0.9) / xpow(rmax, R(1.0 / ((double)ck::order + 1.0)));
-      if (r > R(4.9)) r = R(4.9);
-      if (r < R(1.0)) r = R(1.0);
-      h = r * hOld;
-      return HADJ_INC;
-    }
-    return HADJ_NIL;
-  }
+  // The step-size controller (control_hadjust).
+  int hadjust(const R* y, R& h) { return control_hadjust(dim, y, yerr, epsAbs, epsRel, scale, h); }
 
   // gsl_odeiv2_evolve_apply for a stepper that can use dydt_in (GSL manual,
   // "Evolution"): take one accepted step from *t toward t1, retrying with the
@@ -919,9 +923,242 @@ static int evolve_node(const gal_params& p, const Table& tb, const double* prm, 
 }
 
 // ---------------------------------------------------------------------------
+// Interrupts: a node operator may interrupt the integration (the null
+// component's rate functions do so to create a component that receives a
+// rate, e.g. cooling into a disk that does not exist yet).  standardODEs
+// (node_evolver/standard.F90:895-945) returns zero derivatives from an
+// evaluation that requests one and, when it is the earliest so far, records
+// its time and task and returns odeSolverInterrupt (= GSL_EBADFUNC,
+// numerical/ODE_solver/error_codes.F90:33); GSL's rkck and evolve_apply
+// abandon the step (the state stays at its start); odeSolver%solve
+// (solver.F90:608-620) then re-targets the integration to the interrupt time
+// and carries on, every evaluation at or after that time returning zero
+// derivatives; evolve (standard.F90:575-578, 729-737) reports the node as
+// interrupted at that time with node%timeStep = -1.  The stepper evaluates
+// dydt_out = f(t+h, y_new) on every attempt, as GSL's rkck does, since that
+// evaluation can interrupt too.  After an abandoned attempt the next one
+// starts from the same (t, y) and its derivative.  The interrupt time and
+// task persist over the trials of one evolve call; a trial restarted after
+// an interrupt integrates to the interrupt time (the reference integrates
+// on to the end with zero derivatives beyond it, which leaves the state at
+// the interrupt time up to the steps that straddle it).
+// ---------------------------------------------------------------------------
+enum { GSL_INTERRUPT = -3 };
+
+struct Interrupts {
+  uint32_t components;  // GAL_COMPONENT_* of the components that exist
+  bool found = false;
+  double time = 0.0;
+  int32_t task = 0;     // GAL_INTERRUPT_* of the earliest interrupt
+};
+
+// The components to create for one evaluation: those that do not exist and
+// receive a non-zero rate in one of their properties.
+static int32_t interrupt_request(uint32_t components, const double* d) {
+  int32_t task = 0;
+  if (!(components & GAL_COMPONENT_DISK) && (d[GAL_Y_DISK_GAS] != 0.0 || d[GAL_Y_DISK_GAS_METALS] != 0.0 ||
+                                             d[GAL_Y_DISK_STARS] != 0.0 || d[GAL_Y_DISK_STARS_METALS] != 0.0))
+    task |= GAL_INTERRUPT_CREATE_DISK;
+  if (!(components & GAL_COMPONENT_SPHEROID) &&
+      (d[GAL_Y_SPHEROID_GAS] != 0.0 || d[GAL_Y_SPHEROID_GAS_METALS] != 0.0 || d[GAL_Y_SPHEROID_STARS] != 0.0))
+    task |= GAL_INTERRUPT_CREATE_SPHEROID;
+  if (!(components & GAL_COMPONENT_BLACK_HOLE) && d[GAL_Y_BLACK_HOLE] != 0.0) task |= GAL_INTERRUPT_CREATE_BLACK_HOLE;
+  return task;
+}
+
+template <class F>
+struct SolverI {
+  int dim;
+  F& f;
+  Interrupts& in;
+  double epsAbs, epsRel;
+  const double* scale;
+  uint64_t budget = 0;
+  uint64_t count = 0, failed = 0, accepted = 0;
+  bool haveDydtIn = false;  // dydtIn holds f at the current (t, y)
+  double dydtIn[MAXDIM], dydtOut[MAXDIM], yerr[MAXDIM];
+  double k2[MAXDIM], k3[MAXDIM], k4[MAXDIM], k5[MAXDIM], k6[MAXDIM], tmp[MAXDIM];
+
+  // One evaluation at time ts (standardODEs): zero beyond the first
+  // interrupt; true when it requests the earliest interrupt so far.
+  bool eval(double ts, const double* y, double* d) {
+    if (in.found && ts >= in.time) {
+      for (int i = 0; i < dim; ++i) d[i] = 0.0;
+      return false;
+    }
+    f(ts, y, d);
+    const int32_t req = interrupt_request(in.components, d);
+    if (req) {
+      for (int i = 0; i < dim; ++i) d[i] = 0.0;
+      if (!in.found || ts < in.time) {
+        in.found = true;
+        in.time = ts;
+        in.task = req;
+        return true;
+      }
+    }
+    return false;
+  }
+
+  // rkck_apply with dydt_out: true when an evaluation interrupts (y untouched).
+  bool step(double t, double h, const double* y, double* yn) {
+    const double* k1 = dydtIn;
+    for (int i = 0; i < dim; ++i) tmp[i] = y[i] + ck::b21 * h * k1[i];
+    if (eval(t + ck::a2 * h, tmp, k2)) return true;
+    for (int i = 0; i < dim; ++i) tmp[i] = y[i] + h * (ck::b31 * k1[i] + ck::b32 * k2[i]);
+    if (eval(t + ck::a3 * h, tmp, k3)) return true;
+    for (int i = 0; i < dim; ++i) tmp[i] = y[i] + h * (ck::b41 * k1[i] + ck::b42 * k2[i] + ck::b43 * k3[i]);
+    if (eval(t + ck::a4 * h, tmp, k4)) return true;
+    for (int i = 0; i < dim; ++i) tmp[i] = y[i] + h * (ck::b51 * k1[i] + ck::b52 * k2[i] + ck::b53 * k3[i] + ck::b54 * k4[i]);
+    if (eval(t + ck::a5 * h, tmp, k5)) return true;
+    for (int i = 0; i < dim; ++i)
+      tmp[i] = y[i] + h * (ck::b61 * k1[i] + ck::b62 * k2[i] + ck::b63 * k3[i] + ck::b64 * k4[i] + ck::b65 * k5[i]);
+    if (eval(t + ck::a6 * h, tmp, k6)) return true;
+    for (int i = 0; i < dim; ++i) yn[i] = y[i] + h * (ck::c1 * k1[i] + ck::c3 * k3[i] + ck::c4 * k4[i] + ck::c6 * k6[i]);
+    if (eval(t + h, yn, dydtOut)) return true;
+    for (int i = 0; i < dim; ++i)
+      yerr[i] = h * (ck::e1 * k1[i] + ck::e3 * k3[i] + ck::e4 * k4[i] + ck::e5 * k5[i] + ck::e6 * k6[i]);
+    return false;
+  }
+
+  int hadjust(const double* y, double& h) { return control_hadjust(dim, y, yerr, epsAbs, epsRel, scale, h); }
+
+  int evolve_apply(double& t, double t1, double& h, double* y) {
+    const double t0 = t;
+    double h0 = h;
+    const double dt = t1 - t0;
+    if (!haveDydtIn) {
+      if (eval(t0, y, dydtIn)) return GSL_INTERRUPT;
+      haveDydtIn = true;
+    }
+    for (;;) {
+      const bool finalStep = (dt >= 0.0 && h0 > dt) || (dt < 0.0 && h0 < dt);
+      if (finalStep) h0 = dt;
+      double yn[MAXDIM];
+      if (step(t0, h0, y, yn)) return GSL_INTERRUPT;  // t, y and h as they were
+      ++count;
+      const double tNew = finalStep ? t1 : t0 + h0;
+      const double hOld = h0;
+      if (hadjust(yn, h0) == HADJ_DEC) {
+        volatile double tCurr = tNew, tNext = tNew + h0;
+        if (std::fabs(h0) < std::fabs(hOld) && tNext != tCurr) {
+          ++failed;
+          if (budget && count >= budget) return GSL_BUDGET;
+          continue;
+        }
+        h = hOld;
+        return GSL_FAILURE;
+      }
+      ++accepted;
+      t = tNew;
+      h = h0;
+      for (int i = 0; i < dim; ++i) {
+        y[i] = yn[i];
+        dydtIn[i] = dydtOut[i];
+      }
+      return GSL_SUCCESS;
+    }
+  }
+
+  // driver2_apply, then odeSolver%solve's re-targeting at each interrupt.
+  int solve(double& t, double t1, double& h, double* y, uint64_t stepBudget, bool& budgetExhausted) {
+    budget = stepBudget;
+    double target = t1;
+    while (target - t > 0.0) {
+      const int s = evolve_apply(t, target, h, y);
+      if (s == GSL_INTERRUPT) {
+        target = in.time;
+        continue;
+      }
+      if (s == GSL_BUDGET) {
+        budgetExhausted = true;
+        return GSL_FAILURE;
+      }
+      if (s != GSL_SUCCESS) return s;
+      post_step(y);
+      if (stepBudget && count >= stepBudget && target - t > 0.0) {
+        budgetExhausted = true;
+        return GSL_FAILURE;
+      }
+    }
+    return GSL_SUCCESS;
+  }
+};
+
+// evolve with interrupts (node_evolver/standard.F90:385-755 with the
+// interrupted/functionInterrupt outputs): as evolve_node, plus the time
+// reached and the interrupt task (0: not interrupted).
+static int evolve_node_interruptible(const gal_params& p, const Table& tb, const double* prm, double* yio, double t0,
+                                     double t1, double& stepInOut, uint32_t components, double& tReached,
+                                     int32_t& task, uint32_t counters[3], bool brent) {
+  Node n;
+  node_setup(p, prm, n);
+  double s[GAL_NY];
+  scales(yio, n.massHalo, s);
+  Rhs<double> rhs{p, tb, n, brent};
+  Interrupts in{components};
+  int status = GAL_STATUS_SUCCESS;
+  uint32_t nAcc = 0, nRej = 0;
+  double stepSize = -1.0;
+  if (t0 != t1) {
+    int trial = 0;
+    int ode = GSL_FAILURE;
+    double ysave[GAL_NY];
+    for (int i = 0; i < GAL_NY; ++i) ysave[i] = yio[i];
+    while (trial < p.trial_count_maximum && ode != GSL_SUCCESS) {
+      stepSize = p.reuse_step_size ? stepInOut / std::ldexp(1.0, trial) : -1.0;
+      const double target = in.found ? std::min(in.time, t1) : t1;
+      double hStart = target - t0;
+      if (stepSize > 0.0) hStart = std::min(stepSize, hStart);
+      SolverI<Rhs<double>> sv{GAL_NY, rhs, in, p.ode_tolerance_absolute, p.ode_tolerance_relative, s};
+      double y[GAL_NY];
+      for (int i = 0; i < GAL_NY; ++i) y[i] = yio[i];
+      double t = t0, h = hStart;
+      bool exhausted = false;
+      ode = target > t0 ? sv.solve(t, target, h, y, (uint64_t)p.step_budget, exhausted) : GSL_SUCCESS;
+      nAcc += (uint32_t)sv.accepted;
+      nRej += (uint32_t)sv.failed;
+      if (exhausted) {
+        for (int i = 0; i < GAL_NY; ++i) yio[i] = ysave[i];
+        status = GAL_STATUS_XCPU;
+        break;
+      }
+      if (ode == GSL_SUCCESS) {
+        for (int i = 0; i < GAL_NY; ++i) yio[i] = y[i];
+        stepSize = h;
+      } else {
+        ++trial;
+        for (int i = 0; i < GAL_NY; ++i) yio[i] = ysave[i];
+      }
+    }
+    if (status == GAL_STATUS_SUCCESS && ode != GSL_SUCCESS) status = GAL_STATUS_UNDERFLOW;
+  }
+  tReached = t1;
+  task = 0;
+  if (status == GAL_STATUS_SUCCESS) {
+    for (int i = 0; i < GAL_NY; ++i)
+      if (!std::isfinite(yio[i])) status = GAL_STATUS_NOT_FINITE;
+    stepInOut = stepSize;  // node%timeStepSet(stepSize)
+    if (status == GAL_STATUS_SUCCESS && in.found) {
+      status = GAL_STATUS_INTERRUPTED;
+      tReached = in.time;  // basic%timeSet(timeInterruptFirst)
+      task = in.task;
+      stepInOut = -1.0;    // node%timeStepSet(-1)
+    }
+  }
+  if (counters) {
+    counters[0] = nAcc;
+    counters[1] = nRej;
+    counters[2] = (uint32_t)rhs.evaluations;
+  }
+  return status;
+}
+
+// ---------------------------------------------------------------------------
 // Forests: the tree evolver's node loop (merger_trees/evolver/standard.F90:
 // 762-1035) over a whole forest.  A node evolves from its own time to its
-// parent's, in pieces cut at the output times (each piece one evolve call,
+// parent's, in pieces cut at the output times and at the timestep limit of
+// mergerTreeEvolveTimestepSimple (each piece one evolve call,
 // the step size carried over as node%timeStep), and on reaching the parent
 // the primary progenitor's state is promoted and the other progenitors'
 // states are added to it, component by component in index order.
@@ -933,6 +1170,15 @@ struct Cosmology {
   double redshift(double t) const {
     const double x = std::sinh(1.5 * hubbleGyr() * std::sqrt(ol) * t);
     return 1.0 / std::pow(x / std::sqrt(ol / om), 2.0 / 3.0) - 1.0;
+  }
+  // mergerTreeEvolveTimestepSimple%timeEvolveTo (merger_trees/evolve/
+  // timesteps/simple.F90:124-161): a node at time t may be evolved to at most
+  // t + min(relative / H(t), absolute), H = expansionRate(a(t)) (1/Gyr).
+  double step_limit(double t, double relative, double absolute) const {
+    if (!(relative > 0.0)) return absolute;
+    const double zp = 1.0 + redshift(t);
+    const double rate = hubbleGyr() * std::sqrt(om * zp * zp * zp + ol);
+    return std::min(relative / rate, absolute);
   }
   // Bryan & Norman (1998) contrast relative to the mean density
   // (virial_density_contrast/Bryan_Norman.F90:172-196); r_vir and V_vir.
@@ -984,8 +1230,11 @@ static int evolve_forest_node(const gal_params& p, const Table& tb, const Cosmol
   int32_t k = 0;
   while (k < F.nOut && !(F.tOut[k] > t0)) ++k;
   while (a < t1 && status == GAL_STATUS_SUCCESS) {
-    const bool atOutput = k < F.nOut && F.tOut[k] < t1;
-    const double b = atOutput ? F.tOut[k] : t1;
+    // timeEvolveTo (merger_trees/evolver/standard.F90:762-1035): the earliest
+    // of the parent's time, the next output and the timestep criterion.
+    const double limit = a + cos.step_limit(a, p.timestep_relative, p.timestep_absolute);
+    const bool atOutput = k < F.nOut && F.tOut[k] < t1 && !(limit < F.tOut[k]);
+    const double b = atOutput ? F.tOut[k] : std::min(limit, t1);
     const double M = F.mass[i] + (massEnd - F.mass[i]) * (a - t0) / (t1 - t0);
     double prm[GAL_NP];
     double r, v;
@@ -1035,6 +1284,38 @@ int oracle_evolve_batch(const gal_params* p, const gal_cie_table* table, int64_t
     for (int v = 0; v < GAL_NY; ++v) state[v * n + i] = y[v];
     step[i] = h;
     status[i] = s;
+    if (counters)
+      for (int v = 0; v < 3; ++v) counters[v * n + i] = c[v];
+  }
+  return GAL_OK;
+}
+
+// Evolve a batch with interrupts (gal_gpu_evolve_batch_interrupt's arrays).
+int oracle_evolve_batch_interrupt(const gal_params* p, const gal_cie_table* table, int64_t n, double* state,
+                                  const double* param, const double* t_start, const double* t_end, double* step,
+                                  const int32_t* components, int32_t* status, uint32_t* counters, double* t_reached,
+                                  int32_t* task, int threads, int cooling_brent) {
+  if (!p || !table || n < 0 || !components || !t_reached || !task) return GAL_ERR_ARGUMENT;
+  orc::Table tb;
+  int rc = orc::table_load(table, tb);
+  if (rc) return rc;
+  if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(threads)
+  for (int64_t i = 0; i < n; ++i) {
+    double y[GAL_NY], prm[GAL_NP];
+    for (int v = 0; v < GAL_NY; ++v) y[v] = state[v * n + i];
+    for (int v = 0; v < GAL_NP; ++v) prm[v] = param[v * n + i];
+    double h = step[i];
+    uint32_t c[3];
+    double tr = 0.0;
+    int32_t tk = 0;
+    int s = orc::evolve_node_interruptible(*p, tb, prm, y, t_start[i], t_end[i], h, (uint32_t)components[i], tr, tk, c,
+                                           cooling_brent != 0);
+    for (int v = 0; v < GAL_NY; ++v) state[v * n + i] = y[v];
+    step[i] = h;
+    status[i] = s;
+    t_reached[i] = tr;
+    task[i] = tk;
     if (counters)
       for (int v = 0; v < 3; ++v) counters[v * n + i] = c[v];
   }

@@ -78,6 +78,31 @@ def evolve_batch(params, table, state, param, t_start, t_end, step, threads=0, b
     return state, step, status, counters
 
 
+def evolve_batch_interrupt(params, table, state, param, t_start, t_end, step, components, threads=0, brent=True):
+    """Evolve copies of the given SoA arrays on the CPU with interrupts
+    (gal_gpu_evolve_batch_interrupt's semantics).  Returns (state, step,
+    status, counters, t_reached, task)."""
+    n = state.shape[1]
+    state = np.ascontiguousarray(state, dtype=np.float64).copy()
+    param = np.ascontiguousarray(param, dtype=np.float64)
+    t_start = np.ascontiguousarray(t_start, dtype=np.float64)
+    t_end = np.ascontiguousarray(t_end, dtype=np.float64)
+    step = np.ascontiguousarray(step, dtype=np.float64).copy()
+    components = np.ascontiguousarray(components, dtype=np.int32)
+    status = np.zeros(n, dtype=np.int32)
+    counters = np.zeros((3, n), dtype=np.uint32)
+    t_reached = np.zeros(n)
+    task = np.zeros(n, dtype=np.int32)
+    ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    rc = lib().oracle_evolve_batch_interrupt(
+        ctypes.byref(params), ctypes.byref(table.struct), n, _dp(state), _dp(param), _dp(t_start), _dp(t_end),
+        _dp(step), ip(components), ip(status), counters.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+        _dp(t_reached), ip(task), int(threads), 1 if brent else 0)
+    if rc != 0:
+        raise RuntimeError(f"oracle_evolve_batch_interrupt failed with code {rc}")
+    return state, step, status, counters, t_reached, task
+
+
 def ode_test(problem, x0, x1, y, tol_abs, tol_rel):
     y = np.ascontiguousarray(y, dtype=np.float64).copy()
     rc = lib().oracle_ode_test(problem, x0, x1, _dp(y), tol_abs, tol_rel)

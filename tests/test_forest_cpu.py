@@ -142,3 +142,45 @@ def test_oracle_forest_is_deterministic_across_threads(small_forest, params, tab
     b = oracle_mod.evolve_forest(params, table, small_forest, state0, times, threads=4)
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[3], b[3])
+
+
+def test_timestep_criterion_cuts_evolve_calls(params):
+    """The tree evolver's evolve calls are limited by
+    mergerTreeEvolveTimestepSimple (merger_trees/evolve/timesteps/
+    simple.F90:124-161): a call from t ends no later than
+    t + min(0.1 / H(t), 1 Gyr).  A two-node forest (a leaf at z = 3 whose
+    parent is the root at z = 0) evolved by the oracle equals the chain of
+    single evolve calls over exactly those pieces, each with the halo's mass
+    and virial scales at its start and the step size carried over."""
+    from galacticus_gb300.cie_tables import CieTable
+    from oracle import oracle
+    table = CieTable()
+    cosmo = workloads.Cosmology()
+    t_root, t_leaf = cosmo.time(0.0), cosmo.time(3.0)
+    f = forest.Forest(np.array([0, 0], np.int32), np.array([-1, 0], np.int32), np.array([1, 0], np.int32),
+                      np.array([1, 0], np.int32), np.array([t_root, t_leaf]), np.array([1e12, 3e11]),
+                      np.array([0.04, 0.04]))
+    state0 = forest.initial_state(params, f)
+    got = oracle.evolve_forest(params, table, f, state0, np.array([]), brent=True)[0][:, 1]
+    # The pieces: a_{k+1} = min(a_k + min(0.1/H(a_k), 1), t_root).
+    cuts = [t_leaf]
+    while cuts[-1] < t_root:
+        a = cuts[-1]
+        rate = cosmo.hubble_gyr * np.sqrt(cosmo.omega_matter * (1.0 + cosmo.redshift(a)) ** 3 + cosmo.omega_lambda)
+        cuts.append(min(a + min(0.1 / rate, 1.0), t_root))
+    assert len(cuts) > 8  # the 11 Gyr interval is cut many times
+    y = state0[:, 1:2].copy()
+    step = np.array([-1.0])
+    rate_accretion = (1e12 - 3e11) / (t_root - t_leaf)
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        m = 3e11 + rate_accretion * (a - t_leaf)
+        r, v = cosmo.virial(np.array([m]), cosmo.redshift(np.array([a])))
+        prm = np.array([[m], [rate_accretion], r, v, [0.04]])
+        y, step, status, _ = oracle.evolve_batch(params, table, y, prm, np.array([a]), np.array([b]), step)
+        assert status[0] == 0
+    np.testing.assert_allclose(got, y[:, 0], rtol=1e-7, atol=1e-6)  # numpy vs C++ virial scales: 1e-15 in, ~1e-9 out
+    # Without the limit (one call for the whole interval) the answer moves.
+    q = workloads.isolated_params()
+    q.timestep_relative, q.timestep_absolute = 0.0, 1e6
+    single = oracle.evolve_forest(q, table, f, state0, np.array([]), brent=True)[0][:, 1]
+    assert np.max(np.abs(single - got) / np.maximum(np.abs(got), 1.0)) > 1e-3
