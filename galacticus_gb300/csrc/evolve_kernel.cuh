@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <cstdint>
+#include <type_traits>
 
 #include "../../include/galnode.h"
 #include "galnode_physics.cuh"
@@ -167,6 +168,26 @@ __device__ __forceinline__ int surrogate_net_row(const SurrogateInfo& I, const u
   if (!cooling || !(lt >= I.lo[0] && lt <= I.hi[0])) return -1;
   const int it = min(max((int)((lt - I.mapLoT) * I.mapInvDT), 0), I.mapT - 1);
   return map[I.mapT * I.mapZ + it] ? it * I.mapZ : -1;
+}
+
+// Whether the network may serve the node of this lane at state y: its T
+// row has network cells, it has hot gas, and its metallicity is inside the
+// training domain in a cell the error map leaves to the network (the first
+// tests of surrogate_cooling).  Decided once per attempted step, at the
+// attempt's starting state: a warp none of whose lanes passes takes the
+// step with the table alone, on the unrolled path of the forms without a
+// surrogate.
+template <class NodeT, class Real>
+__device__ __forceinline__ bool surrogate_open(const SurrogateInfo& I, const uint8_t* map, const NodeT& c, const Real* y) {
+  const float massHot = (float)y[GAL_Y_HOT_MASS];
+  if (c.netRow < 0 || !(massHot > 0.0f)) return false;
+  const float metals = (float)y[GAL_Y_HOT_METALS];
+  const float zf = metals > massHot ? 1.0f : (metals <= 0.0f ? 0.0f : __fdividef(metals, massHot));
+  const float zs = zf * (float)(1.0 / k::metallicitySolar);
+  const float lz = zs > 0.0f ? __log10f(zs) : -1.0e30f;
+  if (!(lz >= I.lo[1] && lz <= I.hi[1])) return false;
+  const int iz = min(max((int)((lz - I.mapLoZ) * I.mapInvDZ), 0), I.mapZ - 1);
+  return map[c.netRow + iz] == 0;
 }
 
 // Cooling function (without the n_H^2 factor) and n_e/n_H of one
@@ -352,21 +373,27 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
 
   // One right-hand-side evaluation at xx for the lanes with `active`; with
   // the surrogate, every lane of the warp takes part in the network evaluation.
-  auto eval = [&](const RateT* xx, RateT* d, bool active) {
+  // `net` (std::true_type / std::false_type) selects at compile time
+  // whether this call site may use the network; without it the table is
+  // interpolated as in the forms without a surrogate.
+  auto eval = [&](const RateT* xx, RateT* d, bool active, auto net) {
+    constexpr bool NET = SURR && decltype(net)::value;
     if constexpr (FAST) {
-      if constexpr (SURR) {
+      if constexpr (NET) {
         const CoolingValuesF cv =
             surrogate_cooling(G, SF.tab, SF.lnZ, SF.invDlnZ, N, sd.info, sMap, cf, xx, active, lane, nNet, nTab);
         if (active) rhs_fast(G, SF, cf, xx, d, cv);
       } else {
+        if (SURR && active) ++nTab;
         rhs_fast(G, SF, cf, xx, d);
       }
     } else {
-      if constexpr (SURR) {
+      if constexpr (NET) {
         const CoolingValuesF cv =
             surrogate_cooling(G, S.tab, S.lnZ, S.invDlnZ, N, sd.info, sMap, c, xx, active, lane, nNet, nTab);
         if (active) rhs(G, S, c, xx, d, CoolingValues{cv.use, (double)cv.lambda, (double)cv.electrons});
       } else {
+        if (SURR && active) ++nTab;
         rhs(G, S, c, xx, d);
       }
     }
@@ -810,7 +837,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
         t = t0;
         count = 0;
       }
-      if (any(starting)) eval(yr, k1, starting);  // dydt_in of the first step
+      if (any(starting)) eval(yr, k1, starting, std::false_type{});  // dydt_in of the first step
       if (starting) {
         ++nRhs;
         phase = PH_STEP;
@@ -829,24 +856,24 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
         // Stage arguments: y + h sum_j b_ij k_j (in the rate precision).
 #pragma unroll
         for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + (RateT)ck::b21 * hr * k1[i];
-        eval(x, k2, stepping);
+        eval(x, k2, stepping, std::false_type{});
 #pragma unroll
         for (int i = 0; i < GAL_NY; ++i) x[i] = yr[i] + hr * ((RateT)ck::b31 * k1[i] + (RateT)ck::b32 * k2[i]);
-        eval(x, k3, stepping);
+        eval(x, k3, stepping, std::false_type{});
 #pragma unroll
         for (int i = 0; i < GAL_NY; ++i)
           x[i] = yr[i] + hr * ((RateT)ck::b41 * k1[i] + (RateT)ck::b42 * k2[i] + (RateT)ck::b43 * k3[i]);
-        eval(x, k4, stepping);
+        eval(x, k4, stepping, std::false_type{});
 #pragma unroll
         for (int i = 0; i < GAL_NY; ++i)
           x[i] = yr[i] + hr * ((RateT)ck::b51 * k1[i] + (RateT)ck::b52 * k2[i] + (RateT)ck::b53 * k3[i] +
                                (RateT)ck::b54 * k4[i]);
-        eval(x, k5, stepping);
+        eval(x, k5, stepping, std::false_type{});
 #pragma unroll
         for (int i = 0; i < GAL_NY; ++i)
           x[i] = yr[i] + hr * ((RateT)ck::b61 * k1[i] + (RateT)ck::b62 * k2[i] + (RateT)ck::b63 * k3[i] +
                                (RateT)ck::b64 * k4[i] + (RateT)ck::b65 * k5[i]);
-        eval(x, k6, stepping);
+        eval(x, k6, stepping, std::false_type{});
         if (stepping) {
           nRhs += 5;
           // 5th-order solution, scaled error ratio (sc2_control_hadjust, a_y=1, a_dydt=0), FP64.
@@ -921,7 +948,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       }
       // dydt_out at the accepted point, reused as the next dydt_in; then the
       // post-step clamps (they return GSL_Continue: dydt_out is kept).
-      if (any(needOut)) eval(yr, k1, needOut);
+      if (any(needOut)) eval(yr, k1, needOut, std::false_type{});
       if (needOut) {
         ++nRhs;
         post_step(y);
@@ -975,9 +1002,20 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       double hh = 0.0;
       RateT hr = (RateT)0;
       const bool anyY = any(atY);
+      // With the surrogate: does any lane of the warp start this attempt in
+      // a cell the network may serve?
+      bool warpNet = false;
+      if constexpr (SURR && !FOREST) {
+        bool open = false;
+        if (atY || phase == PH_STEP) {
+          if constexpr (FAST) open = surrogate_open(sd.info, sMap, cf, yr);
+          else open = surrogate_open(sd.info, sMap, c, yr);
+        }
+        warpNet = __any_sync(FULL, open);
+      }
       // One stage: its argument, the evaluation and the slope's slot; false
       // when no lane of the warp steps (the attempt is over).
-      auto stage = [&](const int st) -> bool {
+      auto stage = [&](const int st, auto net) -> bool {
         if (st == 1) {
           // ---- the slopes at y are in: begin one attempted step (a pass of
           // gsl_odeiv2_evolve_apply's try_step) for every lane that steps.
@@ -1035,7 +1073,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
             break;
         }
         RateT d[GAL_NY];
-        eval(x, d, st == 0 ? atY : stepping);
+        eval(x, d, st == 0 ? atY : stepping, net);
         switch (st) {
           case 0:
 #pragma unroll
@@ -1064,18 +1102,25 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
         }
         return true;
       };
-      if constexpr (SURR) {
-        // One right-hand-side call site, for the network's code size.
+      if constexpr (SURR && FOREST) {
+        // Forests keep the one path with the network (a second, unrolled
+        // path for the table made the forest kernel slower: 0.276 -> 0.295 s
+        // on the 4,096-tree forest, 1.52 -> 1.89 s at scale).
 #pragma unroll 1
         for (int st = anyY ? 0 : 1; st <= 5; ++st)
-          if (!stage(st)) break;
+          if (!stage(st, std::true_type{})) break;
+      } else if (SURR && warpNet) {
+        // One right-hand-side call site with the network, for its code size.
+#pragma unroll 1
+        for (int st = anyY ? 0 : 1; st <= 5; ++st)
+          if (!stage(st, std::true_type{})) break;
       } else {
         // Without the network the stages are unrolled: no stage switch, and
         // the compiler schedules across stages.
-        if (anyY) stage(0);
+        if (anyY) stage(0, std::false_type{});
 #pragma unroll
         for (int st = 1; st <= 5; ++st)
-          if (!stage(st)) break;
+          if (!stage(st, std::false_type{})) break;
       }
       if (stepping) {
         nRhs += 5;
