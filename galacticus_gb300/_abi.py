@@ -50,6 +50,7 @@ PHYS_COOLING = 1 << 7
 PHYS_ALL = 0xFF
 
 SF_TIMESCALE_DYNAMICAL, SF_TIMESCALE_FIXED = 0, 1
+SF_RATE_TIMESCALE, SF_RATE_KRUMHOLZ2009 = 0, 1
 OUTFLOW_POWER_LAW, OUTFLOW_FIXED = 0, 1
 
 
@@ -94,6 +95,8 @@ class Params(ctypes.Structure):
         ("bh_efficiency_radiative", ctypes.c_double),
         ("bh_efficiency_jet", ctypes.c_double),
         ("timestep_relative", ctypes.c_double), ("timestep_absolute", ctypes.c_double),
+        ("sf_disk_rate", ctypes.c_int32), ("krumholz_fast", ctypes.c_int32),
+        ("krumholz_frequency", ctypes.c_double), ("krumholz_clumping", ctypes.c_double),
     ]
 
 
@@ -139,6 +142,8 @@ def default_params():
     p.bh_efficiency_radiative = 1.0 - (8.0 / 9.0) ** 0.5
     p.bh_efficiency_jet = 0.0
     p.timestep_relative, p.timestep_absolute = 0.1, 1.0
+    p.sf_disk_rate, p.krumholz_fast = SF_RATE_TIMESCALE, 0
+    p.krumholz_frequency, p.krumholz_clumping = 0.385, 5.0
     return p
 
 

@@ -24,6 +24,8 @@ struct gal_ctx {
   double* dFastExp = nullptr;
   float2* dTabF = nullptr;               // FP32 copies of the tables (FP32-rate forms)
   float* dLnZF = nullptr;
+  double* dKmt = nullptr;                // Krumholz (2009) tables: molecular fraction, then x^0.33
+  float* dKmtF = nullptr;                // their FP32 copies
   unsigned long long* dQueue = nullptr;  // work-queue head
   void* dBuf = nullptr;                  // staging for the host-pointer API
   // Installed cooling-function surrogate (dSurrSmall == nullptr: none).
@@ -54,6 +56,8 @@ size_t ctx_shared_bytes(const gal_ctx* ctx, int mode);
 bool mode_has_threads(int mode, int threads);
 // The launch shape in use for a form.
 void effective_shape(const gal_ctx* ctx, int mode, int& threads, int& blocksPerSm);
+// The device tables of the context.
+DeviceTables ctx_tables(const gal_ctx* ctx);
 
 }  // namespace host
 }  // namespace gal

@@ -5,6 +5,7 @@
 namespace gal {
 
 cudaError_t evolve_launch_forest_fast(int threads, const LaunchArgs& a) {
+  if (krumholz(a)) return threads == 128 ? launch_evolve<128, MODE_FAST, true, false, true>(a) : cudaErrorInvalidConfiguration;
   switch (threads) {
     case 128: return launch_evolve<128, MODE_FAST, true>(a);
     case 256: return launch_evolve<256, MODE_FAST, true>(a);
@@ -14,6 +15,7 @@ cudaError_t evolve_launch_forest_fast(int threads, const LaunchArgs& a) {
 }
 
 cudaError_t evolve_launch_forest_fast_surrogate(int threads, const LaunchArgs& a) {
+  if (krumholz(a)) return cudaErrorInvalidConfiguration;
   switch (threads) {
     case 128: return launch_evolve<128, MODE_FAST_SURROGATE, true>(a);
     case 256: return launch_evolve<256, MODE_FAST_SURROGATE, true>(a);

@@ -9,6 +9,7 @@ cudaError_t evolve_launch_forest_fast(int threads, const LaunchArgs& a);
 cudaError_t evolve_launch_forest_fast_surrogate(int threads, const LaunchArgs& a);
 
 cudaError_t evolve_launch_forest_plain(int threads, const LaunchArgs& a) {
+  if (krumholz(a)) return threads == 128 ? launch_evolve<128, MODE_PLAIN, true, false, true>(a) : cudaErrorInvalidConfiguration;
   switch (threads) {
     case 64: return launch_evolve<64, MODE_PLAIN, true>(a);
     case 128: return launch_evolve<128, MODE_PLAIN, true>(a);

@@ -82,6 +82,8 @@ struct DeviceTables {
   const double* fastExp;  // 2^(j/64) [kExpTableSize]
   const float2* tabF;     // FP32 copy of tab
   const float* lnZF;      // FP32 copy of lnZ (both halves)
+  KmtTables<double> kmt;  // Krumholz (2009) disk tables (global memory)
+  KmtTables<float> kmtF;
 };
 
 // Device copy of an installed cooling-function surrogate.
@@ -271,11 +273,12 @@ __device__ __forceinline__ CoolingValuesF surrogate_cooling(const Globals& G, co
   return cv;
 }
 
-template <int THREADS, int MODE, bool FOREST, bool INTR = false>
+template <int THREADS, int MODE, bool FOREST, bool INTR = false, bool KMT = false>
 __global__ void __launch_bounds__(THREADS, 1)
 evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant__ DeviceTables T,
               const __grid_constant__ SurrogateDev sd, const __grid_constant__ ForestDev F) {
   static_assert(!INTR || (MODE == MODE_PLAIN && !FOREST), "interrupts: batches in the plain form only");
+  static_assert(!KMT || !(MODE & MODE_SURROGATE), "krumholz2009 disks: the forms without a surrogate");
   constexpr bool SURR = (MODE & MODE_SURROGATE) != 0;
   constexpr bool FAST = (MODE & MODE_FAST) != 0;
   using RateT = typename std::conditional<FAST, float, double>::type;
@@ -293,7 +296,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
     float* sLnZ = reinterpret_cast<float*>(sTab + nZ * nT);
     for (int i = threadIdx.x; i < nZ * nT; i += blockDim.x) sTab[i] = T.tabF[i];
     for (int i = threadIdx.x; i < 2 * nZ; i += blockDim.x) sLnZ[i] = T.lnZF[i];
-    SF = SmemF{sTab, sLnZ, sLnZ + nZ};
+    SF = SmemF{sTab, sLnZ, sLnZ + nZ, T.kmtF};
     tail = reinterpret_cast<unsigned char*>(smem) + surrogate_offset(MODE, nT, nZ);
   } else {
     double2* sTab = smem;
@@ -307,7 +310,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
     for (int i = threadIdx.x; i < 2 * nZ; i += blockDim.x) sLnZ[i] = T.lnZ[i];  // ln Z, then the reciprocal spacings
     for (int i = threadIdx.x; i < kLogTableSize; i += blockDim.x) sFastLog[i] = T.fastLog[i];
     for (int i = threadIdx.x; i < kExpTableSize; i += blockDim.x) sFastExp[i] = T.fastExp[i];
-    S = Smem{sTab, sLnZ, sInvDlnZ, FastTables{sFastLog, sFastExp}};
+    S = Smem{sTab, sLnZ, sInvDlnZ, FastTables{sFastLog, sFastExp}, T.kmt};
     sLnT = lnT;
     tail = reinterpret_cast<unsigned char*>(smem) + surrogate_offset(MODE, nT, nZ);
   }
@@ -385,7 +388,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
         if (active) rhs_fast(G, SF, cf, xx, d, cv);
       } else {
         if (SURR && active) ++nTab;
-        rhs_fast(G, SF, cf, xx, d);
+        rhs_fast<KMT>(G, SF, cf, xx, d);
       }
     } else {
       if constexpr (NET) {
@@ -394,7 +397,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
         if (active) rhs(G, S, c, xx, d, CoolingValues{cv.use, (double)cv.lambda, (double)cv.electrons});
       } else {
         if (SURR && active) ++nTab;
-        rhs(G, S, c, xx, d);
+        rhs<KMT>(G, S, c, xx, d);
       }
     }
   };
@@ -1252,15 +1255,18 @@ struct LaunchArgs {
   cudaStream_t stream;
 };
 
-template <int THREADS, int MODE, bool FOREST = false, bool INTR = false>
+template <int THREADS, int MODE, bool FOREST = false, bool INTR = false, bool KMT = false>
 cudaError_t launch_evolve(const LaunchArgs& a) {
-  cudaError_t e = cudaFuncSetAttribute(evolve_kernel<THREADS, MODE, FOREST, INTR>,
+  cudaError_t e = cudaFuncSetAttribute(evolve_kernel<THREADS, MODE, FOREST, INTR, KMT>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a.shm);
   if (e != cudaSuccess) return e;
-  evolve_kernel<THREADS, MODE, FOREST, INTR><<<(unsigned)a.blocks, THREADS, a.shm, a.stream>>>(a.G, a.b, a.tables, a.sd,
-                                                                                               a.forest);
+  evolve_kernel<THREADS, MODE, FOREST, INTR, KMT><<<(unsigned)a.blocks, THREADS, a.shm, a.stream>>>(a.G, a.b, a.tables,
+                                                                                                    a.sd, a.forest);
   return cudaGetLastError();
 }
+
+// The krumholz2009 disk rate is its own instantiation, 128 threads per block.
+inline bool krumholz(const LaunchArgs& a) { return a.G.p.sf_disk_rate == GAL_SF_RATE_KRUMHOLZ2009; }
 
 // Per-form launchers (evolve_plain.cu, evolve_surrogate.cu, evolve_fast.cu,
 // evolve_fast_surrogate.cu); cudaErrorInvalidConfiguration for a block size

@@ -5,6 +5,7 @@
 namespace gal {
 
 cudaError_t evolve_launch_plain(int threads, const LaunchArgs& a) {
+  if (krumholz(a)) return threads == 128 ? launch_evolve<128, MODE_PLAIN, false, false, true>(a) : cudaErrorInvalidConfiguration;
   switch (threads) {
     case 64: return launch_evolve<64, MODE_PLAIN>(a);
     case 128: return launch_evolve<128, MODE_PLAIN>(a);
@@ -14,6 +15,9 @@ cudaError_t evolve_launch_plain(int threads, const LaunchArgs& a) {
   }
 }
 
-cudaError_t evolve_launch_plain_interrupt(const LaunchArgs& a) { return launch_evolve<128, MODE_PLAIN, false, true>(a); }
+cudaError_t evolve_launch_plain_interrupt(const LaunchArgs& a) {
+  if (krumholz(a)) return cudaErrorInvalidConfiguration;
+  return launch_evolve<128, MODE_PLAIN, false, true>(a);
+}
 
 }  // namespace gal

@@ -112,7 +112,7 @@ void release(gal_forest_dev* f) {
 LaunchArgs forest_args(gal_ctx* ctx, gal_forest_dev* f, int mode, int threads, int blocksPerSm) {
   LaunchArgs a{};
   a.G = ctx->globals;
-  a.tables = DeviceTables{ctx->dTab, ctx->dLnT, ctx->dLnZ, ctx->dFastLog, ctx->dFastExp, ctx->dTabF, ctx->dLnZF};
+  a.tables = ctx_tables(ctx);
   if (mode & MODE_SURROGATE)
     a.sd = SurrogateDev{ctx->dSurrSmall, ctx->dSurrPlanes, ctx->dSurrMap, ctx->surrInfo, ctx->dSurrStats};
   ForestDev& F = a.forest;

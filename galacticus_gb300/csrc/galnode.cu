@@ -129,11 +129,19 @@ bool mode_has_threads(int mode, int threads) {
   }
 }
 
+DeviceTables ctx_tables(const gal_ctx* ctx) {
+  return DeviceTables{ctx->dTab,     ctx->dLnT,     ctx->dLnZ,  ctx->dFastLog,
+                      ctx->dFastExp, ctx->dTabF,    ctx->dLnZF,
+                      KmtTables<double>{ctx->dKmt, ctx->dKmt + kmt::kFractionCount},
+                      KmtTables<float>{ctx->dKmtF, ctx->dKmtF + kmt::kFractionCount}};
+}
+
 // The launch shape in use for a form: the requested one, moved to the
 // nearest size the form is built for and to the blocks per SM that fit.
 void effective_shape(const gal_ctx* ctx, int mode, int& threads, int& blocksPerSm) {
   threads = ctx->threads;
   if (!mode_has_threads(mode, threads)) threads = threads < 128 ? 128 : 256;
+  if (ctx->params.sf_disk_rate == GAL_SF_RATE_KRUMHOLZ2009) threads = 128;  // its one instantiation
   const size_t shm = ctx_shared_bytes(ctx, mode);
   blocksPerSm = ctx->blocksPerSm;
   while (blocksPerSm > 1 && (size_t)blocksPerSm * shm > 228 * 1024) --blocksPerSm;
@@ -151,7 +159,7 @@ cudaError_t dispatch(gal_ctx* ctx, const Batch& b, cudaStream_t st) {
   LaunchArgs a{};
   a.G = ctx->globals;
   a.b = b;
-  a.tables = DeviceTables{ctx->dTab, ctx->dLnT, ctx->dLnZ, ctx->dFastLog, ctx->dFastExp, ctx->dTabF, ctx->dLnZF};
+  a.tables = ctx_tables(ctx);
   if (mode & MODE_SURROGATE) a.sd = SurrogateDev{ctx->dSurrSmall, ctx->dSurrPlanes, ctx->dSurrMap, ctx->surrInfo, ctx->dSurrStats};
   a.shm = ctx_shared_bytes(ctx, mode);
   const int64_t warps = (b.n + 31) / 32;
@@ -217,6 +225,10 @@ void gal_params_default(gal_params* p) {
   p->bh_efficiency_jet = 0.0;
   p->timestep_relative = 0.1;
   p->timestep_absolute = 1.0;
+  p->sf_disk_rate = GAL_SF_RATE_TIMESCALE;
+  p->krumholz_fast = 0;
+  p->krumholz_frequency = 0.385;
+  p->krumholz_clumping = 5.0;
 }
 
 int gal_gpu_last_error(const gal_ctx* ctx, char* buf, int len) {
@@ -237,6 +249,8 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
     return fail(nullptr, GAL_ERR_ARGUMENT, "trial_count_maximum must be in 1..30%s");
   if (!(p->timestep_absolute > 0.0) || !(p->timestep_relative == p->timestep_relative))
     return fail(nullptr, GAL_ERR_ARGUMENT, "timestep_absolute must be positive%s");
+  if (p->sf_disk_rate != GAL_SF_RATE_TIMESCALE && p->sf_disk_rate != GAL_SF_RATE_KRUMHOLZ2009)
+    return fail(nullptr, GAL_ERR_ARGUMENT, "sf_disk_rate must be GAL_SF_RATE_TIMESCALE or GAL_SF_RATE_KRUMHOLZ2009%s");
   const int nT = t->n_temperature, nZ = t->n_metallicity;
   if (nT < 2 || nZ < 2 || !t->temperature || !t->metallicity || !t->cooling_rate || !t->electron_density)
     return fail(nullptr, GAL_ERR_TABLE, "CIE table: at least 2x2 entries and all arrays are required%s");
@@ -295,6 +309,16 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
   for (size_t i = 0; i < tab.size(); ++i) tabF[i] = make_float2((float)tab[i].x, (float)tab[i].y);
   for (int j = 0; j < 2 * nZ; ++j) lnZF[j] = (float)lnZ[j];
 
+  // The Krumholz (2009) tables of the reference: the molecular fraction on
+  // 1000 points of s in [0, 10] (Krumholz2009.F90:222-230) and x^0.33 on
+  // [1, 1000] at 100 points per unit (math/exponentiation.F90).
+  std::vector<double> kmtTab(kmt::kFractionCount + kmt::kPowerCount);
+  for (int i = 0; i < kmt::kFractionCount; ++i)
+    kmtTab[i] = kmt_fraction_formula<double>(kmt::kFractionMaximum * i / (kmt::kFractionCount - 1), p->krumholz_fast != 0);
+  for (int i = 0; i < kmt::kPowerCount; ++i)
+    kmtTab[kmt::kFractionCount + i] =
+        std::pow(kmt::kPowerMinimum + (kmt::kPowerMaximum - kmt::kPowerMinimum) * i / (kmt::kPowerCount - 1), 0.33);
+  std::vector<float> kmtTabF(kmtTab.begin(), kmtTab.end());
   auto cleanup = [&](int code) {
     gal_gpu_free(ctx);
     return code;
@@ -307,6 +331,8 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
       cudaMalloc(&ctx->dFastExp, kExpTableSize * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&ctx->dTabF, tab.size() * sizeof(float2)) != cudaSuccess ||
       cudaMalloc(&ctx->dLnZF, 2 * nZ * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&ctx->dKmt, (kmt::kFractionCount + kmt::kPowerCount) * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&ctx->dKmtF, (kmt::kFractionCount + kmt::kPowerCount) * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&ctx->dQueue, sizeof(unsigned long long)) != cudaSuccess) {
     cudaGetLastError();
     fail(nullptr, GAL_ERR_CUDA, "device allocation failed%s");
@@ -318,7 +344,9 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
       cudaMemcpy(ctx->dFastLog, host_fast_log_table(), kLogTableSize * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(ctx->dFastExp, host_fast_exp_table(), kExpTableSize * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(ctx->dTabF, tabF.data(), tabF.size() * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(ctx->dLnZF, lnZF.data(), 2 * nZ * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaMemcpy(ctx->dLnZF, lnZF.data(), 2 * nZ * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->dKmt, kmtTab.data(), kmtTab.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->dKmtF, kmtTabF.data(), kmtTabF.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
     fail(nullptr, GAL_ERR_CUDA, "table upload failed%s");
     return cleanup(GAL_ERR_CUDA);
   }
@@ -336,6 +364,8 @@ void gal_gpu_free(gal_ctx* ctx) {
   cudaFree(ctx->dFastExp);
   cudaFree(ctx->dTabF);
   cudaFree(ctx->dLnZF);
+  cudaFree(ctx->dKmt);
+  cudaFree(ctx->dKmtF);
   cudaFree(ctx->dQueue);
   cudaFree(ctx->dBuf);
   free_surrogate(ctx);
@@ -450,8 +480,9 @@ int gal_gpu_evolve_batch_interrupt_device(gal_ctx* ctx, int64_t n, double* state
   if (!state || !param || !tStart || !tEnd || !step || !components || !status || !tReached || !task)
     return fail(ctx, GAL_ERR_ARGUMENT, "NULL array%s");
   if ((unsigned long long)n * GAL_NY > (1ull << 62)) return fail(ctx, GAL_ERR_TOO_LARGE, "batch too large%s");
-  if (ctx_mode(ctx) != MODE_PLAIN)
-    return fail(ctx, GAL_ERR_ARGUMENT, "interrupts are available in the FP64-rate form without a surrogate%s");
+  if (ctx_mode(ctx) != MODE_PLAIN || ctx->params.sf_disk_rate != GAL_SF_RATE_TIMESCALE)
+    return fail(ctx, GAL_ERR_ARGUMENT,
+                "interrupts are available in the FP64-rate form without a surrogate, with the timescale disk rate%s");
   cudaStream_t st = (cudaStream_t)stream;
   CUDA_TRY(ctx, cudaSetDevice(ctx->device));
   CUDA_TRY(ctx, cudaMemsetAsync(ctx->dQueue, 0, sizeof(unsigned long long), st));
@@ -460,7 +491,7 @@ int gal_gpu_evolve_batch_interrupt_device(gal_ctx* ctx, int64_t n, double* state
   LaunchArgs a{};
   a.G = ctx->globals;
   a.b = Batch{n, state, param, tStart, tEnd, step, status, counters, ctx->dQueue, components, tReached, task};
-  a.tables = DeviceTables{ctx->dTab, ctx->dLnT, ctx->dLnZ, ctx->dFastLog, ctx->dFastExp, ctx->dTabF, ctx->dLnZF};
+  a.tables = ctx_tables(ctx);
   a.shm = ctx_shared_bytes(ctx, MODE_PLAIN);
   const int64_t warps = (n + 31) / 32;
   a.blocks = std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->smCount * blocksPerSm, (warps * 32 + 127) / 128));
@@ -529,6 +560,8 @@ int gal_gpu_set_surrogate(gal_ctx* ctx, const gal_surrogate* sg) {
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   free_surrogate(ctx);
   if (!sg) return GAL_OK;
+  if (ctx->params.sf_disk_rate != GAL_SF_RATE_TIMESCALE)
+    return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_set_surrogate: the surrogate forms use the timescale disk star-formation rate%s");
   if (!sg->params || !sg->use_table || sg->map_t < 1 || sg->map_z < 1 || sg->map_t * sg->map_z > 4096 ||
       !(sg->map_dt > 0.0f) || !(sg->map_dz > 0.0f) || !(sg->y_scale > 0.0f))
     return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_set_surrogate: incomplete surrogate description%s");
@@ -692,6 +725,9 @@ extern "C" int gal_gpu_evolve_batch_noalloc(const gal_params* p, const gal_cie_t
     return fail(nullptr, GAL_ERR_ARGUMENT, "gal_gpu_evolve_batch_noalloc: invalid tolerances or trial count%s");
   if ((unsigned long long)n * GAL_NY > (1ull << 62))
     return fail(nullptr, GAL_ERR_TOO_LARGE, "gal_gpu_evolve_batch_noalloc: batch too large%s");
+  if (p->sf_disk_rate != GAL_SF_RATE_TIMESCALE)
+    return fail(nullptr, GAL_ERR_ARGUMENT,
+                "gal_gpu_evolve_batch_noalloc: only the timescale disk star-formation rate (its tables need memory)%s");
   const int nT = t->n_temperature, nZ = t->n_metallicity;
   if (nT < 2 || nZ < 2 || !t->temperature || !t->metallicity || !t->cooling_rate || !t->electron_density)
     return fail(nullptr, GAL_ERR_TABLE, "gal_gpu_evolve_batch_noalloc: CIE table needs at least 2x2 entries%s");

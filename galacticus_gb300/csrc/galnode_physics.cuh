@@ -13,6 +13,7 @@
 #include <cstdint>
 #include "../../include/galnode.h"
 #include "galnode_fastmath.cuh"
+#include "galnode_krumholz.cuh"
 
 namespace gal {
 
@@ -67,6 +68,7 @@ struct Globals {
   double bhRadiusSpheroidCoef;  // G / c_s^2
   double coolingCoef;         // (dof/2) k_B / ergs / Gyr / densityToHydrogenNumber
   double accretionFraction;   // Omega_b / Omega_m
+  double kmtSTruncation;      // Krumholz (2009) disks: s where the molecular fraction falls to 1e-10
   // FP32 copies for the FP32-rate forms, derived once on the host
   // (fill_fast_constants) so that no rate evaluation converts or divides in FP64.
   struct Fast {
@@ -96,6 +98,7 @@ struct Globals {
     float invTwoPi;
     struct Sf { float fixed, efficiency, exponent, minimum; } sfDisk, sfSph;
     struct Out { float fraction, velocity, exponent, fractionalMinimum; } outDisk, outSph;
+    float kmtFrequency, kmtClumping, kmtSTruncation;  // Krumholz (2009) disks
   } f;
   int tUniform;               // temperature rows evenly spaced in ln T: cell by arithmetic
 };
@@ -143,6 +146,10 @@ inline void fill_fast_constants(Globals& g) {
     return Globals::Fast::Out{(float)o.fraction, (float)o.velocity_characteristic, (float)o.exponent,
                               (float)o.timescale_fractional_minimum};
   };
+  g.kmtSTruncation = kmt_s_truncation(g.p.krumholz_fast != 0);
+  g.f.kmtFrequency = (float)g.p.krumholz_frequency;
+  g.f.kmtClumping = (float)g.p.krumholz_clumping;
+  g.f.kmtSTruncation = (float)g.kmtSTruncation;
   g.f.sfDisk = sf(g.p.sf_disk);
   g.f.sfSph = sf(g.p.sf_spheroid);
   g.f.outDisk = out(g.p.outflow_disk);
@@ -191,6 +198,7 @@ struct Smem {
   const double* lnZ;       // ln Z/Zsun of the rows
   const double* invDlnZ;   // 1/(ln Z[i+1] - ln Z[i])
   FastTables fast;         // tables of the short FP64 log/exp
+  KmtTables<double> kmt;   // Krumholz (2009) tables (global memory)
 };
 
 // Abundances_Mass_To_Mass_Fraction_Packed (objects/abundances.F90:781-809)
@@ -364,6 +372,10 @@ __device__ __forceinline__ double cooling_radius(const Globals& G, const Smem& S
 // Right-hand side of the node ODE system: the node operators of
 // nodeOperatorMulti (nodes/operators/multi.F90:313-332) in the order of
 // parameters/quickTest.xml.  Same logic, branch by branch, as the oracle.
+// KMT: the disk star-formation rate is krumholz2009 (gal_params.sf_disk_rate;
+// a separate kernel instantiation, so that the timescale form carries no
+// call to the integrator).
+template <bool KMT = false>
 __device__ __forceinline__ void rhs(const Globals& G, const Smem& S, const NodeC& c, const double* y, double* dydt,
                                    const CoolingValues& cv = CoolingValues{false, 0.0, 0.0}) {
   const gal_params& p = G.p;
@@ -380,7 +392,15 @@ __device__ __forceinline__ void rhs(const Globals& G, const Smem& S, const NodeC
   // starFormationDisks (star_formation/disks.F90:200-324) + instantaneous populations
   // (stellar_populations/properties/instantaneous.F90:133-219).
   const bool diskOk = !(c.radiusDisk < 0.0 || gasDisk < 0.0);
-  const double sfrDisk = diskOk ? gasDisk * c.sfrDisk : 0.0;
+  double sfrDisk = 0.0;
+  if (diskOk) {
+    if constexpr (KMT)
+      // starFormationRateDisksIntgrtdSurfaceDensity with krumholz2009.
+      sfrDisk = krumholz2009_rate<double>(S.kmt, p.krumholz_frequency, p.krumholz_clumping, G.kmtSTruncation,
+                                          p.krumholz_fast != 0, gasDisk, y[GAL_Y_DISK_GAS_METALS], c.radiusDisk);
+    else
+      sfrDisk = gasDisk * c.sfrDisk;
+  }
   const double zDisk = mass_fraction(y[GAL_Y_DISK_GAS_METALS], gasDisk, gasDisk > 0.0 ? fast_rcp(gasDisk) : 0.0);
   if ((ph & GAL_PHYS_STAR_FORMATION_DISK) && diskOk) {
     const double rateStars = (1.0 - p.recycled_fraction) * sfrDisk;

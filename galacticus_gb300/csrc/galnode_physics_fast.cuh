@@ -159,6 +159,7 @@ struct SmemF {
   const float2* tab;
   const float* lnZ;
   const float* invDlnZ;
+  KmtTables<float> kmt;  // Krumholz (2009) tables (global memory)
 };
 
 struct CoolingValuesF {
@@ -237,6 +238,7 @@ __device__ __forceinline__ float mass_fraction_f(float metals, float mass, float
 
 // rhs() in FP32: the node operators of nodeOperatorMulti
 // (nodes/operators/multi.F90:313-332), branch by branch as in rhs().
+template <bool KMT = false>
 __device__ __forceinline__ void rhs_fast(const Globals& G, const SmemF& S, const NodeF& c, const float* y, float* dydt,
                                         const CoolingValuesF& cv = CoolingValuesF{false, 0.0f, 0.0f}) {
   const gal_params& p = G.p;
@@ -255,7 +257,14 @@ __device__ __forceinline__ void rhs_fast(const Globals& G, const SmemF& S, const
   // starFormationDisks (star_formation/disks.F90:200-324) + instantaneous populations
   // (stellar_populations/properties/instantaneous.F90:133-219).
   const bool diskOk = !(c.radiusDisk < 0.0f || gasDisk < 0.0f);
-  const float sfrDisk = diskOk ? gasDisk * c.sfrDisk : 0.0f;
+  float sfrDisk = 0.0f;
+  if (diskOk) {
+    if constexpr (KMT)
+      sfrDisk = krumholz2009_rate<float>(S.kmt, G.f.kmtFrequency, G.f.kmtClumping, G.f.kmtSTruncation,
+                                         p.krumholz_fast != 0, gasDisk, y[GAL_Y_DISK_GAS_METALS], c.radiusDisk);
+    else
+      sfrDisk = gasDisk * c.sfrDisk;
+  }
   const float zDisk = mass_fraction_f(y[GAL_Y_DISK_GAS_METALS], gasDisk, gasDisk > 0.0f ? __fdividef(1.0f, gasDisk) : 0.0f);
   if ((ph & GAL_PHYS_STAR_FORMATION_DISK) && diskOk) {
     const float rateStars = oneMinusR * sfrDisk;

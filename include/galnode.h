@@ -136,6 +136,14 @@ enum {
   GAL_RATES_FP32 = 1  /* FP32 rates and table: the fast form           */
 };
 
+/* Star-formation rate class of disks (gal_params.sf_disk_rate). */
+enum {
+  GAL_SF_RATE_TIMESCALE = 0,   /* starFormationRateDisksTimescale (P-std)              */
+  GAL_SF_RATE_KRUMHOLZ2009 = 1 /* starFormationRateDisksIntgrtdSurfaceDensity with
+                                  starFormationRateSurfaceDensityDisksKrumholz2009:
+                                  the reference's default                            */
+};
+
 /* Star formation in one component (disk or spheroid).
  * Reference: source/star_formation/timescales/dynamical_time.F90:121-189,
  * source/star_formation/rates/disks/timescale.F90:109-130. */
@@ -200,6 +208,16 @@ typedef struct gal_params {
    * at the call's start (timestep_relative <= 0: the absolute limit alone). */
   double timestep_relative;        /* timeStepRelative (0.1)                 */
   double timestep_absolute;        /* timeStepAbsolute, Gyr (1)              */
+  /* Disk star-formation rate class.  GAL_SF_RATE_KRUMHOLZ2009 integrates the
+   * Krumholz, McKee & Tumlinson (2009) surface density law over the
+   * exponential gas disk (star_formation/rates/disks/
+   * integrated_surface_density.F90:131-190, star_formation/
+   * rate_surface_density/disks/Krumholz2009.F90:312-620); the spheroid keeps
+   * the timescale rate and sf_disk is then unused. */
+  int32_t sf_disk_rate;            /* GAL_SF_RATE_* (P-std: timescale)       */
+  int32_t krumholz_fast;           /* molecularFractionFast (0)              */
+  double krumholz_frequency;       /* frequencyStarFormation, 1/Gyr (0.385)  */
+  double krumholz_clumping;        /* clumpingFactorMolecularComplex (5)     */
 } gal_params;
 
 /* Cooling-function and electron-density tables in the layout of the

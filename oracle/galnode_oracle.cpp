@@ -396,6 +396,209 @@ static R brent(F f, R a, R b, R fa, R fb, double epsabs, double epsrel) {
   return b;
 }
 
+// ---------------------------------------------------------------------------
+// Krumholz, McKee & Tumlinson (2009) star formation in disks: the surface
+// density law of starFormationRateSurfaceDensityDisksKrumholz2009
+// (star_formation/rate_surface_density/disks/Krumholz2009.F90:312-620)
+// integrated over the exponential gas disk by
+// starFormationRateDisksIntgrtdSurfaceDensity (star_formation/rates/disks/
+// integrated_surface_density.F90:131-190) with GSL's adaptive QAG and the
+// 15-point Gauss-Kronrod rule at relative tolerance 1e-3 (absolute 1e-12).
+// The tables are the reference's: the molecular fraction on 1000 points of
+// s in [0, 10] and x^0.33 on [1, 1000] at 100 points per unit
+// (math/exponentiation.F90), both interpolated linearly.
+// ---------------------------------------------------------------------------
+namespace kmt {
+const double sMaximum = 10.0;
+const int sCount = 1000;
+const double fractionTiny = 1.0e-10;
+const double surfaceDensityTransition = 85.0e12;  // Msun/Mpc^2
+
+// krumholz2009MolecularFractionSlow (star_formation/rates/Krumholz2009/utilities.F90:36-63).
+double fraction_slow(double s) {
+  const double deltaInfinity = 0.214008;
+  if (s < 1.0e-6) return 1.0 - 0.75 * s;
+  if (s >= 1.0e10) return 0.0;
+  if (s >= 10.0) return 1.0 / std::pow(0.75 / (1.0 + deltaInfinity), 5.0) / 5.0 / std::pow(s, 5.0);
+  const double delta = 0.0712 / std::pow(0.1 / s + 0.675, 2.8);
+  return 1.0 - 1.0 / std::pow(1.0 + std::pow((1.0 + delta) / 0.75 / s, 5.0), 0.2);
+}
+// krumholz2009MolecularFractionFast (Krumholz2009.F90:462-476).
+double fraction_fast(double s) { return s < 2.0 ? 1.0 - 0.75 * s / (1.0 + 0.25 * s) : 0.0; }
+
+struct Tables {
+  std::vector<double> fraction[2];  // slow, fast on [0, sMaximum]
+  std::vector<double> power;        // x^0.33 on [1, 1000]
+  double sTruncation[2];
+  Tables() {
+    for (int k = 0; k < 2; ++k) {
+      fraction[k].resize(sCount);
+      for (int i = 0; i < sCount; ++i) {
+        const double s = sMaximum * i / (sCount - 1);
+        fraction[k][i] = k ? fraction_fast(s) : fraction_slow(s);
+      }
+    }
+    // The s at which the molecular fraction falls to fractionTiny (found by
+    // a root finder at relative tolerance 1e-6 in the reference; both
+    // fitting functions invert in closed form there).
+    sTruncation[0] = std::pow(1.0 / (fractionTiny * 5.0 * std::pow(0.75 / (1.0 + 0.214008), 5.0)), 0.2);
+    sTruncation[1] = (1.0 - fractionTiny) / (0.5 + 0.25 * fractionTiny);
+    const int n = (int)((1000.0 - 1.0) * 100.0) + 1;
+    power.resize(n);
+    for (int i = 0; i < n; ++i) power[i] = std::pow(1.0 + (1000.0 - 1.0) * i / (n - 1), 0.33);
+  }
+  static double linear(const std::vector<double>& t, double x0, double x1, double x) {
+    const int n = (int)t.size();
+    const double dx = (x1 - x0) / (n - 1);
+    int i = (int)std::floor((x - x0) / dx);
+    i = i < 0 ? 0 : (i > n - 2 ? n - 2 : i);
+    const double h = (x - (x0 + i * dx)) / dx;
+    return t[i] + h * (t[i + 1] - t[i]);
+  }
+  double fraction_of(double s, int fast) const {
+    if (s > sMaximum) return fast ? fraction_fast(s) : fraction_slow(s);
+    return linear(fraction[fast], 0.0, sMaximum, s);
+  }
+  // fastExponentiator%exponentiate (math/exponentiation.F90): table inside [1, 1000].
+  double power033(double x) const { return (x < 1.0 || x > 1000.0) ? std::pow(x, 0.33) : linear(power, 1.0, 1000.0, x); }
+};
+const Tables& tables() {
+  static const Tables t;
+  return t;
+}
+
+// gsl_integration_qk15: the 15-point Kronrod rule with its 7-point Gauss
+// rule and QUADPACK's error estimate (Piessens et al. 1983).
+template <class F>
+double qk15(F& f, double a, double b, double& abserr) {
+  static const double xgk[8] = {0.991455371120812639206854697526329, 0.949107912342758524526189684047851,
+                                0.864864423359769072789712788640926, 0.741531185599394439863864773280788,
+                                0.586087235467691130294144845693013, 0.405845151377397166906606412076961,
+                                0.207784955007898467600689403773245, 0.0};
+  static const double wg[4] = {0.129484966168869693270611432679082, 0.279705391489276667901467771423780,
+                               0.381830050505118944950369775488975, 0.417959183673469387755102040816327};
+  static const double wgk[8] = {0.022935322010529224963732008058970, 0.063092092629978553290700663189204,
+                                0.104790010322250183839876322541518, 0.140653259715525918745189590510238,
+                                0.169004726639267902826583426598550, 0.190350578064785409913256402421014,
+                                0.204432940075298892414161999234649, 0.209482141084727828012999174891714};
+  const double c = 0.5 * (a + b), h = 0.5 * (b - a);
+  const double fc = f(c);
+  double rg = fc * wg[3], rk = fc * wgk[7], rabs = std::fabs(rk);
+  double fv1[7], fv2[7];
+  for (int j = 0; j < 3; ++j) {
+    const int jt = 2 * j + 1;
+    const double dx = h * xgk[jt];
+    const double f1 = f(c - dx), f2 = f(c + dx);
+    fv1[jt] = f1;
+    fv2[jt] = f2;
+    rg += wg[j] * (f1 + f2);
+    rk += wgk[jt] * (f1 + f2);
+    rabs += wgk[jt] * (std::fabs(f1) + std::fabs(f2));
+  }
+  for (int j = 0; j < 4; ++j) {
+    const int jt = 2 * j;
+    const double dx = h * xgk[jt];
+    const double f1 = f(c - dx), f2 = f(c + dx);
+    fv1[jt] = f1;
+    fv2[jt] = f2;
+    rk += wgk[jt] * (f1 + f2);
+    rabs += wgk[jt] * (std::fabs(f1) + std::fabs(f2));
+  }
+  const double mean = 0.5 * rk;
+  double rasc = wgk[7] * std::fabs(fc - mean);
+  for (int j = 0; j < 7; ++j) rasc += wgk[j] * (std::fabs(fv1[j] - mean) + std::fabs(fv2[j] - mean));
+  const double result = rk * h;
+  rabs *= std::fabs(h);
+  rasc *= std::fabs(h);
+  double err = std::fabs((rk - rg) * h);
+  if (rasc != 0.0 && err != 0.0) {
+    const double scale = std::pow(200.0 * err / rasc, 1.5);
+    err = scale < 1.0 ? rasc * scale : rasc;
+  }
+  if (rabs > DBL_MIN / (50.0 * DBL_EPSILON)) err = std::max(err, 50.0 * DBL_EPSILON * rabs);
+  abserr = err;
+  return result;
+}
+
+// gsl_integration_qag's global adaptive bisection: split the interval with
+// the largest error until the summed error meets max(epsabs, epsrel |I|).
+template <class F>
+double qag(F& f, double a, double b, double epsabs, double epsrel) {
+  struct Piece { double a, b, r, e; };
+  std::vector<Piece> pieces;
+  double e0;
+  const double r0 = qk15(f, a, b, e0);
+  pieces.push_back({a, b, r0, e0});
+  for (int it = 0; it < 1000; ++it) {
+    double total = 0.0, error = 0.0;
+    size_t worst = 0;
+    for (size_t k = 0; k < pieces.size(); ++k) {
+      total += pieces[k].r;
+      error += pieces[k].e;
+      if (pieces[k].e > pieces[worst].e) worst = k;
+    }
+    if (error <= std::max(epsabs, epsrel * std::fabs(total))) return total;
+    const Piece p = pieces[worst];
+    const double m = 0.5 * (p.a + p.b);
+    double e1, e2;
+    const double r1 = qk15(f, p.a, m, e1), r2 = qk15(f, m, p.b, e2);
+    pieces[worst] = {p.a, m, r1, e1};
+    pieces.push_back({m, p.b, r2, e2});
+  }
+  double total = 0.0;
+  for (const Piece& p : pieces) total += p.r;
+  return total;
+}
+
+// The disk's star formation rate (Msun/Gyr): 2 pi int r Sigma_SFR(r) dr over
+// [0, 10 R_d], truncated where the molecular fraction falls below 1e-10 and
+// split at the radius where X_H Sigma equals the transition surface density.
+double star_formation_rate(const gal_params& p, double massGas, double metalsGas, double radiusDisk) {
+  if (!(massGas > 0.0) || !(radiusDisk > 0.0)) return 0.0;
+  const Tables& T = tables();
+  // Abundances of the fuel (objects/abundances.F90:781-868).
+  const double Z = metalsGas > massGas ? 1.0 : (metalsGas <= 0.0 ? 0.0 : metalsGas / massGas);
+  const double zs = Z / k::metallicitySolar;
+  const double xH = std::min(std::max(zs * (k::hydrogenByMassSolar - k::hydrogenByMassPrimordial) + k::hydrogenByMassPrimordial, 0.7),
+                             k::hydrogenByMassPrimordial);
+  if (!(zs > 0.0)) return 0.0;
+  // krumholz2009ComputeFactors (Krumholz2009.F90:312-358).
+  const double chi = 0.77 * (1.0 + 3.1 * std::pow(zs, 0.365));
+  const double sigmaNorm = xH * p.krumholz_clumping / 1.0e12;
+  if (!(sigmaNorm > 0.0)) return 0.0;
+  const double sNorm = std::log(1.0 + 0.6 * chi + 0.01 * chi * chi) / (0.04 * zs);
+  const int fast = p.krumholz_fast ? 1 : 0;
+  const double truncation = sNorm / sigmaNorm / T.sTruncation[fast];
+  // The exponential gas disk (mass_distributions/cylindrical/exponential_disk.F90).
+  const double sigma0 = massGas / (2.0 * k::Pi * radiusDisk * radiusDisk);
+  auto sigma_at = [&](double r) { return sigma0 * std::exp(-r / radiusDisk); };
+  // krumholz2009Rate (Krumholz2009.F90:360-414).
+  auto rate = [&](double r) {
+    const double sg = sigma_at(r);
+    if (sg <= 1.0e-100) return 0.0;
+    const double s = sNorm / (sigmaNorm * sg);
+    const double fraction = T.fraction_of(s, fast);
+    const double sd = xH * sg / surfaceDensityTransition;
+    const double factor = sd <= 0.0 ? 0.0 : (sd < 1.0 ? T.power033(1.0 / sd) : T.power033(sd));
+    return p.krumholz_frequency * sg * factor * fraction;
+  };
+  auto integrand = [&](double r) { return r * rate(r); };
+  // krumholz2009Intervals (Krumholz2009.F90:478-587) for the monotonic disk.
+  const double rIn = 0.0, rOut = 10.0 * radiusDisk;
+  if (sigma_at(rIn) <= truncation) return 0.0;
+  const double rMax = sigma_at(rOut) <= truncation ? radiusDisk * std::log(sigma0 / truncation) : rOut;
+  const double sdIn = xH * sigma_at(rIn) / surfaceDensityTransition, sdMax = xH * sigma_at(rMax) / surfaceDensityTransition;
+  double integral;
+  if (sdIn <= 1.0 || sdMax >= 1.0) {
+    integral = qag(integrand, rIn, rMax, 1.0e-12, 1.0e-3);
+  } else {
+    const double rCrit = radiusDisk * std::log(xH * sigma0 / surfaceDensityTransition);
+    integral = qag(integrand, rIn, rCrit, 1.0e-12, 1.0e-3) + qag(integrand, rCrit, rMax, 1.0e-12, 1.0e-3);
+  }
+  return 2.0 * k::Pi * integral;
+}
+}  // namespace kmt
+
 // Right-hand side of the node ODE system for the P-std profile: the sum of
 // the node operators of nodeOperatorMulti (nodes/operators/multi.F90:313-332)
 // in the order of parameters/quickTest.xml.  `dydt` is overwritten.
@@ -473,8 +676,13 @@ struct Rhs {
     const R gasDisk = y[GAL_Y_DISK_GAS];
     const bool diskOk = !(n.radiusDisk < 0.0 || gasDisk < R(0.0));
     if (diskOk) {
-      R ts = sf_timescale(p.sf_disk, n.radiusDisk, n.velocityDisk);
-      sfrDisk = ts > R(0.0) ? gasDisk / ts : R(0.0);  // timescaleRate (rates/disks/timescale.F90:109-130)
+      if (p.sf_disk_rate == GAL_SF_RATE_KRUMHOLZ2009) {
+        // intgrtdSurfaceDensityRate with krumholz2009 (evaluated in FP64; not counted by the counting scalar).
+        sfrDisk = R(kmt::star_formation_rate(p, val(gasDisk), val(y[GAL_Y_DISK_GAS_METALS]), n.radiusDisk));
+      } else {
+        R ts = sf_timescale(p.sf_disk, n.radiusDisk, n.velocityDisk);
+        sfrDisk = ts > R(0.0) ? gasDisk / ts : R(0.0);  // timescaleRate (rates/disks/timescale.F90:109-130)
+      }
     }
     if ((ph & GAL_PHYS_STAR_FORMATION_DISK) && diskOk) {
       // stellarPopulationPropertiesInstantaneous%rates (stellar_populations/properties/instantaneous.F90:133-219)
