@@ -97,6 +97,7 @@ class Params(ctypes.Structure):
         ("timestep_relative", ctypes.c_double), ("timestep_absolute", ctypes.c_double),
         ("sf_disk_rate", ctypes.c_int32), ("krumholz_fast", ctypes.c_int32),
         ("krumholz_frequency", ctypes.c_double), ("krumholz_clumping", ctypes.c_double),
+        ("merger_mass_ratio_major", ctypes.c_double),
     ]
 
 
@@ -144,6 +145,7 @@ def default_params():
     p.timestep_relative, p.timestep_absolute = 0.1, 1.0
     p.sf_disk_rate, p.krumholz_fast = SF_RATE_TIMESCALE, 0
     p.krumholz_frequency, p.krumholz_clumping = 0.385, 5.0
+    p.merger_mass_ratio_major = 0.25
     return p
 
 

@@ -456,8 +456,9 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
   };
   // (forest) Finish the node with state y and status st; while this lane is
   // the last progenitor of the parent to finish, merge the progenitors into
-  // the parent (the primary's state plus the others', component by
-  // component in index order) and go on with the parent.
+  // the parent (the primary's state, then each other progenitor in index
+  // order merged into it as a satellite, merge_satellite) and go on with
+  // the parent.
   auto complete_node = [&](int st) {
     for (;;) {
       // The parent's fields are read-only during the evolution: read them
@@ -493,8 +494,10 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
 #pragma unroll
       for (int v = 0; v < GAL_NY; ++v) y[v] = F.state[v * F.n + c0];
       for (int32_t j = 1; j < cn; ++j) {
+        double sat[GAL_NY];
 #pragma unroll
-        for (int v = 0; v < GAL_NY; ++v) y[v] += F.state[v * F.n + c0 + j];
+        for (int v = 0; v < GAL_NY; ++v) sat[v] = F.state[v * F.n + c0 + j];
+        merge_satellite(y, sat, G.p.merger_mass_ratio_major);
       }
       stepIn = F.stepOut[c0];
       node = par;

@@ -229,6 +229,7 @@ void gal_params_default(gal_params* p) {
   p->krumholz_fast = 0;
   p->krumholz_frequency = 0.385;
   p->krumholz_clumping = 5.0;
+  p->merger_mass_ratio_major = 0.25;
 }
 
 int gal_gpu_last_error(const gal_ctx* ctx, char* buf, int len) {

@@ -550,6 +550,36 @@ __device__ __forceinline__ void rhs(const Globals& G, const Smem& S, const NodeC
   }
 }
 
+// A secondary progenitor (the satellite) merging into the primary (the host)
+// at their parent's time, with the mass movements of
+// mergerMassMovementsSimple (satellites/merging/mass_movements/simple.F90,
+// defaults: gas and stars of a minor merger's satellite to the host's
+// spheroid, the host unmoved; a major merger -- the smaller galaxy at least
+// ratioMajor of the larger in disk plus spheroid mass -- puts both galaxies
+// into the spheroid).  The hot halo, its outflowed reservoir and the black
+// hole add to the host's.  Stellar metals of a disk moving to the spheroid
+// leave the state, which holds no spheroid stellar metals.
+__host__ __device__ inline void merge_satellite(double* host, const double* sat, double ratioMajor) {
+  const double massHost = host[GAL_Y_DISK_GAS] + host[GAL_Y_DISK_STARS] + host[GAL_Y_SPHEROID_GAS] + host[GAL_Y_SPHEROID_STARS];
+  const double massSat = sat[GAL_Y_DISK_GAS] + sat[GAL_Y_DISK_STARS] + sat[GAL_Y_SPHEROID_GAS] + sat[GAL_Y_SPHEROID_STARS];
+  const double smaller = massSat < massHost ? massSat : massHost, larger = massSat < massHost ? massHost : massSat;
+  const bool major = massSat > 0.0 && massHost > 0.0 && smaller >= ratioMajor * larger;
+  host[GAL_Y_HOT_MASS] += sat[GAL_Y_HOT_MASS];
+  host[GAL_Y_HOT_METALS] += sat[GAL_Y_HOT_METALS];
+  host[GAL_Y_OUTFLOWED_MASS] += sat[GAL_Y_OUTFLOWED_MASS];
+  host[GAL_Y_OUTFLOWED_METALS] += sat[GAL_Y_OUTFLOWED_METALS];
+  host[GAL_Y_BLACK_HOLE] += sat[GAL_Y_BLACK_HOLE];
+  host[GAL_Y_SPHEROID_GAS] += sat[GAL_Y_DISK_GAS] + sat[GAL_Y_SPHEROID_GAS];
+  host[GAL_Y_SPHEROID_GAS_METALS] += sat[GAL_Y_DISK_GAS_METALS] + sat[GAL_Y_SPHEROID_GAS_METALS];
+  host[GAL_Y_SPHEROID_STARS] += sat[GAL_Y_DISK_STARS] + sat[GAL_Y_SPHEROID_STARS];
+  if (major) {
+    host[GAL_Y_SPHEROID_GAS] += host[GAL_Y_DISK_GAS];
+    host[GAL_Y_SPHEROID_GAS_METALS] += host[GAL_Y_DISK_GAS_METALS];
+    host[GAL_Y_SPHEROID_STARS] += host[GAL_Y_DISK_STARS];
+    host[GAL_Y_DISK_GAS] = host[GAL_Y_DISK_GAS_METALS] = host[GAL_Y_DISK_STARS] = host[GAL_Y_DISK_STARS_METALS] = 0.0;
+  }
+}
+
 // The components to create for one evaluation of an interrupt-form
 // integration: those missing from `components` (GAL_COMPONENT_*) that
 // receive a non-zero rate in one of their properties (a null component's

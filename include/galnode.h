@@ -218,6 +218,12 @@ typedef struct gal_params {
   int32_t krumholz_fast;           /* molecularFractionFast (0)              */
   double krumholz_frequency;       /* frequencyStarFormation, 1/Gyr (0.385)  */
   double krumholz_clumping;        /* clumpingFactorMolecularComplex (5)     */
+  /* Forests: a secondary progenitor merges into the primary at the parent's
+   * time with the mass movements of mergerMassMovementsSimple
+   * (satellites/merging/mass_movements/simple.F90): a merger is major when
+   * the smaller galaxy has at least this fraction of the larger one's
+   * disk-plus-spheroid mass. */
+  double merger_mass_ratio_major;  /* massRatioMajorMerger (0.25)            */
 } gal_params;
 
 /* Cooling-function and electron-density tables in the layout of the

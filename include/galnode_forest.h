@@ -24,8 +24,12 @@
  *   spin[n]         spin parameter
  * A node evolves from time[i] to time[parent[i]].  On reaching it, the
  * primary progenitor's state becomes the parent's initial state and the
- * other progenitors' states are added to it component by component, in
- * index order.  A primary progenitor's halo mass grows linearly to its
+ * other progenitors merge into it in index order as satellites, with the
+ * mass movements of mergerMassMovementsSimple (satellites/merging/
+ * mass_movements/simple.F90; gal_params.merger_mass_ratio_major): minor
+ * mergers put the satellite's gas and stars into the host's spheroid, major
+ * ones both galaxies; hot gas, outflowed gas and black holes add up (the
+ * satellite's orbit until it merges is not modelled).  A primary progenitor's halo mass grows linearly to its
  * parent's over the interval; its hot halo accretes (Omega_b/Omega_m) times
  * the parent's mass not brought in by its progenitors.  The interval is cut
  * into evolve calls at every output time inside it and wherever a call would

@@ -1368,8 +1368,8 @@ static int evolve_node_interruptible(const gal_params& p, const Table& tb, const
 // parent's, in pieces cut at the output times and at the timestep limit of
 // mergerTreeEvolveTimestepSimple (each piece one evolve call,
 // the step size carried over as node%timeStep), and on reaching the parent
-// the primary progenitor's state is promoted and the other progenitors'
-// states are added to it, component by component in index order.
+// the primary progenitor's state is promoted and the other progenitors
+// merge into it in index order (merge_satellite).
 // ---------------------------------------------------------------------------
 struct Cosmology {
   double om, ol, h0;
@@ -1409,6 +1409,36 @@ struct ForestIn {
   int32_t nOut;
   const double* tOut;
 };
+
+// A secondary progenitor merging into the primary at their parent's time:
+// mergerMassMovementsSimple%get (satellites/merging/mass_movements/simple.F90,
+// defaults massRatioMajorMerger = 0.25, destinationGasMinorMerger =
+// destinationStarsMinorMerger = spheroid): in a major merger (the smaller
+// galaxy, disk plus spheroid, at least the ratio times the larger) both
+// galaxies go to the remnant's spheroid, in a minor one the satellite's
+// gas and stars go to the host's spheroid and the host is unmoved.  The
+// satellite's hot halo and outflowed gas join the host's, and the black
+// holes merge (masses add).  The state holds no spheroid stellar metals, so
+// a disk's stellar metals leave it when its stars move to the spheroid.
+// `sat` is the satellite's column of an [NY][n] array.
+static void merge_satellite(const gal_params& p, double* y, const double* sat, int64_t n) {
+  double s[GAL_NY];
+  for (int v = 0; v < GAL_NY; ++v) s[v] = sat[v * n];
+  const double massHost = y[GAL_Y_DISK_GAS] + y[GAL_Y_DISK_STARS] + y[GAL_Y_SPHEROID_GAS] + y[GAL_Y_SPHEROID_STARS];
+  const double massSat = s[GAL_Y_DISK_GAS] + s[GAL_Y_DISK_STARS] + s[GAL_Y_SPHEROID_GAS] + s[GAL_Y_SPHEROID_STARS];
+  const bool major = massSat > 0.0 && massHost > 0.0 &&
+                     std::min(massSat, massHost) >= p.merger_mass_ratio_major * std::max(massSat, massHost);
+  for (int v : {GAL_Y_HOT_MASS, GAL_Y_HOT_METALS, GAL_Y_OUTFLOWED_MASS, GAL_Y_OUTFLOWED_METALS, GAL_Y_BLACK_HOLE}) y[v] += s[v];
+  y[GAL_Y_SPHEROID_GAS] += s[GAL_Y_DISK_GAS] + s[GAL_Y_SPHEROID_GAS];
+  y[GAL_Y_SPHEROID_GAS_METALS] += s[GAL_Y_DISK_GAS_METALS] + s[GAL_Y_SPHEROID_GAS_METALS];
+  y[GAL_Y_SPHEROID_STARS] += s[GAL_Y_DISK_STARS] + s[GAL_Y_SPHEROID_STARS];
+  if (major) {
+    y[GAL_Y_SPHEROID_GAS] += y[GAL_Y_DISK_GAS];
+    y[GAL_Y_SPHEROID_GAS_METALS] += y[GAL_Y_DISK_GAS_METALS];
+    y[GAL_Y_SPHEROID_STARS] += y[GAL_Y_DISK_STARS];
+    y[GAL_Y_DISK_GAS] = y[GAL_Y_DISK_GAS_METALS] = y[GAL_Y_DISK_STARS] = y[GAL_Y_DISK_STARS_METALS] = 0.0;
+  }
+}
 
 // Evolve one node of a forest whose progenitors are done; y holds its
 // initial state, stepIo the carried step size.
@@ -1670,8 +1700,7 @@ int oracle_evolve_forest(const gal_params* p, const gal_cie_table* table, int64_
       } else {
         const int64_t c0 = childFirst[i];
         for (int v = 0; v < GAL_NY; ++v) y[v] = state[v * n + c0];
-        for (int32_t c = 1; c < childCount[i]; ++c)
-          for (int v = 0; v < GAL_NY; ++v) y[v] += state[v * n + c0 + c];
+        for (int32_t c = 1; c < childCount[i]; ++c) orc::merge_satellite(*p, y, &state[c0 + c], n);
         h = stepOf[(size_t)c0];
       }
       uint32_t cnt[3];

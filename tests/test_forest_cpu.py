@@ -126,8 +126,9 @@ def test_oracle_forest_conserves_baryons(small_forest, params, table, oracle_mod
     fb = params.omega_baryon / params.omega_matter
     rel = np.abs(baryons / (fb * f.mass[roots]) - 1.0)
     assert rel.max() < 1e-3, rel.max()
-    # Stars formed, and every node took steps.
-    assert np.all(state[_abi.Y_DISK_STARS][roots] > 0)
+    # Stars formed, mergers built spheroids, and every node took steps.
+    assert np.all(state[_abi.Y_DISK_STARS][roots] + state[_abi.Y_SPHEROID_STARS][roots] > 0)
+    assert np.mean(state[_abi.Y_SPHEROID_STARS][roots] > 0) > 0.5
     assert counters[0][f.child_count == 0].min() > 0
     # One snapshot per (node, output inside or at the start of its interval).
     first, m = oracle_mod.forest_snapshots(f, times)
@@ -184,3 +185,51 @@ def test_timestep_criterion_cuts_evolve_calls(params):
     q.timestep_relative, q.timestep_absolute = 0.0, 1e6
     single = oracle.evolve_forest(q, table, f, state0, np.array([]), brent=True)[0][:, 1]
     assert np.max(np.abs(single - got) / np.maximum(np.abs(got), 1.0)) > 1e-3
+
+
+def merger_forest():
+    """A root and two progenitors, 1 Gyr earlier."""
+    return forest.Forest(np.array([0, 0, 0], np.int32), np.array([-1, 0, 0], np.int32), np.array([1, 0, 0], np.int32),
+                         np.array([2, 0, 0], np.int32), np.array([13.0, 12.0, 12.0]), np.array([1e12, 6e11, 2e11]),
+                         np.full(3, 0.04))
+
+
+def merger_states(satellite_galaxy):
+    """Progenitor states: a host with a disk and a small spheroid, and a
+    satellite whose disk-plus-spheroid mass is `satellite_galaxy`."""
+    s = np.zeros((_abi.NY, 3))
+    s[:, 1] = [5e10, 1e8, 2e9, 1e7, 1e10, 2e8, 2e10, 3e8, 1e8, 1e6, 1e9, 1e6]
+    s[:, 2] = [1e10, 5e7, 1e9, 1e7, 0.8 * satellite_galaxy, 1e7, 0.2 * satellite_galaxy, 2e7, 0.0, 0.0, 0.0, 2e5]
+    return s
+
+
+@pytest.mark.parametrize("satellite_galaxy,major", [(5e9, False), (1e10, True)])
+def test_progenitors_merge_with_the_reference_mass_movements(params, table, oracle_mod, satellite_galaxy, major):
+    """mergerMassMovementsSimple (satellites/merging/mass_movements/
+    simple.F90): the host galaxy here is 3.11e10 Msun, so a satellite of
+    5e9 Msun (ratio 0.16) merges as a minor merger -- its gas and stars to
+    the host's spheroid, the host's disk unmoved -- and one of 1e10 Msun
+    (0.32 >= 0.25) as a major merger, both galaxies into the spheroid.  With
+    every operator off, the root's state is the merger's result exactly."""
+    q = workloads.isolated_params()
+    q.physics = 0
+    f = merger_forest()
+    s = merger_states(satellite_galaxy)
+    state = oracle_mod.evolve_forest(q, table, f, s, np.array([]))[0]
+    host, sat, root = s[:, 1], s[:, 2], state[:, 0]
+    for v in (_abi.Y_HOT_MASS, _abi.Y_HOT_METALS, _abi.Y_OUTFLOWED_MASS, _abi.Y_OUTFLOWED_METALS, _abi.Y_BLACK_HOLE):
+        assert root[v] == host[v] + sat[v]
+    gas_sph = host[_abi.Y_SPHEROID_GAS] + (sat[_abi.Y_DISK_GAS] + sat[_abi.Y_SPHEROID_GAS])
+    stars_sph = host[_abi.Y_SPHEROID_STARS] + (sat[_abi.Y_DISK_STARS] + sat[_abi.Y_SPHEROID_STARS])
+    if major:
+        assert root[_abi.Y_SPHEROID_GAS] == gas_sph + host[_abi.Y_DISK_GAS]
+        assert root[_abi.Y_SPHEROID_STARS] == stars_sph + host[_abi.Y_DISK_STARS]
+        assert np.all(root[[_abi.Y_DISK_GAS, _abi.Y_DISK_GAS_METALS, _abi.Y_DISK_STARS, _abi.Y_DISK_STARS_METALS]] == 0.0)
+    else:
+        assert root[_abi.Y_SPHEROID_GAS] == gas_sph and root[_abi.Y_SPHEROID_STARS] == stars_sph
+        np.testing.assert_array_equal(root[_abi.Y_DISK_GAS:_abi.Y_DISK_STARS_METALS + 1],
+                                      host[_abi.Y_DISK_GAS:_abi.Y_DISK_STARS_METALS + 1])
+    # Gas, stars and black holes are conserved.
+    masses = [_abi.Y_HOT_MASS, _abi.Y_OUTFLOWED_MASS, _abi.Y_DISK_GAS, _abi.Y_DISK_STARS, _abi.Y_SPHEROID_GAS,
+              _abi.Y_SPHEROID_STARS, _abi.Y_BLACK_HOLE]
+    assert root[masses].sum() == pytest.approx(host[masses].sum() + sat[masses].sum(), rel=1e-15)

@@ -210,3 +210,25 @@ def test_forest_needs_a_built_form(params, table, trained):
     assert np.all(fe.results(snapshots=False)[1] == 0)
     fe.close()
     ev.close()
+
+
+@pytest.mark.parametrize("rates", ["fp64", "fp32"])
+@pytest.mark.parametrize("satellite_galaxy", [5e9, 1e10])
+def test_progenitors_merge_as_in_the_oracle(table, oracle_mod, rates, satellite_galaxy):
+    """The GPU's merger of two progenitors (mergerMassMovementsSimple, a minor
+    and a major case) equals the oracle's bit for bit with every operator
+    off: the merge is the same sequence of FP64 additions."""
+    import test_forest_cpu as cpu
+    q = workloads.isolated_params()
+    q.physics = 0
+    f = cpu.merger_forest()
+    s = cpu.merger_states(satellite_galaxy)
+    ev = _evolver(q, table, rates)
+    fe = forest.ForestEvolver(ev, f, s, np.array([]))
+    fe.evolve()
+    state, status = fe.results(snapshots=False)[:2]
+    fe.close()
+    ev.close()
+    ref = oracle_mod.evolve_forest(q, table, f, s, np.array([]))[0]
+    assert np.all(status == 0)
+    np.testing.assert_array_equal(state[:, 0], ref[:, 0])
