@@ -709,6 +709,12 @@ def run_ours(args):
     headline = timed(forms["surrogate"], clocks=True)
     s1 = surrogate.stats(forms["surrogate"]) if chosen is not None else (0, 0)
     network_share = (s1[0] - s0[0]) / max(1, (s1[0] - s0[0]) + (s1[1] - s0[1]))
+    # The same form in one network kernel over all nodes (no split launch).
+    one_kernel = None
+    if chosen is not None:
+        surrogate.set_split(forms["surrogate"], False)
+        one_kernel = timed(forms["surrogate"], passes=20)["value"]
+        surrogate.set_split(forms["surrogate"], True)
     others = {name: timed(forms[name]) for name in ("plain", "fast")}
     if rank == 0:
         for name in ("plain", "fast"):
@@ -785,7 +791,10 @@ def run_ours(args):
             "forms": {
                 "surrogate": {"value": headline["value"], "ms_per_step": headline["ms_per_step"], "gate_dex": chosen,
                               "table_cells": bar["table_cells"], "network_share": network_share,
-                              "mass_error": err, "bar": bar},
+                              "mass_error": err, "bar": bar,
+                              "launch": "split: nodes the network may serve on the network kernel, the others on the "
+                                        "FP32-rate kernel without it, at once on two streams",
+                              "one_kernel_value": one_kernel},
                 "plain": {k: others["plain"][k] for k in ("value", "ms_per_step", "mass_error", "bar")},
                 "fast_no_network": {k: others["fast"][k] for k in ("value", "ms_per_step", "mass_error", "bar")},
             },

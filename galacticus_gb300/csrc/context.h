@@ -27,6 +27,15 @@ struct gal_ctx {
   double* dKmt = nullptr;                // Krumholz (2009) tables: molecular fraction, then x^0.33
   float* dKmtF = nullptr;                // their FP32 copies
   unsigned long long* dQueue = nullptr;  // work-queue head
+  // The surrogate forms' split launch: the two work lists [2][orderCap],
+  // their lengths and queue heads (4 counters), a second stream, fork and
+  // join events.
+  int32_t* dOrder = nullptr;
+  unsigned long long* dOrderCount = nullptr;
+  int64_t orderCap = 0;
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t evFork = nullptr, evJoin = nullptr;
+  int splitSurrogate = 1;
   void* dBuf = nullptr;                  // staging for the host-pointer API
   // Installed cooling-function surrogate (dSurrSmall == nullptr: none).
   float* dSurrSmall = nullptr;

@@ -70,6 +70,10 @@ struct Batch {
   const int32_t* components;
   double* tReached;
   int32_t* task;
+  // Optional work list (the surrogate forms' split launch): when set, the
+  // queue walks order[0 .. *orderCount) instead of 0 .. n.
+  const int32_t* order;
+  const unsigned long long* orderCount;
 };
 
 // Device tables: the FP64 forms read gTab/gLnT/gLnZ/gFastLog/gFastExp, the
@@ -334,6 +338,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
   if constexpr (SURR) N = surrogate_view(sSmall, sPlanes);
 
   const int64_t n = b.n;
+  const int64_t nWork = (!FOREST && b.order) ? (int64_t)*b.orderCount : n;
   const double epsAbs = G.p.ode_tolerance_absolute, epsRel = G.p.ode_tolerance_relative;
   const float epsAbsF = (float)epsAbs, epsRelF = (float)epsRel;
   const uint32_t budget = (uint32_t)max(G.p.step_budget, 0);
@@ -537,11 +542,11 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       if (seg < segEnd) start_segment();
       else complete_node(GAL_STATUS_SUCCESS);
     } else {
-      node = (int64_t)idx;
-      if (node >= n) {
+      if ((int64_t)idx >= nWork) {
         phase = PH_DONE;
         return;
       }
+      node = b.order ? (int64_t)b.order[idx] : (int64_t)idx;
       double prm[GAL_NP];
 #pragma unroll
       for (int v = 0; v < GAL_NP; ++v) prm[v] = b.param[v * n + node];
@@ -613,6 +618,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
         b.counters[n + node] = nRej;
         b.counters[2 * n + node] = nRhs;
       }
+      if constexpr (!SURR) nTab += nRhs;  // table evaluations, for the split launch's statistics
       phase = PH_NEED;
     }
   };
@@ -1233,8 +1239,10 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       if (finished) finish(finalStatus);
     }
   }
-  if (SURR && sd.stats) {
-    // One atomic pair per warp for the network/table evaluation counts.
+  if (sd.stats) {
+    // One atomic pair per warp for the network/table evaluation counts
+    // (a form without the network counts its table evaluations when it
+    // runs the table half of a surrogate form's split launch).
     for (int o = 16; o > 0; o >>= 1) {
       nNet += __shfl_down_sync(FULL, nNet, o);
       nTab += __shfl_down_sync(FULL, nTab, o);

@@ -152,8 +152,115 @@ void effective_shape(const gal_ctx* ctx, int mode, int& threads, int& blocksPerS
 
 namespace {
 
+// The surrogate forms' split launch, step 1: sort the batch into the nodes
+// the network may serve at their starting state (surrogate_open: a T row
+// with network cells, hot gas, a metallicity in a cell the error map leaves
+// to the network) and the others.  Lists in order of arrival (warp-
+// aggregated atomics): a node's result does not depend on its place.
+template <bool FAST>
+__global__ void surrogate_classify(const __grid_constant__ Globals G, const __grid_constant__ SurrogateInfo I,
+                                   const uint8_t* map, const double* param, const double* state, int64_t n,
+                                   int32_t* orderTable, int32_t* orderNet, unsigned long long* counts) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = i0 + threadIdx.x;
+    bool open = false;
+    if (i < n) {
+      // The node's temperature as the kernel's node set-up forms it.
+      const double vvir = param[GAL_P_VELOCITY_VIRIAL * n + i];
+      float log10T;
+      if (FAST) {
+        const float v = (float)vvir, T = G.f.tempPerV2 * v * v;
+        log10T = T > 0.0f ? log10f(T) : -1.0e30f;
+      } else {
+        const double T = 0.5 * k::atomicMassUnit * k::meanAtomicMassPrimordial * (k::kilo * vvir) * (k::kilo * vvir) /
+                         k::boltzmannsConstant;
+        log10T = T > 0.0 ? (float)log10(T) : -1.0e30f;
+      }
+      struct { int netRow; } c{surrogate_net_row(I, map, log10T, !(vvir > G.p.cooling_velocity_cutoff))};
+      const double y[2] = {state[GAL_Y_HOT_MASS * n + i], state[GAL_Y_HOT_METALS * n + i]};
+      open = surrogate_open(I, map, c, y);
+    }
+    const unsigned active = __ballot_sync(FULL, i < n);
+    const unsigned net = __ballot_sync(FULL, open);
+    const unsigned tab = active & ~net;
+    unsigned long long baseNet = 0, baseTab = 0;
+    if (lane == 0) {
+      if (net) baseNet = atomicAdd(&counts[1], (unsigned long long)__popc(net));
+      if (tab) baseTab = atomicAdd(&counts[0], (unsigned long long)__popc(tab));
+    }
+    baseNet = __shfl_sync(FULL, baseNet, 0);
+    baseTab = __shfl_sync(FULL, baseTab, 0);
+    const unsigned below = (1u << lane) - 1u;
+    if (i < n) {
+      if (open) orderNet[baseNet + __popc(net & below)] = (int32_t)i;
+      else orderTable[baseTab + __popc(tab & below)] = (int32_t)i;
+    }
+  }
+}
+
 cudaError_t dispatch(gal_ctx* ctx, const Batch& b, cudaStream_t st) {
   const int mode = ctx_mode(ctx);
+  if ((mode & MODE_SURROGATE) && ctx->splitSurrogate && b.n <= (int64_t)INT32_MAX) {
+    // The split launch: the nodes the network may serve go to the surrogate
+    // kernel, the others to the kernel of the same rates without it, the two
+    // running at once on two streams (one block of each per SM).  The form
+    // without the network keeps its own registers and code: in one kernel
+    // with the network path it ran ~20% slower.
+    if (b.n > ctx->orderCap) {
+      cudaFree(ctx->dOrder);
+      ctx->dOrder = nullptr;
+      ctx->orderCap = 0;
+      cudaError_t e = cudaMalloc(&ctx->dOrder, 2 * (size_t)b.n * sizeof(int32_t));
+      if (e != cudaSuccess) return e;
+      ctx->orderCap = b.n;
+    }
+    int32_t* orderTable = ctx->dOrder;
+    int32_t* orderNet = ctx->dOrder + ctx->orderCap;
+    unsigned long long* counts = ctx->dOrderCount;  // [0] table list, [1] network list, [2], [3] queue heads
+    cudaError_t e = cudaMemsetAsync(counts, 0, 4 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    const int cb = (int)std::min<int64_t>((b.n + 255) / 256, (int64_t)ctx->smCount * 8);
+    if (mode & MODE_FAST)
+      surrogate_classify<true><<<cb, 256, 0, st>>>(ctx->globals, ctx->surrInfo, ctx->dSurrMap, b.param, b.state, b.n,
+                                                   orderTable, orderNet, counts);
+    else
+      surrogate_classify<false><<<cb, 256, 0, st>>>(ctx->globals, ctx->surrInfo, ctx->dSurrMap, b.param, b.state, b.n,
+                                                    orderTable, orderNet, counts);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ctx->evFork, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(ctx->stream2, ctx->evFork, 0)) != cudaSuccess) return e;
+    int threads, blocksPerSm;
+    effective_shape(ctx, mode, threads, blocksPerSm);
+    const int tableMode = mode & ~MODE_SURROGATE;
+    const int64_t blocksNet = std::max<int64_t>(1, std::min<int64_t>(ctx->smCount, (b.n + threads - 1) / threads));
+    LaunchArgs a{};
+    a.G = ctx->globals;
+    a.tables = ctx_tables(ctx);
+    a.b = b;
+    a.b.order = orderNet;
+    a.b.orderCount = counts + 1;
+    a.b.queue = counts + 3;
+    a.sd = SurrogateDev{ctx->dSurrSmall, ctx->dSurrPlanes, ctx->dSurrMap, ctx->surrInfo, ctx->dSurrStats};
+    a.shm = ctx_shared_bytes(ctx, mode);
+    a.blocks = blocksNet;
+    a.stream = ctx->stream2;
+    if ((e = evolve_launch(mode, threads, a)) != cudaSuccess) return e;
+    const int tableThreads = mode_has_threads(tableMode, threads) ? threads : 128;
+    LaunchArgs t = a;
+    t.b.order = orderTable;
+    t.b.orderCount = counts;
+    t.b.queue = counts + 2;
+    t.sd = SurrogateDev{};
+    t.sd.stats = ctx->dSurrStats;  // the table evaluations of these nodes
+    t.shm = ctx_shared_bytes(ctx, tableMode);
+    t.blocks = std::max<int64_t>(1, std::min<int64_t>(ctx->smCount, (b.n + tableThreads - 1) / tableThreads));
+    t.stream = st;
+    if ((e = evolve_launch(tableMode, tableThreads, t)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ctx->evJoin, ctx->stream2)) != cudaSuccess) return e;
+    ctx->launches += 2;  // the classification and the second kernel (the caller counts one)
+    return cudaStreamWaitEvent(st, ctx->evJoin, 0);
+  }
   int threads, blocksPerSm;
   effective_shape(ctx, mode, threads, blocksPerSm);
   LaunchArgs a{};
@@ -334,7 +441,11 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
       cudaMalloc(&ctx->dLnZF, 2 * nZ * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&ctx->dKmt, (kmt::kFractionCount + kmt::kPowerCount) * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&ctx->dKmtF, (kmt::kFractionCount + kmt::kPowerCount) * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(&ctx->dQueue, sizeof(unsigned long long)) != cudaSuccess) {
+      cudaMalloc(&ctx->dQueue, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&ctx->dOrderCount, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->evFork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->evJoin, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     fail(nullptr, GAL_ERR_CUDA, "device allocation failed%s");
     return cleanup(GAL_ERR_CUDA);
@@ -368,6 +479,14 @@ void gal_gpu_free(gal_ctx* ctx) {
   cudaFree(ctx->dKmt);
   cudaFree(ctx->dKmtF);
   cudaFree(ctx->dQueue);
+  cudaFree(ctx->dOrder);
+  cudaFree(ctx->dOrderCount);
+  if (ctx->stream2) {
+    cudaStreamSynchronize(ctx->stream2);
+    cudaStreamDestroy(ctx->stream2);
+  }
+  if (ctx->evFork) cudaEventDestroy(ctx->evFork);
+  if (ctx->evJoin) cudaEventDestroy(ctx->evJoin);
   cudaFree(ctx->dBuf);
   free_surrogate(ctx);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -613,6 +732,12 @@ int gal_gpu_set_surrogate(gal_ctx* ctx, const gal_surrogate* sg) {
     free_surrogate(ctx);
     return fail(ctx, GAL_ERR_CUDA, "gal_gpu_set_surrogate: upload failed%s");
   }
+  return GAL_OK;
+}
+
+int gal_gpu_set_surrogate_split(gal_ctx* ctx, int32_t split) {
+  if (!ctx) return fail(nullptr, GAL_ERR_ARGUMENT, "gal_gpu_set_surrogate_split: NULL context%s");
+  ctx->splitSurrogate = split ? 1 : 0;
   return GAL_OK;
 }
 

@@ -60,6 +60,8 @@ def _declare(lib):
     lib.gal_surrogate_predict.restype = ctypes.c_int
     lib.gal_gpu_set_surrogate.argtypes = [ctypes.c_void_p, ctypes.POINTER(SurrogateStruct)]
     lib.gal_gpu_set_surrogate.restype = ctypes.c_int
+    lib.gal_gpu_set_surrogate_split.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    lib.gal_gpu_set_surrogate_split.restype = ctypes.c_int
     lib.gal_gpu_surrogate_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
     lib.gal_gpu_surrogate_stats.restype = ctypes.c_int
     lib._surrogate_declared = True
@@ -255,6 +257,14 @@ def gradient(params, x_norm, y_norm):
     if rc:
         raise RuntimeError(f"gal_surrogate_gradient failed ({rc})")
     return loss.value, g
+
+
+def set_split(evolver, split):
+    """The batch launch with a surrogate: split (default) or one kernel."""
+    lib = _declare(evolver.lib)
+    rc = lib.gal_gpu_set_surrogate_split(evolver.ctx, 1 if split else 0)
+    if rc:
+        raise RuntimeError(f"gal_gpu_set_surrogate_split failed ({rc})")
 
 
 def stats(evolver):

@@ -76,6 +76,16 @@ int gal_surrogate_predict(const float* params, const float* x, int64_t n, float*
  * it (512 threads per block is not available then). */
 int gal_gpu_set_surrogate(gal_ctx* ctx, const gal_surrogate* s);
 
+/* How a batch is launched while a surrogate is installed: split = 1
+ * (default) sorts the nodes by whether the network may serve them at their
+ * starting state and runs those with the network kernel and the others
+ * with the kernel of the same rates without it, at once on two streams;
+ * split = 0 runs one network kernel over all nodes.  Results are the same
+ * except that in the split launch a node whose starting cell the error map
+ * gives to the table uses the table throughout the call.  No counterpart in
+ * the reference. */
+int gal_gpu_set_surrogate_split(gal_ctx* ctx, int32_t split);
+
 /* Cooling-function evaluations by the surrogate and by the table fallback
  * since the surrogate was installed (one per node and right-hand side). */
 int gal_gpu_surrogate_stats(const gal_ctx* ctx, uint64_t* network, uint64_t* table);

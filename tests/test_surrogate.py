@@ -84,3 +84,34 @@ def test_evolution_with_surrogate_against_the_table(trained, table, oracle_mod, 
     errs = compare.relative_mass_errors(g.state, ref)
     for name, (rel, big) in errs.items():
         assert np.median(rel[big]) < 1e-3, f"{name}: median rel error {np.median(rel[big]):.2e}"
+
+
+def test_split_launch_matches_one_kernel(trained, table):
+    """The surrogate form's split launch (the nodes the network may serve on
+    the network kernel, the others on the kernel without it, at once) against
+    one network kernel over all nodes: every node succeeds, nearly every node
+    is bit for bit the same (a node may use the network in the one-kernel
+    launch once its metallicity reaches a served cell), and the evaluation
+    counts add up to the RHS evaluations."""
+    from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
+    params = workloads.isolated_params()
+    batch = workloads.isolated_halos(n=8192, seed=2)
+    ev = MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision="fp32")
+    trained.build_error_map(table, tolerance=0.003)
+    trained.install(ev)
+    out = {}
+    for split in (True, False):
+        surrogate.set_split(ev, split)
+        a = surrogate.stats(ev)
+        g = batch.copy()
+        status, counters = ev.evolve(g.state, g.param, g.t_start, g.t_end, g.step, return_status=True, counters=True)
+        b = surrogate.stats(ev)
+        assert np.all(status == 0)
+        out[split] = (g.state, counters, (b[0] - a[0], b[1] - a[1]))
+    ev.close()
+    same = np.all(out[True][0] == out[False][0], axis=0)
+    assert same.mean() > 0.95
+    for split in (True, False):
+        net, tab = out[split][2]
+        assert net + tab == int(out[split][1][2].sum())
+        assert net > 0.2 * (net + tab)
