@@ -30,6 +30,21 @@ def case(params, table, oracle_mod):
     return f, state0, times, ref
 
 
+@pytest.fixture(scope="module")
+def sensitivity(case, table, oracle_mod):
+    """How far the oracle's own final states and snapshots move when the
+    relative tolerance changes by 10%: the conditioning of each value.
+    Mergers build spheroids in these trees, and a spheroid black hole that
+    grows by Bondi-Hoyle accretion (rate ~ M^2) towards its Eddington limit
+    can end anywhere between hundreds and 5e5 Msun with such a change (or
+    with the last bits of the host's libm)."""
+    f, state0, times, (ref, _, _, ref_snaps) = case
+    moved = [oracle_mod.evolve_forest(workloads.isolated_params(1e-3 * k), table, f, state0, times, brent=False)
+             for k in (0.9, 1.1)]
+    return (np.maximum(np.abs(moved[0][0] - ref), np.abs(moved[1][0] - ref)),
+            np.maximum(np.abs(moved[0][3] - ref_snaps), np.abs(moved[1][3] - ref_snaps)))
+
+
 def _evolver(params, table, rates="fp64"):
     from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
     return MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision=rates)
@@ -50,8 +65,9 @@ def _worst(a, ref, bound):
     return [(int(v), int(i), float(a[v, i]), float(ref[v, i])) for v, i in bad[:5]]
 
 
-def test_plain_forest_matches_oracle(case, params, table, oracle_mod):
+def test_plain_forest_matches_oracle(case, sensitivity, params, table, oracle_mod):
     f, state0, times, (ref, ref_status, ref_counters, ref_snaps) = case
+    sens, sens_snaps = sensitivity
     ev = _evolver(params, table)
     fe = forest.ForestEvolver(ev, f, state0, times)
     fe.evolve()
@@ -59,15 +75,19 @@ def test_plain_forest_matches_oracle(case, params, table, oracle_mod):
     assert np.all(status == 0) and np.all(ref_status == 0)
     # The plain form is the reference's FP64 arithmetic: every final mass and
     # metal mass of every node within ten times the tolerance of the oracle
-    # (in practice to rounding).
+    # (in practice to rounding), or, for the values whose oracle answer moves
+    # by more than that under a 10% change of the tolerance, within twice
+    # that movement.
     bound = _bound(ref, params, f)
-    assert np.all(np.abs(state - ref) <= bound), _worst(state, ref, bound)
+    within = np.abs(state - ref) <= bound
+    assert np.all(within | (np.abs(state - ref) <= bound + 2.0 * sens)), _worst(state, ref, bound + 2.0 * sens)
+    assert np.mean(np.all(within, axis=0)) > 0.998
     assert np.median(np.abs(state - ref) / np.maximum(np.abs(ref), 1e-300)) < 1e-12
     # Snapshots: same slots, same values.
     first, m = oracle_mod.forest_snapshots(f, times)
     assert snaps.shape == ref_snaps.shape == (_abi.NY, m)
     expected_node = np.repeat(np.arange(f.n), np.diff(np.append(first, m)))
-    sbound = _bound(ref_snaps, params, f, expected_node)
+    sbound = _bound(ref_snaps, params, f, expected_node) + 2.0 * sens_snaps
     assert np.all(np.abs(snaps - ref_snaps) <= sbound), _worst(snaps, ref_snaps, sbound)
     np.testing.assert_array_equal(snap_node, expected_node)
     assert np.all(times[snap_out] >= f.time[snap_node])
@@ -129,16 +149,17 @@ def test_autotune_picks_a_built_shape(case, params, table):
     ev.close()
 
 
-def test_forest_matches_reference_root_finder(case, params, table, oracle_mod):
+def test_forest_matches_reference_root_finder(case, sensitivity, params, table, oracle_mod):
     """Against the oracle with the reference's Brent cooling radius: within
-    ten times the tolerance everywhere."""
+    ten times the tolerance everywhere (ill-conditioned values: within twice
+    the oracle's own movement beyond it)."""
     f, state0, times, _ = case
     ref, _, _, _ = oracle_mod.evolve_forest(params, table, f, state0, times, brent=True)
     ev = _evolver(params, table)
     fe = forest.ForestEvolver(ev, f, state0, times)
     fe.evolve()
     state = fe.results()[0]
-    bound = _bound(ref, params, f)
+    bound = _bound(ref, params, f) + 2.0 * sensitivity[0]
     assert np.all(np.abs(state - ref) <= bound), _worst(state, ref, bound)
     fe.close()
     ev.close()
