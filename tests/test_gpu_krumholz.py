@@ -91,7 +91,7 @@ def test_krumholz_forest_parity(table, oracle_mod, rates):
     ref, ref_status = oracle_mod.evolve_forest(params, table, f, state0, times, brent=False)[:2]
     assert np.all(status == 0) and np.all(ref_status == 0)
     roots = f.parent < 0
-    assert np.all(ref[_abi.Y_DISK_STARS, roots] > 0.0)
+    assert np.all(ref[_abi.Y_DISK_STARS, roots] + ref[_abi.Y_SPHEROID_STARS, roots] > 0.0)
     param = np.zeros((_abi.NP, f.n))
     param[_abi.P_MASS] = f.mass
     within = np.abs(state - ref) <= compare.parity_bound(ref, ref, param, params)
