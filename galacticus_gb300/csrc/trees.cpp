@@ -20,11 +20,12 @@
 // (the larger one first); a branch that drops below the resolution or
 // reaches the maximum redshift ends in a leaf node.
 //
-// sigma(M) is that of a power law n_s times the Eisenstein & Hu (1998)
-// zero-baryon transfer function, normalised to sigma8 (the reference's
-// default is the Eisenstein & Hu 1999 fit, transfer_function/
-// Eisenstein_Hu1999.F90); D(z) is the linear growth factor of a flat
-// matter + Lambda model; delta_c0 = 3 (12 pi)^(2/3) / 20.
+// sigma(M) is that of a power law n_s times the transfer function squared,
+// normalised to sigma8: by default the Eisenstein & Hu (1999) fit with
+// massive-neutrino suppression, the reference's default (transfer_function/
+// Eisenstein_Hu1999.F90), or the Eisenstein & Hu (1998) zero-baryon form;
+// D(z) is the linear growth factor of a flat matter + Lambda model;
+// delta_c0 = 3 (12 pi)^(2/3) / 20.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -72,6 +73,57 @@ double transfer_no_wiggle(double k, const Cosmo& c, double tcmb) {
   return l0 / (l0 + c0 * q * q);
 }
 
+// Eisenstein & Hu (1999, ApJ 511, 5) transfer function of cold dark matter,
+// baryons and massive neutrinos, k in 1/Mpc, as the reference evaluates it
+// (transfer_function/Eisenstein_Hu1999.F90:100-420): the shape parameter
+// with the small-scale suppression alpha_nu (eqs. 15-16), the zero-baryon
+// form L / (L + C q_eff^2) (eqs. 17-20) with beta_c (eq. 21), and the
+// suppression near the neutrino free-streaming scale for 0 < f_nu <= 0.3.
+struct EisensteinHu1999 {
+  double omh2, theta, s, alphaNu, betaC, fNu, nEff;
+
+  EisensteinHu1999(const Cosmo& c, const gal_pch_params& pch) {
+    const double h = c.h0 / 100.0;
+    omh2 = c.om * h * h;
+    const double obh2 = c.ob * h * h;
+    theta = pch.temperature_cmb / 2.7;
+    const double zEq = 2.50e4 * omh2 / std::pow(theta, 4);
+    const double b1 = 0.313 * std::pow(omh2, -0.419) * (1.0 + 0.607 * std::pow(omh2, 0.674));
+    const double b2 = 0.238 * std::pow(omh2, 0.223);
+    const double zDrag = 1291.0 * std::pow(omh2, 0.251) * (1.0 + b1 * std::pow(obh2, b2)) / (1.0 + 0.659 * std::pow(omh2, 0.828));
+    const double yD = (1.0 + zEq) / (1.0 + zDrag);
+    s = 44.5 * std::log(9.83 / omh2) / std::sqrt(1.0 + 10.0 * std::pow(obh2, 0.75));
+    fNu = pch.neutrino_mass_summed / 94.0 / (h * h) / c.om;
+    nEff = pch.neutrino_number_effective;
+    const double fB = c.ob / c.om, fC = (c.om - c.ob) / c.om, fCB = fB + fC, fNuB = fNu + fB;
+    const double pC = 0.25 * (5.0 - std::sqrt(1.0 + 24.0 * fC)), pCB = 0.25 * (5.0 - std::sqrt(1.0 + 24.0 * fCB));
+    alphaNu = (fC / fCB) * ((5.0 - 2.0 * (pC + pCB)) / (5.0 - 4.0 * pCB)) *
+              ((1.0 - 0.533 * fNuB + 0.126 * fNuB * fNuB * fNuB) * std::pow(1.0 + yD, pCB - pC) /
+               (1.0 - 0.193 * std::sqrt(fNu * nEff) + 0.169 * fNu * std::pow(nEff, 0.2))) *
+              (1.0 + 0.5 * (pC - pCB) * (1.0 + 1.0 / ((3.0 - 4.0 * pC) * (7.0 - 4.0 * pCB))) / (1.0 + yD));
+    betaC = 1.0 / (1.0 - 0.949 * fNuB);
+  }
+  double operator()(double k) const {
+    const double sa = std::sqrt(alphaNu);
+    const double ks = 0.43 * k * s;
+    const double gammaEff = omh2 * (sa + (1.0 - sa) / (1.0 + ks * ks * ks * ks));
+    const double q = k * theta * theta / gammaEff;
+    const double L = std::log(std::exp(1.0) + 1.84 * betaC * sa * q);
+    const double C = 14.4 + 325.0 / (1.0 + 60.5 * std::pow(q, 1.11));
+    double t = L / (L + C * q * q);
+    if (fNu > 0.0 && fNu <= 0.3) {
+      const double qNu = 3.92 * (k * theta * theta / omh2) * std::sqrt(nEff) / fNu;
+      t *= 1.0 + 1.2 * std::pow(fNu, 0.64) * std::pow(nEff, 0.3 + 0.6 * fNu) / (std::pow(qNu, -1.6) + std::pow(qNu, 0.8));
+    }
+    return t;
+  }
+};
+
+double transfer(double k, const Cosmo& c, const gal_pch_params& pch) {
+  if (pch.transfer_function == GAL_TRANSFER_EISENSTEIN_HU_1998) return transfer_no_wiggle(k, c, pch.temperature_cmb);
+  return EisensteinHu1999(c, pch)(k);
+}
+
 double window_top_hat(double x) {
   if (x < 1.0e-3) return 1.0 - x * x / 10.0;
   return 3.0 * (std::sin(x) - x * std::cos(x)) / (x * x * x);
@@ -86,9 +138,12 @@ struct SigmaTable {
     const int nk = 8000;
     const double lnk0 = std::log(1.0e-6), lnk1 = std::log(1.0e4), dlnk = (lnk1 - lnk0) / (nk - 1);
     std::vector<double> kk(nk), pk(nk);
+    const EisensteinHu1999 eh99(c, pch);
     for (int i = 0; i < nk; ++i) {
       kk[i] = std::exp(lnk0 + i * dlnk);
-      const double t = transfer_no_wiggle(kk[i], c, pch.temperature_cmb);
+      const double t = pch.transfer_function == GAL_TRANSFER_EISENSTEIN_HU_1998
+                           ? transfer_no_wiggle(kk[i], c, pch.temperature_cmb)
+                           : eh99(kk[i]);
       pk[i] = std::pow(kk[i], pch.n_s) * t * t;
     }
     auto sigma2R = [&](double R) {
@@ -390,6 +445,12 @@ struct Builder {
   }
 };
 
+bool valid_transfer(const gal_pch_params& pch) {
+  return (pch.transfer_function == GAL_TRANSFER_EISENSTEIN_HU_1999 ||
+          pch.transfer_function == GAL_TRANSFER_EISENSTEIN_HU_1998) &&
+         pch.neutrino_number_effective >= 0.0 && pch.neutrino_mass_summed >= 0.0;
+}
+
 uint64_t splitmix64(uint64_t x) {
   x += 0x9e3779b97f4a7c15ull;
   x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
@@ -417,13 +478,21 @@ void gal_pch_params_default(gal_pch_params* p) {
   p->sigma8 = 0.8;
   p->n_s = 0.96;
   p->temperature_cmb = 2.72548;
+  p->transfer_function = GAL_TRANSFER_EISENSTEIN_HU_1999;
+  p->neutrino_number_effective = 3.046;
+  p->neutrino_mass_summed = 0.0;
 }
 
 double gal_cosmic_time(const gal_params* p, double z) { return p ? cosmo_of(p).time(z) : NAN; }
 double gal_redshift(const gal_params* p, double t) { return p ? cosmo_of(p).redshift(t) : NAN; }
 
+double gal_pch_transfer(const gal_params* p, const gal_pch_params* pch, double k) {
+  if (!p || !pch || !(k > 0.0) || !valid_transfer(*pch)) return NAN;
+  return transfer(k, cosmo_of(p), *pch);
+}
+
 double gal_pch_sigma(const gal_params* p, const gal_pch_params* pch, double mass) {
-  if (!p || !pch || !(mass > 0.0)) return NAN;
+  if (!p || !pch || !(mass > 0.0) || !valid_transfer(*pch)) return NAN;
   SigmaTable s;
   s.build(cosmo_of(p), *pch);
   return std::sqrt(s.sigma2(mass));
@@ -454,7 +523,7 @@ int gal_pch_branching_rates(const gal_pch_params* pch, double alpha, double sigm
 int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec, gal_forest** out) {
   if (!out) return GAL_ERR_ARGUMENT;
   *out = nullptr;
-  if (!p || !pch || !spec || spec->n_trees < 0 || !(spec->mass_resolution > 0.0) ||
+  if (!p || !pch || !spec || !valid_transfer(*pch) || spec->n_trees < 0 || !(spec->mass_resolution > 0.0) ||
       !(spec->root_mass_min >= spec->mass_resolution) || !(spec->root_mass_max >= spec->root_mass_min) ||
       !(spec->redshift_max > spec->root_redshift) || spec->root_redshift < 0.0 || spec->redshift_max > 30.0)
     return GAL_ERR_ARGUMENT;

@@ -16,9 +16,15 @@ import numpy as np
 from . import _abi
 
 
+TRANSFER_EISENSTEIN_HU_1999 = 0  # the reference's default transfer function
+TRANSFER_EISENSTEIN_HU_1998 = 1
+
+
 class PchParams(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in ("g0", "gamma1", "gamma2", "accuracy_first", "accuracy_second",
-                                                "sigma8", "n_s", "temperature_cmb")]
+                                                "sigma8", "n_s", "temperature_cmb")] + \
+               [("transfer_function", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("neutrino_number_effective", ctypes.c_double), ("neutrino_mass_summed", ctypes.c_double)]
 
 
 class ForestSpec(ctypes.Structure):
@@ -49,6 +55,8 @@ def _declare(lib):
     lib.gal_redshift.restype = ctypes.c_double
     lib.gal_pch_sigma.argtypes = [pp, ctypes.POINTER(PchParams), ctypes.c_double]
     lib.gal_pch_sigma.restype = ctypes.c_double
+    lib.gal_pch_transfer.argtypes = [pp, ctypes.POINTER(PchParams), ctypes.c_double]
+    lib.gal_pch_transfer.restype = ctypes.c_double
     dp = ctypes.POINTER(ctypes.c_double)
     lib.gal_pch_branching_rates.argtypes = [ctypes.POINTER(PchParams)] + [ctypes.c_double] * 5 + [dp, dp]
     lib.gal_pch_branching_rates.restype = ctypes.c_int

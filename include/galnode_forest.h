@@ -57,7 +57,17 @@ typedef struct gal_pch_params {
   double accuracy_second;     /* step limit on d(delta_c) relative to sigma (0.1)          */
   double sigma8, n_s;         /* power-spectrum normalisation and slope                     */
   double temperature_cmb;     /* K (2.72548)                                               */
+  int32_t transfer_function;  /* GAL_TRANSFER_* (the reference's default, Eisenstein & Hu 1999) */
+  int32_t reserved;
+  double neutrino_number_effective; /* Eisenstein & Hu (1999): N_eff (3.046)              */
+  double neutrino_mass_summed;      /* Eisenstein & Hu (1999): sum of masses, eV (0)      */
 } gal_pch_params;
+
+/* Transfer functions of the builder's power spectrum: the reference's
+ * transferFunctionEisensteinHu1999 (its default; structure_formation/
+ * transfer_function/Eisenstein_Hu1999.F90) and the Eisenstein & Hu (1998)
+ * zero-baryon form. */
+enum { GAL_TRANSFER_EISENSTEIN_HU_1999 = 0, GAL_TRANSFER_EISENSTEIN_HU_1998 = 1 };
 
 typedef struct gal_forest_spec {
   int64_t n_trees;
@@ -90,6 +100,9 @@ double gal_cosmic_time(const gal_params* p, double z);
 double gal_redshift(const gal_params* p, double t);
 /* sigma(M) of the builder's power spectrum at z = 0 (for tests). */
 double gal_pch_sigma(const gal_params* p, const gal_pch_params* pch, double mass);
+/* The builder's transfer function at wavenumber k (1/Mpc) (for tests);
+ * the reference's transferFunctionClass%value. */
+double gal_pch_transfer(const gal_params* p, const gal_pch_params* pch, double k);
 /* The builder's branching rates, per unit of the critical overdensity w,
  * for a branch of mass_parent at w when sigma(M) is the power law
  * sigma_parent (M/mass_parent)^alpha: rate = the probability rate of a

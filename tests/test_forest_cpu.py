@@ -30,6 +30,67 @@ def test_sigma_normalisation(params):
     assert lib.gal_pch_sigma(ctypes.byref(params), ctypes.byref(pch), 1e10) > s
 
 
+def eisenstein_hu_1999(k, omega_matter, omega_baryon, h, t_cmb, n_eff=3.046, m_nu=0.0):
+    """Eisenstein & Hu (1999, ApJ 511, 5) eqs. 2-4 and 15-22, written out
+    independently of the builder, k in 1/Mpc."""
+    omh2, obh2, theta = omega_matter * h * h, omega_baryon * h * h, t_cmb / 2.7
+    z_eq = 2.5e4 * omh2 * theta ** -4
+    b1 = 0.313 * omh2 ** -0.419 * (1 + 0.607 * omh2 ** 0.674)
+    b2 = 0.238 * omh2 ** 0.223
+    z_d = 1291 * omh2 ** 0.251 / (1 + 0.659 * omh2 ** 0.828) * (1 + b1 * obh2 ** b2)
+    y_d = (1 + z_eq) / (1 + z_d)
+    s = 44.5 * np.log(9.83 / omh2) / np.sqrt(1 + 10 * obh2 ** 0.75)
+    f_nu = m_nu / (94 * h * h * omega_matter)
+    f_b = omega_baryon / omega_matter
+    f_c = 1 - f_b
+    f_cb, f_nub = f_c + f_b, f_nu + f_b
+    p_c, p_cb = (5 - np.sqrt(1 + 24 * f_c)) / 4, (5 - np.sqrt(1 + 24 * f_cb)) / 4
+    alpha = (f_c / f_cb) * (5 - 2 * (p_c + p_cb)) / (5 - 4 * p_cb) \
+        * (1 - 0.533 * f_nub + 0.126 * f_nub ** 3) / (1 - 0.193 * np.sqrt(f_nu * n_eff) + 0.169 * f_nu * n_eff ** 0.2) \
+        * (1 + y_d) ** (p_cb - p_c) * (1 + (p_c - p_cb) / 2 * (1 + 1 / ((3 - 4 * p_c) * (7 - 4 * p_cb))) / (1 + y_d))
+    gamma_eff = omh2 * (np.sqrt(alpha) + (1 - np.sqrt(alpha)) / (1 + (0.43 * k * s) ** 4))
+    q_eff = k * theta ** 2 / gamma_eff
+    beta_c = 1 / (1 - 0.949 * f_nub)
+    big_l = np.log(np.e + 1.84 * beta_c * np.sqrt(alpha) * q_eff)
+    big_c = 14.4 + 325 / (1 + 60.5 * q_eff ** 1.11)
+    t = big_l / (big_l + big_c * q_eff ** 2)
+    if 0 < f_nu <= 0.3:
+        q_nu = 3.92 * k * theta ** 2 / omh2 * np.sqrt(n_eff) / f_nu
+        t = t * (1 + 1.2 * f_nu ** 0.64 * n_eff ** (0.3 + 0.6 * f_nu) / (q_nu ** -1.6 + q_nu ** 0.8))
+    return t
+
+
+@pytest.mark.parametrize("m_nu", [0.0, 0.06])
+def test_transfer_function_eisenstein_hu_1999(params, m_nu):
+    """The builder's default transfer function is the reference's default,
+    transferFunctionEisensteinHu1999 (structure_formation/transfer_function/
+    Eisenstein_Hu1999.F90), with and without massive neutrinos (the
+    reference's transfer-function test uses both, source/tests/
+    transfer_functions.F90:65-78)."""
+    import ctypes
+    lib = forest._declare(_abi.load_library())
+    pch = forest.pch_params()
+    assert pch.transfer_function == forest.TRANSFER_EISENSTEIN_HU_1999
+    assert pch.neutrino_number_effective == 3.046 and pch.neutrino_mass_summed == 0.0
+    pch.neutrino_mass_summed = m_nu
+    h = params.hubble_constant / 100.0
+    for k in np.geomspace(1e-3, 1e2, 16):
+        got = lib.gal_pch_transfer(ctypes.byref(params), ctypes.byref(pch), k)
+        want = eisenstein_hu_1999(k, params.omega_matter, params.omega_baryon, h, pch.temperature_cmb, m_nu=m_nu)
+        assert abs(got / want - 1.0) < 1e-12, (k, got, want)
+    # Large scales are unsuppressed; the 1998 zero-baryon form stays a
+    # selectable alternative and differs from the 1999 fit by percents.
+    assert abs(lib.gal_pch_transfer(ctypes.byref(params), ctypes.byref(pch), 1e-5) - 1.0) < 2e-3
+    eh98 = forest.pch_params()
+    eh98.transfer_function = forest.TRANSFER_EISENSTEIN_HU_1998
+    ratio = [lib.gal_pch_transfer(ctypes.byref(params), ctypes.byref(eh98), k) /
+             lib.gal_pch_transfer(ctypes.byref(params), ctypes.byref(forest.pch_params()), k) for k in (0.1, 1.0, 10.0)]
+    assert all(0.8 < r < 1.2 for r in ratio) and any(abs(r - 1.0) > 1e-3 for r in ratio)
+    bad = forest.pch_params()
+    bad.transfer_function = 7
+    assert np.isnan(lib.gal_pch_transfer(ctypes.byref(params), ctypes.byref(bad), 1.0))
+
+
 @pytest.mark.parametrize("w", [1.686, 4.0])
 def test_branching_rates_match_reference_known_answers(w):
     """The builder's branching rates against the reference's known answers
