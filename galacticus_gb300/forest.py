@@ -178,6 +178,12 @@ def branching_rates(pch, alpha, sigma_parent, mass_parent, mass_resolution, w=1.
     return r.value, a.value
 
 
+def redshift(params, t):
+    """Redshift at cosmic time t (Gyr) in the cosmology of params."""
+    lib = _declare(_abi.load_library())
+    return lib.gal_redshift(ctypes.byref(params), float(t))
+
+
 def output_times(params, n=20, redshift_max=8.0):
     """n output times from redshift_max to 0, evenly spaced in ln(1+z)."""
     lib = _declare(_abi.load_library())

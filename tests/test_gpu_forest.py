@@ -105,6 +105,18 @@ def test_plain_forest_matches_oracle(case, sensitivity, params, table, oracle_mo
     assert fe.accepted_steps() == int(counters[0].sum())
     fe.close()
     ev.close()
+    # The device snapshots in the reference's output layout: the last output
+    # holds every root, with the snapshot values under the reference's names.
+    from galacticus_gb300 import output
+    out = output.layout(params, f, times, snaps, snap_node, snap_out)
+    last = f"Outputs/Output{len(times)}"
+    roots = np.flatnonzero(f.parent < 0)
+    np.testing.assert_array_equal(np.sort(out[f"{last}/nodeData/nodeIndex"]), roots)
+    idx = out[f"{last}/nodeData/nodeIndex"]
+    slot = {int(n): j for j, n in enumerate(snap_node) if snap_out[j] == len(times) - 1}
+    np.testing.assert_array_equal(out[f"{last}/nodeData/diskMassStellar"],
+                                  snaps[_abi.Y_DISK_STARS, [slot[int(n)] for n in idx]])
+    assert out[f"{last}/mergerTreeCount"].sum() == roots.size
 
 
 def test_graph_replays_are_identical(case, params, table):
