@@ -59,12 +59,12 @@ extern "C" int gal_calibrate_fp64(double* flops, double* ms) {
 #include "galnode_fastmath.cuh"
 
 namespace {
-constexpr int kTests = 8;
+constexpr int kTests = 12;
 
 __global__ void fastmath_errors(double* blockMax, int samples, const double2* logT, const double* expT) {
   __shared__ double sMax[kTests][256];
   const gal::FastTables F{logT, expT};
-  double m[kTests] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double m[kTests] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < samples; i += gridDim.x * blockDim.x) {
     // Log-spaced arguments over 1e-29 .. 1e29 with a non-smooth mantissa.
     const double u = (double)i / samples;
@@ -85,6 +85,42 @@ __global__ void fastmath_errors(double* blockMax, int samples, const double2* lo
     const double r = exp(log(3.0e-5) + (log(1900.0) - log(3.0e-5)) * u);
     m[6] = fmax(m[6], fabs(gal::inv_root<5>(r) / pow(r, -0.2) - 1.0));
     m[7] = fmax(m[7], fabs(gal::inv_root<6>(r) / pow(r, -1.0 / 6.0) - 1.0));
+    // The controller's 0.9 r^(-1/Q) from an FP32 seed ratio that is off by up
+    // to 3e-6 (the FP32 pick's ratio), with the same fallback as the kernel;
+    // m[10] counts the fallbacks.
+    const float rf = (float)(r * (1.0 + 3.0e-6 * sin(5.0e3 * u)));
+    double c5 = gal::ctrl_root09<5>(r, rf), c6 = gal::ctrl_root09<6>(r, rf);
+    if (c5 < 0.0) { c5 = 0.9 * gal::inv_root<5>(r); m[10] += 1.0; }
+    if (c6 < 0.0) { c6 = 0.9 * gal::inv_root<6>(r); m[10] += 1.0; }
+    m[8] = fmax(m[8], fabs(c5 / (0.9 * pow(r, -0.2)) - 1.0));
+    m[9] = fmax(m[9], fabs(c6 / (0.9 * pow(r, -1.0 / 6.0)) - 1.0));
+    // The integer-pipe comparisons against IEEE ones, on pairs drawn from
+    // signed zeros, subnormals, infinities, NaNs and the log-spaced x of
+    // both signs; m[11] counts disagreements.
+    const double special[12] = {0.0, -0.0, 4.9e-324, -4.9e-324, 2.2250738585072014e-308, 1.1, -1.1,
+                                __longlong_as_double(0x7ff0000000000000LL), __longlong_as_double(0xfff0000000000000LL),
+                                __longlong_as_double(0x7ff8000000000000LL), __longlong_as_double(0xfff8000000000001LL), 0.5};
+    const double p = (i & 1) ? special[(i >> 1) % 12] : ((i & 2) ? -x : x);
+    const double q = (i & 4) ? special[(i >> 3) % 12] : ((i & 8) ? -p * (1.0 + 1.0e-16 * (i % 3)) : p * 0.5);
+    int bad = 0;
+    bad += gal::d_lt(p, q) != (p < q);
+    bad += gal::d_le(p, q) != (p <= q);
+    bad += gal::d_gt(p, q) != (p > q);
+    bad += gal::d_ge(p, q) != (p >= q);
+    bad += gal::d_neg(p) != (p < 0.0);
+    bad += gal::d_isnan(p) != (p != p);
+    bad += (!(gal::d_isnan(p) || gal::d_isnan(q)) && gal::d_key(p) == gal::d_key(q)) != (p == q);
+    // The integer-pipe conversions against the conversion instructions, bit
+    // for bit, on bit patterns spread over every exponent of both formats.
+    const unsigned long long bits = (unsigned long long)i * 0x9E3779B97F4A7C15ULL;
+    const double dv = __longlong_as_double((long long)bits);
+    const float fv = __uint_as_float((unsigned)(bits >> 32));
+    bad += __double_as_longlong(gal::f2d_int(fv)) != __double_as_longlong((double)fv) && !(fv != fv);
+    bad += __float_as_uint(gal::d2f_int(dv)) != __float_as_uint((float)dv) && !(dv != dv);
+    const double dn = x * (1.0 + 1.0e-9 * (i % 7));  // normal-range doubles with long significands
+    bad += __float_as_uint(gal::d2f_int(dn)) != __float_as_uint((float)dn);
+    bad += __float_as_uint(gal::d2f_int(-dn)) != __float_as_uint((float)-dn);
+    m[11] += bad;
   }
   for (int t = 0; t < kTests; ++t) sMax[t][threadIdx.x] = m[t];
   __syncthreads();

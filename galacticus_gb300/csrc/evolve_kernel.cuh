@@ -369,6 +369,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
     ynew = x;
   }
   double t = 0.0, t0 = 0.0, t1 = 0.0, h = 0.0, stepIn = -1.0;
+  double dtLeft = 0.0;  // t1 - t (FP32-rate forms: formed when t changes, not per attempt)
   int trial = 0;
   uint32_t count = 0, nAcc = 0, nRej = 0, nRhs = 0, nNet = 0, nTab = 0;
   // Lanes that never take a node still hold in-range table coordinates.
@@ -438,8 +439,14 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
   auto sync_yr = [&]() {
     if constexpr (FAST) {
 #pragma unroll
-      for (int v = 0; v < GAL_NY; ++v) yf[v] = (float)y[v];
+      for (int v = 0; v < GAL_NY; ++v) yf[v] = d2f_int(y[v]);
     }
+  };
+  // The post-step clamps; the FP32-rate forms test for a negative mass on
+  // the integer pipe first (post_step's FP64 compares only when one is).
+  auto post_step_any = [&](double* yy) -> bool {
+    if constexpr (FAST) return post_step_int(yy);
+    else return post_step(yy);
   };
 
   // ---- work source and completion: a batch of independent nodes, or a forest
@@ -995,7 +1002,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       if (__all_sync(FULL, phase == PH_DONE)) break;
 
       // ---- start (or restart) an ODE trial: odeSolverSolve + driver reset
-      if (phase == PH_TRIAL && t0 == t1) zero_interval();
+      if (phase == PH_TRIAL && (FAST ? !(d_isnan(t0) || d_isnan(t1)) && d_key(t0) == d_key(t1) : t0 == t1)) zero_interval();
       const bool starting = phase == PH_TRIAL;
       if (starting) {
         const double stepSize = G.p.reuse_step_size ? stepIn / (double)(1u << trial) : -1.0;
@@ -1004,6 +1011,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
         if (trial > 0) restore_start();
         sync_yr();
         t = t0;
+        dtLeft = t1 - t0;
         count = 0;
       }
       const bool atY = starting || needOut;
@@ -1039,7 +1047,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
             // The post-step clamps return GSL_Continue: dydt_out is kept.
             needOut = false;
             ++nRhs;
-            if (post_step(y)) sync_yr();
+            if (post_step_any(y)) sync_yr();
             if (budget && count >= budget) {
               finished = true;
               finalStatus = GAL_STATUS_XCPU;
@@ -1047,10 +1055,18 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
           }
           stepping = phase == PH_STEP && !finished;
           if (!any(stepping)) return false;
-          const double dt = t1 - t;
-          finalStep = (dt >= 0.0 && h > dt) || (dt < 0.0 && h < dt);
-          hh = finalStep ? dt : h;
-          hr = (RateT)hh;
+          if constexpr (FAST) {
+            // The same last-step test with the compares on the integer pipe.
+            const double dt = dtLeft;
+            finalStep = (d_ge(dt, 0.0) && d_gt(h, dt)) || (d_lt(dt, 0.0) && d_lt(h, dt));
+            hh = finalStep ? dt : h;
+            hr = (RateT)d2f_int(hh);
+          } else {
+            const double dt = t1 - t;
+            finalStep = (dt >= 0.0 && h > dt) || (dt < 0.0 && h < dt);
+            hh = finalStep ? dt : h;
+            hr = (RateT)hh;
+          }
         }
         // Argument of this evaluation: y, or y + h sum_j b_ij k_j (in the rate precision).
         switch (st) {
@@ -1143,8 +1159,8 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
         // FP64 error and the FP64 D_i.  (Picking at FP32 precision can only
         // exchange two components whose ratios agree to ~1e-7.)
         float errMaxF = 0.0f, dMaxF = 1.0f;
-        RateT estSel = (RateT)0, incSel = (RateT)0;
-        double ySel = 0.0, sSel = 1.0;
+        RateT estSel = (RateT)0, incSel = (RateT)0, sSel = (RateT)1;
+        double ySel = 0.0;
 #pragma unroll
         for (int i = 0; i < GAL_NY; ++i) {
           const RateT inc = (RateT)ck::c1 * k1[i] + (RateT)ck::c3 * k3[i] + (RateT)ck::c4 * k4[i] + (RateT)ck::c6 * k6[i];
@@ -1173,31 +1189,89 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
             sSel = s[i];
           }
         }
-        if constexpr (FAST) ySel += hh * (double)incSel;  // the picked component's new state, FP64
         // With nothing picked (every error zero) the ratio is 0, as in FP64.
-        const double errMax = fabs(hh * (double)estSel);
-        const double dMax = fabs(epsRel * fabs(ySel) + epsAbs * sSel);
-        const double rmax = dmax(fast_div(errMax, dMax), 2.2250738585072014e-308);  // floor DBL_MIN as cscal2.c
+        // (FP32-rate forms: the picked FP32 values are widened exactly on the
+        // integer pipe, f2d_int.)
+        double errMax, dMax;
+        if constexpr (FAST) {
+          ySel = fma(hh, f2d_int(incSel), ySel);  // the picked component's new state, FP64
+          errMax = fabs(hh * f2d_int(estSel));
+          dMax = fabs(epsRel * fabs(ySel) + epsAbs * f2d_int(sSel));
+        } else {
+          errMax = fabs(hh * (double)estSel);
+          dMax = fabs(epsRel * fabs(ySel) + epsAbs * (double)sSel);
+        }
         ++count;
-        const double tNew = finalStep ? t1 : t + hh;
         double hNew = hh;
         bool decrease = false;
         // 0.9 rmax^(-1/5), floored at 0.2 (reached for rmax >= 4.5^5 exactly),
         // and 0.9 rmax^(-1/6) capped at 4.9 (reached below (0.9/4.9)^6).
-        if (rmax > 1.1) {
-          double r = rmax > 1845.28125 ? 0.2 : 0.9 * inv_root<5>(rmax);
-          if (r < 0.2) r = 0.2;
-          hNew = r * hh;
-          decrease = true;
-        } else if (rmax < 0.5) {
-          double r = rmax < 3.8394e-5 ? 4.9 : 0.9 * inv_root<6>(rmax);
-          if (r > 4.9) r = 4.9;
-          if (r < 1.0) r = 1.0;
-          hNew = r * hh;
+        if constexpr (FAST) {
+          // The same decisions and values with the FP64 pipe used only for
+          // arithmetic: the comparisons of the (non-negative) ratio with the
+          // thresholds on the integer pipe, and the roots from the FP32
+          // ratio of the pick as seed (ctrl_root09).
+          const double q = errMax * rcp_seeded(dMax, dMaxF);
+          const double rmax = (d_isnan(q) || dpos_lt(q, 2.2250738585072014e-308)) ? 2.2250738585072014e-308 : q;
+          const float rF = __fdividef(errMaxF, dMaxF);
+          if (dpos_gt(rmax, 1.1)) {
+            double r = 0.2;
+            if (!dpos_gt(rmax, 1845.28125)) {
+              r = ctrl_root09<5>(rmax, rF);
+              if (__double2hiint(r) < 0) r = 0.9 * inv_root<5>(rmax);
+              if (dpos_lt(r, 0.2)) r = 0.2;
+            }
+            hNew = r * hh;
+            decrease = true;
+          } else if (dpos_lt(rmax, 0.5)) {
+            double r = 4.9;
+            if (!dpos_lt(rmax, 3.8394e-5)) {
+              r = ctrl_root09<6>(rmax, rF);
+              if (__double2hiint(r) < 0) r = 0.9 * inv_root<6>(rmax);
+              if (dpos_gt(r, 4.9)) r = 4.9;
+              if (dpos_lt(r, 1.0)) r = 1.0;
+            }
+            hNew = r * hh;
+          }
+        } else {
+          const double rmax = dmax(fast_div(errMax, dMax), 2.2250738585072014e-308);  // floor DBL_MIN as cscal2.c
+          if (rmax > 1.1) {
+            double r = rmax > 1845.28125 ? 0.2 : 0.9 * inv_root<5>(rmax);
+            if (r < 0.2) r = 0.2;
+            hNew = r * hh;
+            decrease = true;
+          } else if (rmax < 0.5) {
+            double r = rmax < 3.8394e-5 ? 4.9 : 0.9 * inv_root<6>(rmax);
+            if (r > 4.9) r = 4.9;
+            if (r < 1.0) r = 1.0;
+            hNew = r * hh;
+          }
         }
         if (decrease) {
-          const double tNext = tNew + hNew;
-          if (fabs(hNew) < fabs(hh) && tNext != tNew) {
+          // A smaller step that still moves t: |hNew| < |hh| and
+          // t_new + hNew != t_new.  In the FP32-rate forms the second test is
+          // settled by exponents when |hNew| is at least two ulps of every
+          // time involved (|t_new| <= 2 max(|t|, |t1|, |hh|)), else in FP64.
+          bool smaller, moves;
+          if constexpr (FAST) {
+            const long long hb = __double_as_longlong(hNew) & 0x7fffffffffffffffLL;
+            const long long hhb = __double_as_longlong(hh) & 0x7fffffffffffffffLL;
+            smaller = hb < hhb && hhb <= 0x7ff0000000000000LL;
+            const int eh = (int)(hb >> 52);
+            const int eT = 1 + max(max((__double2hiint(t) >> 20) & 0x7ff, (__double2hiint(t1) >> 20) & 0x7ff),
+                                   (int)(hhb >> 52));
+            if (smaller && eh >= 1 && eT < 0x7ff && eh >= eT - 51) {
+              moves = true;
+            } else {
+              const double tNew = finalStep ? t1 : t + hh;
+              moves = tNew + hNew != tNew;
+            }
+          } else {
+            const double tNew = finalStep ? t1 : t + hh;
+            smaller = fabs(hNew) < fabs(hh);
+            moves = tNew + hNew != tNew;
+          }
+          if (smaller && moves) {
             h = hNew;  // reject: retry from the same (t, y) with the smaller step
             ++nRej;
             if (budget && count >= budget) { finished = true; finalStatus = GAL_STATUS_XCPU; }
@@ -1213,6 +1287,9 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
           if constexpr (FAST) {
 #pragma unroll
             for (int i = 0; i < GAL_NY; ++i) {
+              // (The conversion instructions here: the integer-pipe ones of
+              // the controller cost more registers than they save in this
+              // twelve-fold loop -- measured.)
               y[i] += hh * (double)x[i];
               yf[i] = (float)y[i];
             }
@@ -1220,12 +1297,19 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
 #pragma unroll
             for (int i = 0; i < GAL_NY; ++i) y[i] = ynew[i];
           }
-          t = tNew;
+          t = finalStep ? t1 : t + hh;
           h = hNew;
           ++nAcc;
-          const bool reached = !(t1 - t > 0.0 || t1 - t < 0.0);
+          bool reached;
+          if constexpr (FAST) {
+            // !(t1 - t > 0 || t1 - t < 0): t1 - t is zero or NaN.
+            reached = d_isnan(t) || d_isnan(t1) || d_key(t) == d_key(t1);
+            dtLeft = t1 - t;
+          } else {
+            reached = !(t1 - t > 0.0 || t1 - t < 0.0);
+          }
           if (reached) {
-            post_step(y);
+            post_step_any(y);
             finished = true;
             bool finite = true;
 #pragma unroll

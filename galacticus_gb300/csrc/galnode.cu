@@ -204,9 +204,9 @@ cudaError_t dispatch(gal_ctx* ctx, const Batch& b, cudaStream_t st) {
   if ((mode & MODE_SURROGATE) && ctx->splitSurrogate && b.n <= (int64_t)INT32_MAX) {
     // The split launch: the nodes the network may serve go to the surrogate
     // kernel, the others to the kernel of the same rates without it, the two
-    // running at once on two streams (one block of each per SM).  The form
-    // without the network keeps its own registers and code: in one kernel
-    // with the network path it ran ~20% slower.
+    // running at once on two streams.  The form without the network keeps
+    // its own registers and code: in one kernel with the network path it ran
+    // ~20% slower.
     if (b.n > ctx->orderCap) {
       cudaFree(ctx->dOrder);
       ctx->dOrder = nullptr;
@@ -254,7 +254,14 @@ cudaError_t dispatch(gal_ctx* ctx, const Batch& b, cudaStream_t st) {
     t.sd = SurrogateDev{};
     t.sd.stats = ctx->dSurrStats;  // the table evaluations of these nodes
     t.shm = ctx_shared_bytes(ctx, tableMode);
-    t.blocks = std::max<int64_t>(1, std::min<int64_t>(ctx->smCount, (b.n + tableThreads - 1) / tableThreads));
+    // The table kernel takes most of the nodes, the hardest among them: it
+    // gets the context's blocks per SM, as the form alone does (a block
+    // that does not fit beside the network kernel's starts when that one's
+    // few nodes are done).
+    int tableBlocksPerSm = blocksPerSm;
+    while (tableBlocksPerSm > 1 && (size_t)tableBlocksPerSm * t.shm > 228 * 1024) --tableBlocksPerSm;
+    t.blocks = std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->smCount * tableBlocksPerSm,
+                                                      (b.n + tableThreads - 1) / tableThreads));
     t.stream = st;
     if ((e = evolve_launch(tableMode, tableThreads, t)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ctx->evJoin, ctx->stream2)) != cudaSuccess) return e;

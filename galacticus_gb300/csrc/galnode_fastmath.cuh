@@ -135,6 +135,104 @@ __device__ __forceinline__ double inv_root(double x) {
 __device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
 __device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
 
+// ---------------------------------------------------------------------------
+// Exact IEEE-754 comparisons of doubles on the integer pipe.  On GB300 every
+// FP64 instruction of a warp -- compare and conversion included -- holds
+// its SM sub-partition's FP64 pipe for ~64 cycles (an FP64 compare with its
+// select ~110), while a 64-bit integer compare takes a few cycles; a lone
+// node's step control is a chain of such compares.  Each function returns
+// what the IEEE comparison returns, NaNs (false for every ordered
+// comparison) and signed zeros (-0 == +0) included.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool d_isnan(double x) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+// Order-preserving key of a non-NaN double: a < b <=> d_key(a) < d_key(b),
+// with -0 mapped onto +0.
+__device__ __forceinline__ long long d_key(double x) {
+  long long b = __double_as_longlong(x);
+  if (b == (long long)0x8000000000000000ULL) b = 0;
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool d_lt(double a, double b) { return !(d_isnan(a) || d_isnan(b)) && d_key(a) < d_key(b); }
+__device__ __forceinline__ bool d_le(double a, double b) { return !(d_isnan(a) || d_isnan(b)) && d_key(a) <= d_key(b); }
+__device__ __forceinline__ bool d_gt(double a, double b) { return d_lt(b, a); }
+__device__ __forceinline__ bool d_ge(double a, double b) { return d_le(b, a); }
+// x < 0.0: sign bit set, not -0, not NaN.
+__device__ __forceinline__ bool d_neg(double x) {
+  const long long b = __double_as_longlong(x);
+  return b < 0 && b != (long long)0x8000000000000000ULL && (b & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL;
+}
+// Exact conversions between FP32 and FP64 on the integer pipe, for the
+// values that are normal in both formats (a conversion instruction holds
+// the FP64 pipe like an FP64 operation does).  float -> double: rebias the
+// exponent and shift the significand; zero keeps its sign; subnormals,
+// infinities and NaNs take the conversion instruction.
+__device__ __forceinline__ double f2d_int(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned a = u & 0x7fffffffu;
+  if (a - 0x00800000u >= 0x7f000000u) {  // zero, subnormal, infinity or NaN
+    if (a == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)f;
+  }
+  return __hiloint2double((int)((u & 0x80000000u) | ((a >> 3) + 0x38000000u)), (int)(u << 29));
+}
+// double -> float with round-to-nearest-even, for doubles whose float is
+// normal (a carry out of the largest float gives infinity, as the
+// conversion does); everything else takes the conversion instruction.
+__device__ __forceinline__ float d2f_int(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned ahi = hi & 0x7fffffffu;
+  if (ahi - 0x38100000u >= 0x0fe00000u) return (float)d;  // float exponent outside 1..254 (or inf/NaN)
+  unsigned f = ((ahi - 0x38000000u) << 3) | (lo >> 29);
+  const unsigned rem = lo & 0x1fffffffu;
+  f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;
+  return __uint_as_float(f | (hi & 0x80000000u));
+}
+// Comparisons of a non-negative, non-NaN double with a positive constant:
+// the bit patterns order as signed integers.
+__device__ __forceinline__ bool dpos_gt(double x, double c) { return __double_as_longlong(x) > __double_as_longlong(c); }
+__device__ __forceinline__ bool dpos_lt(double x, double c) { return __double_as_longlong(x) < __double_as_longlong(c); }
+
+// 0.9 x^(-1/Q) (Q = 5 or 6) for the step-size controller, to full FP64
+// precision, from the FP32 ratio xf ~ x that is at hand before x is.  The
+// seed g0 = xf^(-1/Q) is formed in FP32 (its error, from xf's and the FP32
+// functions', is ~1e-6); with e = 1 - x g0^Q, exactly
+// x^(-1/Q) = g0 (1 - e)^(-1/Q) = g0 (1 + e/Q + (1+Q) e^2/(2Q^2) + c3 e^3 + ...),
+// and for |e| < 2^-17 the terms from e^3 on are below 4e-17 relative, so the
+// series to e^2 gives the root to rounding.  FP64 work: one conversion, Q's
+// three products, four FMA/products -- against the two Newton steps of
+// inv_root, 12 operations after a conversion round trip.  Returns a
+// negative value when the seed is too far off (|e| >= 2^-17, or xf not a
+// usable float); the caller then takes inv_root.
+template <int Q>
+__device__ __forceinline__ double ctrl_root09(double x, float xf) {
+  if (!(xf > 1.0e-30f && xf < 1.0e30f)) return -1.0;
+  const double g0 = f2d_int(exp2f(-(1.0f / Q) * __log2f(xf)));
+  const double g2 = g0 * g0;  // exact: g0 has a 24-bit significand
+  const double gq = Q == 5 ? (g2 * g2) * g0 : (g2 * g0) * (g2 * g0);
+  const double e = fma(-x, gq, 1.0);
+  if ((__double2hiint(e) & 0x7fffffff) >= ((1023 - 17) << 20)) return -1.0;  // |e| >= 2^-17 (or NaN)
+  constexpr double c1 = 1.0 / Q, c2 = (1.0 + Q) / (2.0 * Q * Q);
+  const double u = e * fma(c2, e, c1);
+  return 0.9 * fma(g0, u, g0);
+}
+
+// 1/y to full FP64 precision from an FP32 approximation ys of y that is at
+// hand before y is: two Newton steps from the FP32 reciprocal of ys, with
+// no FP64<->FP32 conversion on the FP64 pipe.  Newton squares the relative
+// error, so the second step lands at rounding when the residual after the
+// first is below 2^-27; otherwise (a poor or unusable seed) fast_rcp.
+__device__ __forceinline__ double rcp_seeded(double y, float ys) {
+  if (!(ys > 1.0e-30f && ys < 1.0e30f) || !abs_exponent_in(y, -99, 99)) return fast_rcp(y);
+  double r = f2d_int(__frcp_rn(ys));
+  double e = fma(-y, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-y, r, 1.0);
+  if ((__double2hiint(e) & 0x7fffffff) >= ((1023 - 27) << 20)) return fast_rcp(y);  // |e| >= 2^-27 (or NaN)
+  return fma(r, e, r);
+}
+
 // Host-side construction of the tables.
 inline void fast_tables_host(double2* logTable, double* exp2Table) {
   for (int j = 0; j < kLogTableSize; ++j) {

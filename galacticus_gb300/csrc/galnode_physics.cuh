@@ -636,6 +636,16 @@ __device__ __forceinline__ bool post_step(double* y) {
   return true;
 }
 
+// post_step() with its test for a negative mass done on the integer pipe
+// (exact, d_neg), so that the usual case -- nothing to clamp -- issues no
+// FP64 compare.
+__device__ __forceinline__ bool post_step_int(double* y) {
+  if (!(d_neg(y[GAL_Y_HOT_MASS]) || d_neg(y[GAL_Y_DISK_GAS]) || d_neg(y[GAL_Y_DISK_STARS]) ||
+        d_neg(y[GAL_Y_SPHEROID_GAS]) || d_neg(y[GAL_Y_SPHEROID_STARS])))
+    return false;
+  return post_step(y);
+}
+
 // Absolute-tolerance scales from the initial state (scaleSetTask hooks of
 // hot_halo :804-850, disk :735-824, spheroid :804-897, black hole :195-257).
 __device__ __forceinline__ void scales(const double* y, double massHalo, double* s) {

@@ -23,8 +23,15 @@ int gal_calibrate_fp64(double* flops, double* ms);
  * over 4M arguments: reciprocal, quotient, reciprocal square root and square
  * root on 1e-29..1e29 (relative error), log on 1e-29..1e29 (error relative
  * to max(1, |ln x|)), exp on -120..5 (relative error) and the controller's inverse fifth
- * and sixth roots on 3e-5..1900 (relative error).  Writes the eight worst
- * errors to maxRelErr[0..7].  Returns 0 on success. */
+ * and sixth roots on 3e-5..1900 (relative error), then the FP32-rate
+ * controller's 0.9 x^(-1/5) and 0.9 x^(-1/6) from a seed ratio off by up to
+ * 3e-6 (relative error; [10] counts the arguments that needed the Newton
+ * fallback), and the integer-pipe comparisons and conversions of doubles
+ * and floats against the IEEE comparisons and the conversion instructions,
+ * on signed zeros, subnormals, infinities, NaNs and bit patterns spread
+ * over every exponent ([11] counts the disagreements).  Writes twelve values to maxRelErr[0..11]: the worst
+ * errors, and in [10] and [11] the largest per-thread counts.  Returns 0 on
+ * success. */
 int gal_selftest_fastmath(double* maxRelErr);
 
 #ifdef __cplusplus

@@ -145,8 +145,12 @@ def test_fastmath_helpers_are_full_precision():
     a few ulp of the CUDA library functions."""
     import ctypes
     lib = _abi.load_library()
-    err = (ctypes.c_double * 8)()
+    err = (ctypes.c_double * 12)()
     assert lib.gal_selftest_fastmath(err) == 0
-    names = ["rcp", "div", "rsqrt", "sqrt", "log", "exp", "inv_root5", "inv_root6"]
+    names = ["rcp", "div", "rsqrt", "sqrt", "log", "exp", "inv_root5", "inv_root6", "ctrl_root5", "ctrl_root6"]
     for name, e in zip(names, err):
         assert e < 2e-15, f"{name}: max error {e:.3g}"
+    # The FP32-seeded controller roots never needed their fallback, and the
+    # integer-pipe comparisons agree with IEEE ones on every pair.
+    assert err[10] == 0, f"controller root fallbacks: {err[10]:.0f}"
+    assert err[11] == 0, f"integer comparison disagreements: {err[11]:.0f}"
