@@ -285,6 +285,10 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
   static_assert(!KMT || !(MODE & MODE_SURROGATE), "krumholz2009 disks: the forms without a surrogate");
   constexpr bool SURR = (MODE & MODE_SURROGATE) != 0;
   constexpr bool FAST = (MODE & MODE_FAST) != 0;
+  // Step control with few FP64 instructions (integer-pipe compares, seeded
+  // reciprocal and roots): the FP32-rate batch forms.  The forest forms keep
+  // the plain controller: there it measured 3-4% slower (registers).
+  constexpr bool FASTCTL = FAST && !FOREST;
   using RateT = typename std::conditional<FAST, float, double>::type;
   extern __shared__ double2 smem[];
   const int nT = G.nT, nZ = G.nZ;
@@ -437,15 +441,18 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
   };
   // The FP32 copy of y in the FAST forms.
   auto sync_yr = [&]() {
-    if constexpr (FAST) {
+    if constexpr (FASTCTL) {
 #pragma unroll
       for (int v = 0; v < GAL_NY; ++v) yf[v] = d2f_int(y[v]);
+    } else if constexpr (FAST) {
+#pragma unroll
+      for (int v = 0; v < GAL_NY; ++v) yf[v] = (float)y[v];
     }
   };
   // The post-step clamps; the FP32-rate forms test for a negative mass on
   // the integer pipe first (post_step's FP64 compares only when one is).
   auto post_step_any = [&](double* yy) -> bool {
-    if constexpr (FAST) return post_step_int(yy);
+    if constexpr (FASTCTL) return post_step_int(yy);
     else return post_step(yy);
   };
 
@@ -1002,7 +1009,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
       if (__all_sync(FULL, phase == PH_DONE)) break;
 
       // ---- start (or restart) an ODE trial: odeSolverSolve + driver reset
-      if (phase == PH_TRIAL && (FAST ? !(d_isnan(t0) || d_isnan(t1)) && d_key(t0) == d_key(t1) : t0 == t1)) zero_interval();
+      if (phase == PH_TRIAL && (FASTCTL ? !(d_isnan(t0) || d_isnan(t1)) && d_key(t0) == d_key(t1) : t0 == t1)) zero_interval();
       const bool starting = phase == PH_TRIAL;
       if (starting) {
         const double stepSize = G.p.reuse_step_size ? stepIn / (double)(1u << trial) : -1.0;
@@ -1055,7 +1062,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
           }
           stepping = phase == PH_STEP && !finished;
           if (!any(stepping)) return false;
-          if constexpr (FAST) {
+          if constexpr (FASTCTL) {
             // The same last-step test with the compares on the integer pipe.
             const double dt = dtLeft;
             finalStep = (d_ge(dt, 0.0) && d_gt(h, dt)) || (d_lt(dt, 0.0) && d_lt(h, dt));
@@ -1190,14 +1197,15 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
           }
         }
         // With nothing picked (every error zero) the ratio is 0, as in FP64.
-        // (FP32-rate forms: the picked FP32 values are widened exactly on the
-        // integer pipe, f2d_int.)
+        // (FP32-rate batch forms: the picked FP32 values are widened exactly
+        // on the integer pipe, f2d_int.)
         double errMax, dMax;
-        if constexpr (FAST) {
+        if constexpr (FASTCTL) {
           ySel = fma(hh, f2d_int(incSel), ySel);  // the picked component's new state, FP64
           errMax = fabs(hh * f2d_int(estSel));
           dMax = fabs(epsRel * fabs(ySel) + epsAbs * f2d_int(sSel));
         } else {
+          if constexpr (FAST) ySel += hh * (double)incSel;  // the picked component's new state, FP64
           errMax = fabs(hh * (double)estSel);
           dMax = fabs(epsRel * fabs(ySel) + epsAbs * (double)sSel);
         }
@@ -1206,7 +1214,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
         bool decrease = false;
         // 0.9 rmax^(-1/5), floored at 0.2 (reached for rmax >= 4.5^5 exactly),
         // and 0.9 rmax^(-1/6) capped at 4.9 (reached below (0.9/4.9)^6).
-        if constexpr (FAST) {
+        if constexpr (FASTCTL) {
           // The same decisions and values with the FP64 pipe used only for
           // arithmetic: the comparisons of the (non-negative) ratio with the
           // thresholds on the integer pipe, and the roots from the FP32
@@ -1253,7 +1261,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
           // settled by exponents when |hNew| is at least two ulps of every
           // time involved (|t_new| <= 2 max(|t|, |t1|, |hh|)), else in FP64.
           bool smaller, moves;
-          if constexpr (FAST) {
+          if constexpr (FASTCTL) {
             const long long hb = __double_as_longlong(hNew) & 0x7fffffffffffffffLL;
             const long long hhb = __double_as_longlong(hh) & 0x7fffffffffffffffLL;
             smaller = hb < hhb && hhb <= 0x7ff0000000000000LL;
@@ -1301,7 +1309,7 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
           h = hNew;
           ++nAcc;
           bool reached;
-          if constexpr (FAST) {
+          if constexpr (FASTCTL) {
             // !(t1 - t > 0 || t1 - t < 0): t1 - t is zero or NaN.
             reached = d_isnan(t) || d_isnan(t1) || d_key(t) == d_key(t1);
             dtLeft = t1 - t;
