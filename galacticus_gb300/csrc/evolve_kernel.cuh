@@ -71,9 +71,13 @@ struct Batch {
   double* tReached;
   int32_t* task;
   // Optional work list (the surrogate forms' split launch): when set, the
-  // queue walks order[0 .. *orderCount) instead of 0 .. n.
+  // queue walks order[0 .. *orderCount) instead of 0 .. n, and then, when
+  // orderBackCount is set, the *orderBackCount entries written from the
+  // list's far end down: order[orderCap - 1], order[orderCap - 2], ...
   const int32_t* order;
   const unsigned long long* orderCount;
+  const unsigned long long* orderBackCount;
+  int64_t orderCap;
 };
 
 // Device tables: the FP64 forms read gTab/gLnT/gLnZ/gFastLog/gFastExp, the
@@ -342,7 +346,8 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
   if constexpr (SURR) N = surrogate_view(sSmall, sPlanes);
 
   const int64_t n = b.n;
-  const int64_t nWork = (!FOREST && b.order) ? (int64_t)*b.orderCount : n;
+  const int64_t nFront = (!FOREST && b.order) ? (int64_t)*b.orderCount : n;
+  const int64_t nWork = nFront + ((!FOREST && b.order && b.orderBackCount) ? (int64_t)*b.orderBackCount : 0);
   const double epsAbs = G.p.ode_tolerance_absolute, epsRel = G.p.ode_tolerance_relative;
   const float epsAbsF = (float)epsAbs, epsRelF = (float)epsRel;
   const uint32_t budget = (uint32_t)max(G.p.step_budget, 0);
@@ -560,7 +565,8 @@ evolve_kernel(const __grid_constant__ Globals G, Batch b, const __grid_constant_
         phase = PH_DONE;
         return;
       }
-      node = b.order ? (int64_t)b.order[idx] : (int64_t)idx;
+      node = !b.order ? (int64_t)idx
+                      : (int64_t)b.order[(int64_t)idx < nFront ? (int64_t)idx : b.orderCap - 1 - ((int64_t)idx - nFront)];
       double prm[GAL_NP];
 #pragma unroll
       for (int v = 0; v < GAL_NP; ++v) prm[v] = b.param[v * n + node];

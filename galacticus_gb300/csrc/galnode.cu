@@ -152,15 +152,42 @@ void effective_shape(const gal_ctx* ctx, int mode, int& threads, int& blocksPerS
 
 namespace {
 
+// Work estimate of a node for the order in which the table kernel of the
+// split launch takes its nodes: the number of dynamical times in its
+// interval times the disk's outflow mass loading (V_out/V_vir)^alpha_out.
+// On the 65,536-halo isolated batch it tracks the right-hand-side count
+// (mean 7, 15, 29 and 55 evaluations for estimates below 1, 1-10, 10-100
+// and above 100; the batch's hardest halo, 1,061 evaluations, ranks 49th),
+// and nodes at or above kFrontWork (about a fifth of that batch) are
+// queued first, so that the long integrations start in the first wave of a
+// kernel that shares the GPU with the network kernel.  It only orders the
+// queue: a node's result does not depend on it.
+constexpr float kFrontWork = 10.0f;
+
+__device__ __forceinline__ float work_estimate(const Globals& G, const double* param, const double* tStart,
+                                               const double* tEnd, int64_t n, int64_t i) {
+  const float v = (float)param[GAL_P_VELOCITY_VIRIAL * n + i], r = (float)param[GAL_P_RADIUS_VIRIAL * n + i];
+  const float dt = (float)(tEnd[i] - tStart[i]);
+  const float tdyn = r / v * (float)k::MpcPerKmPerSToGyr;
+  const float loading = G.p.outflow_disk.type == GAL_OUTFLOW_POWER_LAW
+                            ? __powf((float)G.p.outflow_disk.velocity_characteristic / v, (float)G.p.outflow_disk.exponent)
+                            : 1.0f;
+  const float w = fabsf(dt) / tdyn * loading;
+  return w == w ? w : 0.0f;
+}
+
 // The surrogate forms' split launch, step 1: sort the batch into the nodes
 // the network may serve at their starting state (surrogate_open: a T row
 // with network cells, hot gas, a metallicity in a cell the error map leaves
 // to the network) and the others.  Lists in order of arrival (warp-
-// aggregated atomics): a node's result does not depend on its place.
+// aggregated atomics); in the table list the nodes with a work estimate at
+// or above kFrontWork go to its front, the others fill it from its far end
+// down.  A node's result does not depend on its place.
 template <bool FAST>
 __global__ void surrogate_classify(const __grid_constant__ Globals G, const __grid_constant__ SurrogateInfo I,
-                                   const uint8_t* map, const double* param, const double* state, int64_t n,
-                                   int32_t* orderTable, int32_t* orderNet, unsigned long long* counts) {
+                                   const uint8_t* map, const double* param, const double* state, const double* tStart,
+                                   const double* tEnd, int64_t n, int64_t cap, int32_t* orderTable, int32_t* orderNet,
+                                   unsigned long long* counts) {
   const int lane = threadIdx.x & 31;
   for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = i0 + threadIdx.x;
@@ -181,20 +208,25 @@ __global__ void surrogate_classify(const __grid_constant__ Globals G, const __gr
       const double y[2] = {state[GAL_Y_HOT_MASS * n + i], state[GAL_Y_HOT_METALS * n + i]};
       open = surrogate_open(I, map, c, y);
     }
+    const bool front = i < n && !open && work_estimate(G, param, tStart, tEnd, n, i) >= kFrontWork;
     const unsigned active = __ballot_sync(FULL, i < n);
     const unsigned net = __ballot_sync(FULL, open);
-    const unsigned tab = active & ~net;
-    unsigned long long baseNet = 0, baseTab = 0;
+    const unsigned tabFront = __ballot_sync(FULL, front);
+    const unsigned tabBack = active & ~net & ~tabFront;
+    unsigned long long baseNet = 0, baseFront = 0, baseBack = 0;
     if (lane == 0) {
       if (net) baseNet = atomicAdd(&counts[1], (unsigned long long)__popc(net));
-      if (tab) baseTab = atomicAdd(&counts[0], (unsigned long long)__popc(tab));
+      if (tabFront) baseFront = atomicAdd(&counts[0], (unsigned long long)__popc(tabFront));
+      if (tabBack) baseBack = atomicAdd(&counts[4], (unsigned long long)__popc(tabBack));
     }
     baseNet = __shfl_sync(FULL, baseNet, 0);
-    baseTab = __shfl_sync(FULL, baseTab, 0);
+    baseFront = __shfl_sync(FULL, baseFront, 0);
+    baseBack = __shfl_sync(FULL, baseBack, 0);
     const unsigned below = (1u << lane) - 1u;
     if (i < n) {
       if (open) orderNet[baseNet + __popc(net & below)] = (int32_t)i;
-      else orderTable[baseTab + __popc(tab & below)] = (int32_t)i;
+      else if (front) orderTable[baseFront + __popc(tabFront & below)] = (int32_t)i;
+      else orderTable[cap - 1 - (int64_t)(baseBack + __popc(tabBack & below))] = (int32_t)i;
     }
   }
 }
@@ -217,16 +249,17 @@ cudaError_t dispatch(gal_ctx* ctx, const Batch& b, cudaStream_t st) {
     }
     int32_t* orderTable = ctx->dOrder;
     int32_t* orderNet = ctx->dOrder + ctx->orderCap;
-    unsigned long long* counts = ctx->dOrderCount;  // [0] table list, [1] network list, [2], [3] queue heads
-    cudaError_t e = cudaMemsetAsync(counts, 0, 4 * sizeof(unsigned long long), st);
+    // [0] table list (front), [1] network list, [2], [3] queue heads, [4] table list (back)
+    unsigned long long* counts = ctx->dOrderCount;
+    cudaError_t e = cudaMemsetAsync(counts, 0, 5 * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
     const int cb = (int)std::min<int64_t>((b.n + 255) / 256, (int64_t)ctx->smCount * 8);
     if (mode & MODE_FAST)
-      surrogate_classify<true><<<cb, 256, 0, st>>>(ctx->globals, ctx->surrInfo, ctx->dSurrMap, b.param, b.state, b.n,
-                                                   orderTable, orderNet, counts);
+      surrogate_classify<true><<<cb, 256, 0, st>>>(ctx->globals, ctx->surrInfo, ctx->dSurrMap, b.param, b.state,
+                                                   b.tStart, b.tEnd, b.n, ctx->orderCap, orderTable, orderNet, counts);
     else
-      surrogate_classify<false><<<cb, 256, 0, st>>>(ctx->globals, ctx->surrInfo, ctx->dSurrMap, b.param, b.state, b.n,
-                                                    orderTable, orderNet, counts);
+      surrogate_classify<false><<<cb, 256, 0, st>>>(ctx->globals, ctx->surrInfo, ctx->dSurrMap, b.param, b.state,
+                                                    b.tStart, b.tEnd, b.n, ctx->orderCap, orderTable, orderNet, counts);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ctx->evFork, st)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(ctx->stream2, ctx->evFork, 0)) != cudaSuccess) return e;
@@ -250,6 +283,8 @@ cudaError_t dispatch(gal_ctx* ctx, const Batch& b, cudaStream_t st) {
     LaunchArgs t = a;
     t.b.order = orderTable;
     t.b.orderCount = counts;
+    t.b.orderBackCount = counts + 4;
+    t.b.orderCap = ctx->orderCap;
     t.b.queue = counts + 2;
     t.sd = SurrogateDev{};
     t.sd.stats = ctx->dSurrStats;  // the table evaluations of these nodes
@@ -449,7 +484,7 @@ int gal_gpu_init(const gal_params* p, const gal_cie_table* t, gal_ctx** out) {
       cudaMalloc(&ctx->dKmt, (kmt::kFractionCount + kmt::kPowerCount) * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&ctx->dKmtF, (kmt::kFractionCount + kmt::kPowerCount) * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&ctx->dQueue, sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMalloc(&ctx->dOrderCount, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&ctx->dOrderCount, 5 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->evFork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->evJoin, cudaEventDisableTiming) != cudaSuccess) {

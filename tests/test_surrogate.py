@@ -111,6 +111,10 @@ def test_split_launch_matches_one_kernel(trained, table):
     ev.close()
     same = np.all(out[True][0] == out[False][0], axis=0)
     assert same.mean() > 0.95
+    # Every node was taken exactly once from the split lists (the table list
+    # is filled from both ends: long integrations at its front).
+    assert np.all(out[True][1][2] > 0)
+    np.testing.assert_allclose(out[True][1][0].sum(), out[False][1][0].sum(), rtol=0.01)
     for split in (True, False):
         net, tab = out[split][2]
         assert net + tab == int(out[split][1][2].sum())
