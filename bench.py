@@ -49,7 +49,13 @@ UNIT = "node-timesteps/s"
 N_NODES = 65536
 WORKLOAD = "isolated-halo step: 65,536 halos/GPU, M 1e10-1e14 Msun, dt 0.01-1 Gyr, rel tol 1e-3, P-std physics"
 TREES_WORKLOAD = ("uneven trees: {} PCH trees (seed 3), roots dN/dlnM ~ M^-0.9 on 1e10-1e14 Msun, resolution "
-                  "1e8 Msun, z=8->0 with 20 outputs, rel tol 1e-3")
+                  "1e8 Msun, z=8->0 with 20 outputs, rel tol 1e-3{}")
+SATELLITES = {"jiang2008": 1, "none": 0}
+
+
+def satellite_note(args):
+    return ("; satellites merge after the Jiang et al. (2008) time (x0.75) on Benson (2005) orbits"
+            if args.satellites == "jiang2008" else "; secondary progenitors merge at their parent's time")
 # Error-map gates tried for the surrogate form (dex), loose to tight; the
 # table alone comes after them.
 GATES = (0.01, 0.003, 0.001, 0.0003, 0.0001)
@@ -77,6 +83,8 @@ def parse():
     ap.add_argument("--workload", choices=["isolated", "scale"], default="isolated",
                     help="scale: the full chosen form on a forest at scale (one JSON line of its own)")
     ap.add_argument("--trees-scale", type=int, default=65536, help="trees of the scale workload (0: skip it)")
+    ap.add_argument("--satellites", choices=sorted(SATELLITES), default="jiang2008",
+                    help="forests: satellites as the reference's default classes have them, or none")
     ap.add_argument("--halo", type=int, default=-1,
                     help="with a single --form: evolve only this halo of the batch (profiling the batch's tail)")
     return ap.parse_args()
@@ -314,12 +322,12 @@ def run_trees(args, params, table, net, gate, rank, dist, device):
     t0 = time.perf_counter()
     # One forest of `trees` per rank (seed 3), split over the ranks by
     # longest processing time first on node counts (weak scaling).
-    f_all = forest.build(params, n_trees=args.trees * world, seed=3)
+    f_all = forest.build(params, n_trees=args.trees * world, seed=3, satellites=SATELLITES[args.satellites])
     f, _ = forest.partition(f_all, rank, world)
     build_s = time.perf_counter() - t0
     state0 = forest.initial_state(params, f)
     times = forest.output_times(params)
-    out = {"workload": TREES_WORKLOAD.format(args.trees * world), "nodes": f.n, "leaves": int((f.child_count == 0).sum()),
+    out = {"workload": TREES_WORKLOAD.format(args.trees * world, satellite_note(args)), "nodes": f.n, "leaves": int((f.child_count == 0).sum()),
            "max_tree_nodes": int(np.bincount(f.tree).max()), "build_s": build_s,
            "split": f"{world} rank(s), trees assigned longest processing time first by node count",
            "graph": "one CUDA graph per evolution: counter reset, leaf-queue reset, one persistent kernel",
@@ -393,12 +401,13 @@ def scale_record(args, params, table, net, gate):
     from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
     from oracle import oracle
     t0 = time.perf_counter()
-    f = forest.build(params, n_trees=args.trees_scale, seed=5, redshift_max=10.0)
+    f = forest.build(params, n_trees=args.trees_scale, seed=5, redshift_max=10.0, satellites=SATELLITES[args.satellites])
     build_s = time.perf_counter() - t0
     state0 = forest.initial_state(params, f)
     times = forest.output_times(params, n=50, redshift_max=10.0)
     out = {"workload": f"scale: {args.trees_scale} PCH trees (seed 5), roots dN/dlnM ~ M^-0.9 on 1e10-1e14 Msun, "
-                       f"resolution 1e8 Msun, z=10->0 with 50 outputs, rel tol 1e-3", "metric": METRIC, "unit": UNIT,
+                       f"resolution 1e8 Msun, z=10->0 with 50 outputs, rel tol 1e-3{satellite_note(args)}",
+           "metric": METRIC, "unit": UNIT,
            "nodes": f.n, "leaves": int((f.child_count == 0).sum()), "max_tree_nodes": int(np.bincount(f.tree).max()),
            "build_s": build_s, "timing": "host clock around one graph launch and its completion, after one warm-up",
            "forms": {}}
@@ -612,7 +621,8 @@ def run_ours(args):
         if name == "surrogate":
             net.build_error_map(table, tolerance=args.gate)
             net.install(ev)
-        f, _ = forest_mod.partition(forest_mod.build(params, n_trees=args.trees * world, seed=3), rank, world)
+        f, _ = forest_mod.partition(forest_mod.build(params, n_trees=args.trees * world, seed=3,
+                                                     satellites=SATELLITES[args.satellites]), rank, world)
         fe = forest_mod.ForestEvolver(ev, f, forest_mod.initial_state(params, f), forest_mod.output_times(params))
         for _ in range(args.warmup):
             fe.evolve()

@@ -192,7 +192,8 @@ extern "C" {
 
 int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const int32_t* childFirst,
                           const int32_t* childCount, const double* time, const double* mass, const double* spin,
-                          const double* state0, int32_t nOut, const double* tOut, gal_forest_dev** out) {
+                          const int32_t* satHost, const double* state0, int32_t nOut, const double* tOut,
+                          gal_forest_dev** out) {
   if (!out) return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: out is NULL%s");
   *out = nullptr;
   if (!ctx) return fail(nullptr, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: NULL context%s");
@@ -210,7 +211,16 @@ int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const 
     for (int32_t c = 0; c < childCount[i]; ++c)
       if (parent[childFirst[i] + c] != (int32_t)i)
         return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: progenitors must be contiguous%s");
+    if (satHost && (satHost[i] < -1 || satHost[i] >= n || (satHost[i] >= 0 && time[satHost[i]] != time[i])))
+      return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: a satellite's host must be a node of its infall time%s");
   }
+  // The mass each node gains at its own time from the satellites that fall
+  // into it (their halos join its halo there).
+  std::vector<double> massIn((size_t)n, 0.0);
+  if (satHost)
+    for (int64_t i = 0; i < n; ++i)
+      if (satHost[i] >= 0) massIn[(size_t)satHost[i]] += mass[i];
+  auto isSatellite = [&](int64_t i) { return satHost && satHost[i] >= 0; };
   const gal_params& p = ctx->params;
   const HostCosmology cos{p.omega_matter, p.omega_dark_energy, p.hubble_constant};
   std::vector<int32_t> leaves, pending0(n), segFirst(n), segCount(n), snapInitial(n, -1), segSnap;
@@ -225,13 +235,19 @@ int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const 
     const int32_t par = parent[i];
     const double t0 = time[i], t1 = par >= 0 ? time[par] : time[i];
     const bool primary = par >= 0 && childFirst[par] == (int32_t)i;
+    // The primary progenitor grows by its parent's unresolved mass (the
+    // parent's mass beyond its progenitors' and the satellites falling in);
+    // other progenitors and satellites keep theirs and accrete nothing.
     double massEnd = mass[i], accretion = 0.0;
-    if (primary && t1 > t0) {
-      massEnd = mass[par];
-      double brought = 0.0;
-      for (int32_t c = 0; c < childCount[par]; ++c) brought += mass[childFirst[par] + c];
+    if (primary && t1 > t0 && !isSatellite(i)) {
+      double brought = massIn[(size_t)par];
+      for (int32_t c = 0; c < childCount[par]; ++c)
+        if (!isSatellite(childFirst[par] + c)) brought += mass[childFirst[par] + c];
       accretion = std::max(mass[par] - brought, 0.0) / (t1 - t0);
+      massEnd = mass[i] + accretion * (t1 - t0);
     }
+    // A satellite's virial scales are those of its infall time.
+    const double zFrozen = isSatellite(i) ? cos.redshift(t0) : 0.0;
     // Snapshot slots: outputs at the node's own time, then inside its interval.
     for (int32_t k = 0; k < nOut; ++k)
       if (tOut[k] == t0 && (par < 0 || t0 < t1)) {
@@ -251,7 +267,7 @@ int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const 
       const double b = atOutput ? tOut[k] : std::min(limit, t1);
       const double M = mass[i] + (massEnd - mass[i]) * (a - t0) / (t1 - t0);
       double r, v;
-      cos.virial(M, cos.redshift(a), r, v);
+      cos.virial(M, isSatellite(i) ? zFrozen : cos.redshift(a), r, v);
       segParam[GAL_P_MASS].push_back(M);
       segParam[GAL_P_MASS_RATE].push_back(accretion);
       segParam[GAL_P_RADIUS_VIRIAL].push_back(r);

@@ -458,10 +458,216 @@ uint64_t splitmix64(uint64_t x) {
   return x ^ (x >> 31);
 }
 
+// Virial radius (Mpc) and velocity (km/s) of a halo of mass M at redshift z
+// in the flat matter + Lambda cosmology, with the Bryan & Norman (1998)
+// contrast relative to the mean density (the forest's segment constants use
+// the same relation).
+void virial(const Cosmo& c, double M, double z, double& r, double& v) {
+  const double zp = (1.0 + z) * (1.0 + z) * (1.0 + z);
+  const double omz = c.om * zp / (c.om * zp + c.ol);
+  const double x = omz - 1.0;
+  const double contrast = (18.0 * kPi * kPi + 82.0 * x - 39.0 * x * x) / (x + 1.0);
+  const double rhoMean = c.om * 3.0 * c.h0 * c.h0 / (8.0 * kPi * kGravity) * zp;
+  r = std::cbrt(3.0 * M / (4.0 * kPi * contrast * rhoMean));
+  v = std::sqrt(kGravity * M / r);
+}
+
+// Jiang et al. (2008) merging time of a satellite on an orbit with radial
+// and tangential velocities (ur, ut) at the host's virial radius, in units
+// of the host's virial velocity (satelliteMergingTimescalesJiang2008%
+// timeUntilMerging, satellites/merging/timescale/Jiang2008.F90): with the
+// orbit's energy E = -1 + (ur^2 + ut^2) mu/2 (units of V_vir^2, mu =
+// M_host/(M_host + M_sat) the specific reduced mass, as the reference's
+// virial-orbit sampler forms it), the circular orbit of the same energy in
+// a singular isothermal host truncated at r_vir (point mass beyond it) has
+// radius r_c = r_vir exp(E + 1/2) (E <= -1/2) or r_vir/(-2E), and the
+// orbit's circularity is its angular momentum r_vir ut V_vir over
+// r_c V_c(r_c).  Negative for an unbound orbit.
+double jiang2008_time(double tdyn, double q, double mu, double ur, double ut, double multiplier) {
+  const double E = -1.0 + 0.5 * mu * (ur * ur + ut * ut);
+  if (!(E < 0.0)) return -1.0;
+  double rc, eps;
+  if (E <= -0.5) {
+    rc = std::exp(E + 0.5);
+    eps = ut / rc;
+  } else {
+    rc = -0.5 / E;
+    eps = ut * std::sqrt(1.0 / rc);
+  }
+  constexpr double C = 0.43, a = 0.94, b = 0.60, d = 0.60;  // Jiang et al. (2008), eq. 5
+  if (!(q > 0.0)) return 0.0;
+  return multiplier * tdyn * std::sqrt(rc) * ((a * std::pow(eps, b) + d) / (2.0 * C)) * q / std::log1p(q);
+}
+
+// An orbit from the Benson (2005, MNRAS 358, 551) distribution of radial and
+// tangential velocities of infalling satellites at the host's virial radius
+// (units of its virial velocity), by rejection as virialOrbitBenson2005%orbit
+// does (satellites/merging/virial_orbits/Benson2005.F90): velocities uniform
+// on [0, 3], accepted with probability f(ur, ut)/f_max, bound orbits only
+// (E < -1e-4).  The fit's coefficients are the paper's.
+void benson2005_orbit(std::mt19937_64& rng, double mu, double& ur, double& ut) {
+  constexpr double pMax = 1.96797, velocityMax = 3.0;
+  constexpr double a[9] = {3.90052, 2.47973, 10.2373, 0.683922, 0.353953, 1.07716, 0.509837, 0.206204, 0.314641};
+  std::uniform_real_distribution<double> U(0.0, 1.0);
+  for (int attempt = 0; attempt < 1000000; ++attempt) {
+    ur = U(rng) * velocityMax;
+    ut = U(rng) * velocityMax;
+    const double b1 = a[2] * std::exp(-a[3] * (ut - a[4]) * (ut - a[4]));
+    const double b2 = a[5] * std::exp(-a[6] * (ut - a[7]) * (ut - a[7]));
+    const double f = a[0] * ut * std::exp(-a[1] * (ut - a[8]) * (ut - a[8])) * std::exp(-b1 * (ur - b2) * (ur - b2));
+    if (pMax * U(rng) <= f && -1.0 + 0.5 * mu * (ur * ur + ut * ut) < -1.0e-4) return;
+  }
+  ur = 0.0;  // not reached for the fit's distribution: a circular orbit
+  ut = 1.0;
+}
+
+// One tree as built (children contiguous, primary first), with node times.
+struct TreeIn {
+  const std::vector<Builder::Node>* nodes;
+  std::vector<double> time;
+};
+
+// A node of a tree with satellites before it is laid out.
+struct SatNode {
+  double mass, time, spin;
+  int32_t parent, satHost;  // satHost: the host at infall of a satellite phase, else -1
+  std::vector<int32_t> children;  // primary first
+};
+
+// Satellites as the reference's tree evolver has them (merger_trees/
+// evolver/standard.F90: a secondary progenitor becomes a satellite at its
+// parent's time and merges when its merging time runs out): each secondary
+// progenitor s of a node p gets a node S, its satellite phase (time t_p,
+// its halo's mass, s as its only progenitor), and a merging time t_m = t_p
+// + tau on a Benson (2005) orbit in the primary progenitor (its host at
+// infall, satelliteMergingTimescalesJiang2008 with node%parent%firstChild as
+// the host and q = M_host/M_sat).  The host at t_m is the node alive then
+// on p's line of descendants (the halo that holds the satellite, through
+// its own infall into a larger halo, as the reference moves satellites of
+// satellites to the new host); that node is cut at t_m into the piece
+// before and a piece from t_m on whose progenitors are the piece before
+// (primary) and the satellites merging at t_m.  A satellite that outlives
+// the tree ends in a root of its own at the tree's final time.  The host's
+// mass line is kept: the piece from t_m starts at the mass its halo has
+// reached by then.
+void add_satellites(const TreeIn& in, const std::vector<double>& spin, const Cosmo& c, double multiplier,
+                    std::mt19937_64& rng, std::vector<SatNode>& out) {
+  const std::vector<Builder::Node>& tr = *in.nodes;
+  const int32_t n = (int32_t)tr.size();
+  const std::vector<double>& t = in.time;
+  out.clear();
+  out.reserve((size_t)n * 2);
+  for (int32_t i = 0; i < n; ++i) out.push_back(SatNode{tr[i].mass, t[i], spin[i], tr[i].parent, -1, {}});
+  for (int32_t i = 0; i < n; ++i)
+    for (int32_t k = 0; k < tr[i].childCount; ++k) out[i].children.push_back(tr[i].childFirst + k);
+  // The halo mass a node reaches by time x (its mass line: a primary
+  // progenitor grows by its parent's unresolved mass, others stay).
+  auto massAt = [&](int32_t i, double x) {
+    const int32_t p = tr[i].parent;
+    if (p < 0 || tr[p].childFirst != i || !(t[p] > t[i])) return tr[i].mass;
+    double brought = 0.0;
+    for (int32_t k = 0; k < tr[p].childCount; ++k) brought += tr[tr[p].childFirst + k].mass;
+    const double unresolved = std::max(tr[p].mass - brought, 0.0);
+    return tr[i].mass + unresolved * (x - t[i]) / (t[p] - t[i]);
+  };
+  int32_t root = 0;
+  while (tr[root].parent >= 0) root = tr[root].parent;
+  const double tEnd = t[root];
+  struct Event { double tm; int32_t sat; };
+  std::vector<std::vector<Event>> events((size_t)n);  // merging events on each original node
+  std::vector<int32_t> unmerged;
+  for (int32_t p = 0; p < n; ++p) {
+    if (tr[p].childCount < 2) continue;
+    const int32_t c0 = tr[p].childFirst;
+    double massSat = 0.0;
+    for (int32_t k = 1; k < tr[p].childCount; ++k) massSat += tr[c0 + k].mass;
+    // The host at infall: the primary progenitor at t_p.
+    const double massHost = std::max(tr[p].mass - massSat, tr[c0].mass);
+    double rv, vv;
+    virial(c, massHost, std::max(c.redshift(t[p]), 0.0), rv, vv);
+    const double tdyn = rv / vv * kMpcPerKmPerSToGyr;
+    std::vector<int32_t> kept{c0};  // p's progenitors: the primary, and satellites that merge at once
+    for (int32_t k = 1; k < tr[p].childCount; ++k) {
+      const int32_t s = c0 + k;
+      const double ms = tr[s].mass, mu = massHost / (massHost + ms);
+      double ur, ut;
+      benson2005_orbit(rng, mu, ur, ut);
+      double tau = jiang2008_time(tdyn, massHost / ms, mu, ur, ut, multiplier);
+      const double tm = tau < 0.0 ? HUGE_VAL : t[p] + tau;
+      if (!(tm > t[p])) {
+        kept.push_back(s);
+        continue;
+      }
+      // The satellite phase S replaces s among p's progenitors.
+      const int32_t S = (int32_t)out.size();
+      out.push_back(SatNode{ms, t[p], spin[s], -1, p, {s}});
+      out[s].parent = S;
+      // The node alive at t_m on p's line of descendants.
+      int32_t d = p;
+      while (tr[d].parent >= 0 && !(tm < t[tr[d].parent])) d = tr[d].parent;
+      if (tr[d].parent < 0 && !(tm < tEnd)) unmerged.push_back(S);
+      else events[d].push_back(Event{tm, S});
+    }
+    out[p].children = kept;  // the satellites' phases hang from their merging pieces
+  }
+  // Cut each host node at its merging times.
+  for (int32_t d = 0; d < n; ++d) {
+    std::vector<Event>& ev = events[d];
+    if (ev.empty()) continue;
+    std::stable_sort(ev.begin(), ev.end(), [](const Event& a, const Event& b) { return a.tm < b.tm; });
+    const int32_t par = out[d].parent;
+    int32_t prev = d;
+    size_t j = 0;
+    // Mergers at the node's own time join its progenitors directly.
+    while (j < ev.size() && !(ev[j].tm > t[d])) {
+      out[ev[j].sat].parent = d;
+      out[d].children.push_back(ev[j].sat);
+      ++j;
+    }
+    while (j < ev.size()) {
+      const double tm = ev[j].tm;
+      const int32_t J = (int32_t)out.size();
+      out.push_back(SatNode{massAt(d, tm), tm, spin[d], -1, -1, {prev}});
+      out[prev].parent = J;
+      for (; j < ev.size() && ev[j].tm == tm; ++j) {
+        out[ev[j].sat].parent = J;
+        out[J].children.push_back(ev[j].sat);
+      }
+      prev = J;
+    }
+    // The last piece takes the node's place among its parent's progenitors.
+    out[prev].parent = par;
+    if (par >= 0)
+      for (int32_t& ch : out[par].children)
+        if (ch == d) ch = prev;
+  }
+  // Satellites that outlive the tree: a root of their own at its final time.
+  for (int32_t S : unmerged) {
+    if (!(tEnd > out[S].time)) continue;  // fell in at the final time: S is the root
+    const int32_t E = (int32_t)out.size();
+    out.push_back(SatNode{out[S].mass, tEnd, out[S].spin, -1, -1, {S}});
+    out[S].parent = E;
+  }
+}
+
+// Lay a tree with satellites out as the forest layout wants it: roots
+// first (the tree's own root, then the roots of satellites that outlive
+// it), then breadth first, so that each node's progenitors are contiguous
+// with the primary first.  Returns the order of the nodes.
+std::vector<int32_t> layout(const std::vector<SatNode>& nodes) {
+  std::vector<int32_t> order;
+  order.reserve(nodes.size());
+  for (int32_t i = 0; i < (int32_t)nodes.size(); ++i)
+    if (nodes[i].parent < 0) order.push_back(i);
+  for (size_t q = 0; q < order.size(); ++q)
+    for (int32_t ch : nodes[order[q]].children) order.push_back(ch);
+  return order;
+}
+
 }  // namespace
 
 struct gal_forest {
-  std::vector<int32_t> tree, parent, childFirst, childCount;
+  std::vector<int32_t> tree, parent, childFirst, childCount, satHost;
   std::vector<double> time, mass, spin;
 };
 
@@ -536,11 +742,17 @@ int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_f
   rt.build(Rates{sig, *pch, spec->mass_resolution}, spec->root_mass_max);
   const Builder B{sig, *pch, spec->mass_resolution, gt.w_of_z(spec->redshift_max), rt};
   const int64_t nTrees = spec->n_trees;
+  if (spec->satellites != GAL_SATELLITES_NONE &&
+      !(spec->satellites == GAL_SATELLITES_JIANG2008 && spec->satellite_timescale_multiplier >= 0.0))
+    return GAL_ERR_ARGUMENT;
+  const bool satellites = spec->satellites == GAL_SATELLITES_JIANG2008;
   std::vector<std::vector<Builder::Node>> trees((size_t)nTrees);
   std::vector<std::vector<double>> spins((size_t)nTrees);
+  std::vector<std::vector<SatNode>> satTrees((size_t)(satellites ? nTrees : 0));
   const double s = spec->root_mass_slope;
   const double a = std::pow(spec->root_mass_min, s), b = std::pow(spec->root_mass_max, s);
   const double wRoot = gt.w_of_z(spec->root_redshift);
+  const double tMaxTree = c.time(spec->redshift_max);
 #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t t = 0; t < nTrees; ++t) {
     std::mt19937_64 rng(splitmix64(spec->seed ^ splitmix64((uint64_t)t)));
@@ -554,11 +766,23 @@ int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_f
     std::normal_distribution<double> N(0.0, 0.5);
     spins[(size_t)t].resize(trees[(size_t)t].size());
     for (double& x : spins[(size_t)t]) x = 0.04326 * std::exp(N(rng));
+    if (satellites) {
+      // Orbits drawn from the tree's stream after its spins.
+      TreeIn in{&trees[(size_t)t], std::vector<double>(trees[(size_t)t].size())};
+      for (size_t j = 0; j < in.time.size(); ++j) {
+        const double w = trees[(size_t)t][j].w;
+        in.time[j] = w >= B.wMax ? tMaxTree : c.time(gt.z_of_w(w));
+      }
+      add_satellites(in, spins[(size_t)t], c, spec->satellite_timescale_multiplier, rng, satTrees[(size_t)t]);
+    }
   }
   gal_forest* f = new (std::nothrow) gal_forest();
   if (!f) return GAL_ERR_ARGUMENT;
   size_t total = 0;
-  for (const auto& tr : trees) total += tr.size();
+  if (satellites)
+    for (const auto& tr : satTrees) total += tr.size();
+  else
+    for (const auto& tr : trees) total += tr.size();
   f->tree.resize(total);
   f->parent.resize(total);
   f->childFirst.resize(total);
@@ -566,8 +790,32 @@ int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_f
   f->time.resize(total);
   f->mass.resize(total);
   f->spin.resize(total);
+  f->satHost.assign(total, -1);
   size_t off = 0;
-  const double tMax = c.time(spec->redshift_max);
+  const double tMax = tMaxTree;
+  if (satellites) {
+    for (int64_t t = 0; t < nTrees; ++t) {
+      const std::vector<SatNode>& tr = satTrees[(size_t)t];
+      const std::vector<int32_t> order = layout(tr);
+      std::vector<int32_t> at(tr.size());
+      for (size_t j = 0; j < order.size(); ++j) at[(size_t)order[j]] = (int32_t)j;
+      for (size_t j = 0; j < order.size(); ++j) {
+        const SatNode& nd = tr[(size_t)order[j]];
+        const size_t g = off + j;
+        f->tree[g] = (int32_t)t;
+        f->parent[g] = nd.parent < 0 ? -1 : (int32_t)(off + at[(size_t)nd.parent]);
+        f->childCount[g] = (int32_t)nd.children.size();
+        f->childFirst[g] = nd.children.empty() ? 0 : (int32_t)(off + at[(size_t)nd.children[0]]);
+        f->time[g] = nd.time;
+        f->mass[g] = nd.mass;
+        f->spin[g] = nd.spin;
+        f->satHost[g] = nd.satHost < 0 ? -1 : (int32_t)(off + at[(size_t)nd.satHost]);
+      }
+      off += tr.size();
+    }
+    *out = f;
+    return GAL_OK;
+  }
   for (int64_t t = 0; t < nTrees; ++t) {
     const auto& tr = trees[(size_t)t];
     for (size_t j = 0; j < tr.size(); ++j) {
@@ -604,6 +852,23 @@ int gal_forest_get(const gal_forest* f, int32_t* tree, int32_t* parent, int32_t*
   put(mass, f->mass);
   put(spin, f->spin);
   return GAL_OK;
+}
+
+int gal_forest_get_satellite_host(const gal_forest* f, int32_t* satellite_host) {
+  if (!f || !satellite_host) return GAL_ERR_ARGUMENT;
+  std::memcpy(satellite_host, f->satHost.data(), f->satHost.size() * sizeof(int32_t));
+  return GAL_OK;
+}
+
+double gal_satellite_merging_time(const gal_params* p, double mass_host, double mass_satellite, double t,
+                                  double velocity_radial, double velocity_tangential, double multiplier) {
+  if (!p || !(mass_host > 0.0) || !(mass_satellite > 0.0)) return NAN;
+  const Cosmo c = cosmo_of(p);
+  double rv, vv;
+  virial(c, mass_host, std::max(c.redshift(t), 0.0), rv, vv);
+  const double mu = mass_host / (mass_host + mass_satellite);
+  return jiang2008_time(rv / vv * kMpcPerKmPerSToGyr, mass_host / mass_satellite, mu, velocity_radial,
+                        velocity_tangential, multiplier);
 }
 
 void gal_forest_free(gal_forest* f) { delete f; }

@@ -27,11 +27,16 @@ class PchParams(ctypes.Structure):
                 ("neutrino_number_effective", ctypes.c_double), ("neutrino_mass_summed", ctypes.c_double)]
 
 
+SATELLITES_NONE = 0       # secondary progenitors merge at their parent's time
+SATELLITES_JIANG2008 = 1  # satellites merge after the Jiang et al. (2008) time on a Benson (2005) orbit
+
+
 class ForestSpec(ctypes.Structure):
     _fields_ = [("n_trees", ctypes.c_int64), ("seed", ctypes.c_uint64), ("root_mass_min", ctypes.c_double),
                 ("root_mass_max", ctypes.c_double), ("root_mass_slope", ctypes.c_double),
                 ("root_redshift", ctypes.c_double), ("redshift_max", ctypes.c_double),
-                ("mass_resolution", ctypes.c_double)]
+                ("mass_resolution", ctypes.c_double), ("satellites", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("satellite_timescale_multiplier", ctypes.c_double)]
 
 
 def _declare(lib):
@@ -49,6 +54,10 @@ def _declare(lib):
     lib.gal_forest_get.restype = ctypes.c_int
     lib.gal_forest_free.argtypes = [vp]
     lib.gal_forest_free.restype = None
+    lib.gal_forest_get_satellite_host.argtypes = [vp, vp]
+    lib.gal_forest_get_satellite_host.restype = ctypes.c_int
+    lib.gal_satellite_merging_time.argtypes = [pp] + [ctypes.c_double] * 6
+    lib.gal_satellite_merging_time.restype = ctypes.c_double
     lib.gal_cosmic_time.argtypes = [pp, ctypes.c_double]
     lib.gal_cosmic_time.restype = ctypes.c_double
     lib.gal_redshift.argtypes = [pp, ctypes.c_double]
@@ -60,7 +69,7 @@ def _declare(lib):
     dp = ctypes.POINTER(ctypes.c_double)
     lib.gal_pch_branching_rates.argtypes = [ctypes.POINTER(PchParams)] + [ctypes.c_double] * 5 + [dp, dp]
     lib.gal_pch_branching_rates.restype = ctypes.c_int
-    lib.gal_gpu_forest_create.argtypes = [vp, ctypes.c_int64] + [vp] * 7 + [ctypes.c_int32, vp, ctypes.POINTER(vp)]
+    lib.gal_gpu_forest_create.argtypes = [vp, ctypes.c_int64] + [vp] * 8 + [ctypes.c_int32, vp, ctypes.POINTER(vp)]
     lib.gal_gpu_forest_create.restype = ctypes.c_int
     for name in ("gal_gpu_forest_evolve", "gal_gpu_forest_sync"):
         getattr(lib, name).argtypes = [vp, vp]
@@ -92,6 +101,9 @@ class Forest:
     time: np.ndarray
     mass: np.ndarray
     spin: np.ndarray
+    # For a satellite's phase (from its infall to its merger), the node it
+    # fell into; -1 for every other node.  None: no satellites.
+    satellite_host: np.ndarray = None
 
     @property
     def n(self):
@@ -114,8 +126,12 @@ class Forest:
         count = self.child_count[idx].copy()
         first = np.where(count > 0, new[self.child_first[idx]], 0).astype(np.int32)
         _, renum = np.unique(self.tree[idx], return_inverse=True)
+        host = None
+        if self.satellite_host is not None:
+            host = self.satellite_host[idx]
+            host = np.where(host >= 0, new[np.maximum(host, 0)], -1).astype(np.int32)
         return Forest(renum.astype(np.int32), parent, first, count, self.time[idx].copy(), self.mass[idx].copy(),
-                      self.spin[idx].copy()), idx
+                      self.spin[idx].copy(), host), idx
 
 
 def lpt_assignment(forest, n_ranks):
@@ -150,10 +166,14 @@ def pch_params():
 
 
 def build(params, n_trees, seed=3, root_mass_min=1e10, root_mass_max=1e14, root_mass_slope=-0.9, redshift_max=8.0,
-          mass_resolution=1e8, pch=None):
-    """Build a forest on the host (OpenMP over trees)."""
+          mass_resolution=1e8, pch=None, satellites=SATELLITES_NONE, satellite_timescale_multiplier=0.75):
+    """Build a forest on the host (OpenMP over trees).  With
+    satellites=SATELLITES_JIANG2008 secondary progenitors orbit as
+    satellites until their merging time (timescaleMultiplier as in the
+    reference's quickTest, 0.75)."""
     lib = _declare(_abi.load_library())
-    spec = ForestSpec(n_trees, seed, root_mass_min, root_mass_max, root_mass_slope, 0.0, redshift_max, mass_resolution)
+    spec = ForestSpec(n_trees, seed, root_mass_min, root_mass_max, root_mass_slope, 0.0, redshift_max, mass_resolution,
+                      satellites, 0, satellite_timescale_multiplier)
     pch = pch or pch_params()
     handle = ctypes.c_void_p()
     rc = lib.gal_forest_build(ctypes.byref(params), ctypes.byref(pch), ctypes.byref(spec), ctypes.byref(handle))
@@ -162,8 +182,22 @@ def build(params, n_trees, seed=3, root_mass_min=1e10, root_mass_max=1e14, root_
     n = lib.gal_forest_node_count(handle)
     arrays = [np.zeros(n, np.int32) for _ in range(4)] + [np.zeros(n) for _ in range(3)]
     lib.gal_forest_get(handle, *[_vp(a) for a in arrays])
+    host = None
+    if satellites != SATELLITES_NONE:
+        host = np.zeros(n, np.int32)
+        lib.gal_forest_get_satellite_host(handle, _vp(host))
     lib.gal_forest_free(handle)
-    return Forest(*arrays)
+    return Forest(*arrays, host)
+
+
+def satellite_merging_time(params, mass_host, mass_satellite, t, velocity_radial, velocity_tangential,
+                           multiplier=0.75):
+    """The builder's Jiang et al. (2008) merging time (Gyr) for one orbit
+    (velocities in units of the host's virial velocity); negative when the
+    orbit is unbound."""
+    lib = _declare(_abi.load_library())
+    return lib.gal_satellite_merging_time(ctypes.byref(params), mass_host, mass_satellite, t, velocity_radial,
+                                          velocity_tangential, multiplier)
 
 
 def branching_rates(pch, alpha, sigma_parent, mass_parent, mass_resolution, w=1.686):
@@ -216,7 +250,10 @@ class ForestEvolver:
         self.state0 = np.ascontiguousarray(state0, dtype=np.float64)
         self.times = np.ascontiguousarray(times, dtype=np.float64)
         handle = ctypes.c_void_p()
-        rc = self.lib.gal_gpu_forest_create(evolver.ctx, self.n, *[_vp(a) for a in self._keep], _vp(self.state0),
+        self._host = None if forest.satellite_host is None else np.ascontiguousarray(forest.satellite_host,
+                                                                                    dtype=np.int32)
+        rc = self.lib.gal_gpu_forest_create(evolver.ctx, self.n, *[_vp(a) for a in self._keep],
+                                            None if self._host is None else _vp(self._host), _vp(self.state0),
                                             len(self.times), _vp(self.times), ctypes.byref(handle))
         if rc:
             raise RuntimeError(f"gal_gpu_forest_create failed ({rc}): {self._message()}")

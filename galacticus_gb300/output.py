@@ -46,20 +46,37 @@ GIGA_YEAR_SI = 3.15581497635456e16  # s
 MEGA_PARSEC_SI = 3.08567758135e22  # m
 
 
+def _satellite(forest):
+    host = forest.satellite_host
+    return np.zeros(forest.n, bool) if host is None else np.asarray(host) >= 0
+
+
 def halo_mass(forest, node, t):
-    """Basic (halo) mass of each node at time t: the node's mass growing
-    linearly in time to its parent's along a primary branch, fixed otherwise
-    (the forest evolver's segment masses; dark_matter_only_mass/
-    interpolate.F90:217-239)."""
+    """Basic (halo) mass of each node at time t, as the forest evolver's
+    segments have it (dmoInterpolateNodeInitialize, nodes/operators/physics/
+    dark_matter_only_mass/interpolate.F90:84-168, 217-239): a primary
+    progenitor grows linearly by its parent's unresolved mass (the parent's
+    mass beyond its other progenitors' and the satellites falling into it),
+    every other node -- satellites included -- keeps its mass."""
     node = np.asarray(node)
+    n = forest.n
+    sat = _satellite(forest)
+    host = np.full(n, -1) if forest.satellite_host is None else np.asarray(forest.satellite_host)
+    par_all = forest.parent
+    has_all = par_all >= 0
+    brought = np.bincount(host[sat], weights=forest.mass[sat], minlength=n) + \
+        np.bincount(par_all[has_all], weights=np.where(sat, 0.0, forest.mass)[has_all], minlength=n)
     par = forest.parent[node]
     t0 = forest.time[node]
     m0 = forest.mass[node]
     has = par >= 0
-    t1 = np.where(has, forest.time[np.where(has, par, 0)], t0)
-    primary = has & (forest.child_first[np.where(has, par, 0)] == node) & (t1 > t0)
-    m1 = np.where(primary, forest.mass[np.where(has, par, 0)], m0)
-    frac = np.where(primary, (t - t0) / np.where(primary, t1 - t0, 1.0), 0.0)
+    p0 = np.where(has, par, 0)
+    t1 = np.where(has, forest.time[p0], t0)
+    primary = has & (forest.child_first[p0] == node) & (t1 > t0) & ~sat[node]
+    dt = np.where(primary, t1 - t0, 1.0)
+    rate = np.maximum(forest.mass[p0] - brought[p0], 0.0) / dt
+    m1 = np.where(primary, m0 + rate * dt, m0)
+    frac = np.where(primary, (t - t0) / dt, 0.0)
     return m0 + (m1 - m0) * frac
 
 
@@ -96,9 +113,11 @@ def layout(params, forest, output_times, snapshots, snapshot_node, snapshot_outp
         d = f"{g}/nodeData"
         out[f"{d}/nodeIndex"] = nodes.astype(np.int64)
         out[f"{d}/parentIndex"] = forest.parent[nodes].astype(np.int64)
-        out[f"{d}/nodeIsIsolated"] = np.ones(nodes.size, dtype=np.int64)
+        sat = _satellite(forest)[nodes]
+        out[f"{d}/nodeIsIsolated"] = np.where(sat, 0, 1).astype(np.int64)
         out[f"{d}/basicMass"] = halo_mass(forest, nodes, t)
-        out[f"{d}/basicTimeLastIsolated"] = np.full(nodes.size, t)
+        # A satellite was last isolated at its infall (its phase's start).
+        out[f"{d}/basicTimeLastIsolated"] = np.where(sat, forest.time[nodes], t)
         for y, name in PROPERTY_NAMES.items():
             out[f"{d}/{name}"] = snapshots[y, sel].astype(np.float64)
         trees, start, count = np.unique(forest.tree[nodes], return_index=True, return_counts=True)

@@ -77,7 +77,19 @@ typedef struct gal_forest_spec {
   double root_redshift;                /* 0                                                    */
   double redshift_max;                 /* branches end here (8)                                */
   double mass_resolution;              /* Msun                                                 */
+  /* Satellites.  GAL_SATELLITES_NONE: a secondary progenitor merges into
+   * the primary at their parent's time.  GAL_SATELLITES_JIANG2008: it
+   * becomes a satellite there and merges with the central galaxy of the
+   * halo that holds it after the Jiang et al. (2008) dynamical-friction
+   * time on a Benson (2005) orbit (satellites/merging/timescale/
+   * Jiang2008.F90, satellites/merging/virial_orbits/Benson2005.F90, the
+   * reference's default classes); see gal_satellite_merging_time. */
+  int32_t satellites;
+  int32_t reserved;
+  double satellite_timescale_multiplier; /* Jiang2008 timescaleMultiplier (quickTest: 0.75)    */
 } gal_forest_spec;
+
+enum { GAL_SATELLITES_NONE = 0, GAL_SATELLITES_JIANG2008 = 1 };
 
 typedef struct gal_forest gal_forest;  /* host-side forest built by gal_forest_build */
 
@@ -93,7 +105,32 @@ int64_t gal_forest_node_count(const gal_forest* f);
  * tree[n] receives the tree index of each node. */
 int gal_forest_get(const gal_forest* f, int32_t* tree, int32_t* parent, int32_t* child_first, int32_t* child_count,
                    double* time, double* mass, double* spin);
+/* With satellites: satellite_host[n] receives, for each node that is a
+ * satellite's phase from its infall to its merger (or to the end), the
+ * node it fell into (its host at infall), and -1 for every other node.  A
+ * satellite's phase is its own node: its only progenitor is the halo that
+ * fell in, its parent the piece of the host's branch that starts at the
+ * merger (a node whose primary progenitor is the host's branch before the
+ * merger), or none when it outlives the tree.  Its halo mass and virial
+ * scales stay those at infall and it accretes nothing
+ * (dmoInterpolateNodeInitialize, nodes/operators/physics/
+ * dark_matter_only_mass/interpolate.F90:118-120). */
+int gal_forest_get_satellite_host(const gal_forest* f, int32_t* satellite_host);
 void gal_forest_free(gal_forest* f);
+
+/* The merging time (Gyr) of a satellite of mass_satellite that falls into a
+ * host halo of mass_host at time t on an orbit with radial and tangential
+ * velocities velocity_radial and velocity_tangential at the host's virial
+ * radius, in units of its virial velocity: Jiang et al. (2008, ApJ 675,
+ * 1095) as satelliteMergingTimescalesJiang2008%timeUntilMerging
+ * (satellites/merging/timescale/Jiang2008.F90),
+ *   multiplier t_dyn (r_c/r_vir)^1/2 (0.94 eps^0.60 + 0.60)/(2 0.43) q/ln(1+q),
+ * q = mass_host/mass_satellite, t_dyn = r_vir/V_vir of the host, r_c and
+ * eps the radius and circularity of the circular orbit of the same energy
+ * in a singular isothermal host truncated at r_vir (point mass outside).
+ * Returns a negative value for an unbound orbit. */
+double gal_satellite_merging_time(const gal_params* p, double mass_host, double mass_satellite, double t,
+                                  double velocity_radial, double velocity_tangential, double multiplier);
 
 /* Cosmic time (Gyr) at redshift z and its inverse, in the cosmology of p. */
 double gal_cosmic_time(const gal_params* p, double z);
@@ -123,11 +160,20 @@ typedef struct gal_forest_dev gal_forest_dev;  /* a forest resident on the GPU o
  * the segment table (per piece: halo mass, accretion rate, virial radius
  * and velocity, spin, start and end time) is built on the host, and
  * state0[GAL_NY][n] holds the initial states (only progenitor-less nodes
- * are read).  The returned object owns every device array and a CUDA graph
- * of one evolution (reset, counters, kernel). */
+ * are read).  A node's halo mass grows by the mass its parent holds beyond
+ * its progenitors' (the unresolved mass, over the node's interval) when it
+ * is its parent's primary progenitor, and stays constant otherwise
+ * (dmoInterpolateNodeInitialize, nodes/operators/physics/
+ * dark_matter_only_mass/interpolate.F90:84-168).  satellite_host (may be
+ * NULL: no satellites) marks the satellite phases as gal_forest_get_
+ * satellite_host does: such a node keeps its halo mass and the virial
+ * scales of its infall time, accretes nothing, and its mass counts as
+ * brought into its host at infall.  The returned object owns every device
+ * array and a CUDA graph of one evolution (reset, counters, kernel). */
 int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const int32_t* child_first,
                           const int32_t* child_count, const double* time, const double* mass, const double* spin,
-                          const double* state0, int32_t n_outputs, const double* output_times, gal_forest_dev** out);
+                          const int32_t* satellite_host, const double* state0, int32_t n_outputs,
+                          const double* output_times, gal_forest_dev** out);
 /* Evolve the whole forest from state0 (one graph launch on the context
  * stream; asynchronous: gal_gpu_forest_sync waits).  Available in the FP64
  * form and the FP32-rate forms (with or without the surrogate); with a

@@ -1408,6 +1408,9 @@ struct ForestIn {
   const double *time, *mass, *spin, *state0;
   int32_t nOut;
   const double* tOut;
+  const int32_t* satHost;      // host at infall of a satellite phase, else -1 (NULL: no satellites)
+  std::vector<double> massIn;  // mass of the satellites falling into each node at its time
+  bool satellite(int64_t i) const { return satHost && satHost[i] >= 0; }
 };
 
 // A secondary progenitor merging into the primary at their parent's time:
@@ -1448,13 +1451,22 @@ static int evolve_forest_node(const gal_params& p, const Table& tb, const Cosmol
   const int32_t par = F.parent[i];
   const double t0 = F.time[i], t1 = par >= 0 ? F.time[par] : F.time[i];
   const bool primary = par >= 0 && F.childFirst[par] == i;
+  // dmoInterpolateNodeInitialize (nodes/operators/physics/dark_matter_only_
+  // mass/interpolate.F90:118-168): the primary progenitor's mass grows by
+  // its parent's unresolved mass (beyond its progenitors' and the
+  // satellites falling in) at a constant rate; other progenitors and
+  // satellites (isSatellite: accretion zero) keep their mass.
   double massEnd = F.mass[i], accretion = 0.0;
-  if (primary && t1 > t0) {
-    massEnd = F.mass[par];
-    double brought = 0.0;
-    for (int32_t c = 0; c < F.childCount[par]; ++c) brought += F.mass[F.childFirst[par] + c];
+  if (primary && t1 > t0 && !F.satellite(i)) {
+    double brought = F.massIn[(size_t)par];
+    for (int32_t c = 0; c < F.childCount[par]; ++c)
+      if (!F.satellite(F.childFirst[par] + c)) brought += F.mass[F.childFirst[par] + c];
     accretion = std::max(F.mass[par] - brought, 0.0) / (t1 - t0);
+    massEnd = F.mass[i] + accretion * (t1 - t0);
   }
+  // A satellite's dark-matter halo scales are those at its infall (its time
+  // of last isolation).
+  const double zFrozen = F.satellite(i) ? cos.redshift(t0) : 0.0;
   int64_t slot = snapFirst[i];
   auto snap = [&](const double* v) {
     for (int k = 0; k < GAL_NY; ++k) snapshot[k * snapTotal + slot] = v[k];
@@ -1476,7 +1488,7 @@ static int evolve_forest_node(const gal_params& p, const Table& tb, const Cosmol
     const double M = F.mass[i] + (massEnd - F.mass[i]) * (a - t0) / (t1 - t0);
     double prm[GAL_NP];
     double r, v;
-    cos.virial(M, cos.redshift(a), r, v);
+    cos.virial(M, F.satellite(i) ? zFrozen : cos.redshift(a), r, v);
     prm[GAL_P_MASS] = M;
     prm[GAL_P_MASS_RATE] = accretion;
     prm[GAL_P_RADIUS_VIRIAL] = r;
@@ -1662,8 +1674,9 @@ int64_t oracle_forest_snapshots(int64_t n, const int32_t* parent, const double* 
 // output times (slots of oracle_forest_snapshots).
 int oracle_evolve_forest(const gal_params* p, const gal_cie_table* table, int64_t n, const int32_t* parent,
                          const int32_t* childFirst, const int32_t* childCount, const double* time, const double* mass,
-                         const double* spin, const double* state0, int32_t nOut, const double* tOut, double* state,
-                         int32_t* status, uint32_t* counters, double* snapshot, int threads, int cooling_brent) {
+                         const double* spin, const int32_t* satHost, const double* state0, int32_t nOut,
+                         const double* tOut, double* state, int32_t* status, uint32_t* counters, double* snapshot,
+                         int threads, int cooling_brent) {
   if (!p || !table || n < 0 || !parent || !childFirst || !childCount || !time || !mass || !spin || !state0 || !state ||
       !status || (nOut > 0 && !tOut))
     return GAL_ERR_ARGUMENT;
@@ -1672,7 +1685,11 @@ int oracle_evolve_forest(const gal_params* p, const gal_cie_table* table, int64_
   if (rc) return rc;
   if (threads <= 0) threads = omp_get_max_threads();
   const orc::Cosmology cos{p->omega_matter, p->omega_dark_energy, p->hubble_constant};
-  const orc::ForestIn F{n, parent, childFirst, childCount, time, mass, spin, state0, nOut, tOut};
+  orc::ForestIn F{n, parent, childFirst, childCount, time, mass, spin, state0, nOut, tOut, satHost, {}};
+  F.massIn.assign((size_t)n, 0.0);
+  if (satHost)
+    for (int64_t i = 0; i < n; ++i)
+      if (satHost[i] >= 0) F.massIn[(size_t)satHost[i]] += mass[i];
   std::vector<int64_t> snapFirst((size_t)n);
   const int64_t snapTotal = oracle_forest_snapshots(n, parent, time, nOut, tOut, snapFirst.data());
   std::vector<double> stepOf((size_t)n, -1.0);

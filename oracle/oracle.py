@@ -166,10 +166,13 @@ def evolve_forest(params, table, forest, state0, output_times, threads=0, brent=
     vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
     l = lib()
     l.oracle_evolve_forest.restype = ctypes.c_int
+    host = getattr(forest, "satellite_host", None)
+    host = None if host is None else np.ascontiguousarray(host, dtype=np.int32)
     rc = l.oracle_evolve_forest(ctypes.byref(params), ctypes.byref(table.struct), ctypes.c_int64(n), vp(forest.parent),
                                 vp(forest.child_first), vp(forest.child_count), vp(forest.time), vp(forest.mass),
-                                vp(forest.spin), vp(state0), ctypes.c_int32(len(t_out)), vp(t_out), vp(state), vp(status),
-                                vp(counters), vp(snap), ctypes.c_int(threads), ctypes.c_int(1 if brent else 0))
+                                vp(forest.spin), None if host is None else vp(host), vp(state0),
+                                ctypes.c_int32(len(t_out)), vp(t_out), vp(state), vp(status), vp(counters), vp(snap),
+                                ctypes.c_int(threads), ctypes.c_int(1 if brent else 0))
     if rc != 0:
         raise RuntimeError(f"oracle_evolve_forest failed with code {rc}")
     return state, status, counters, snap[:, :m]

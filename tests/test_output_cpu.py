@@ -71,14 +71,21 @@ def test_layout_and_values(tmp_path, evolved):
 
 
 def test_halo_mass_interpolates_along_primary_branches(evolved):
+    """A primary progenitor's halo grows by its parent's unresolved mass (the
+    parent's mass beyond all its progenitors'), linearly in time, as the
+    reference's dmoInterpolate operator has it; secondaries keep theirs."""
     _, f, _, _, _, _ = evolved
     prim = [i for i in range(f.n) if f.parent[i] >= 0 and f.child_first[f.parent[i]] == i and
-            f.time[f.parent[i]] > f.time[i]]
+            f.time[f.parent[i]] > f.time[i] and f.child_count[f.parent[i]] > 1]
     i = prim[0]
     p = f.parent[i]
+    unresolved = f.mass[p] - f.mass[f.child_first[p]:f.child_first[p] + f.child_count[p]].sum()
+    assert unresolved > 0.0
     mid = 0.5 * (f.time[i] + f.time[p])
     assert output.halo_mass(f, [i], f.time[i])[0] == f.mass[i]
-    assert abs(output.halo_mass(f, [i], mid)[0] - 0.5 * (f.mass[i] + f.mass[p])) < 1e-6 * f.mass[p]
+    assert abs(output.halo_mass(f, [i], mid)[0] - (f.mass[i] + 0.5 * unresolved)) < 1e-9 * f.mass[p]
+    assert abs(output.halo_mass(f, [i], f.time[p])[0] - (f.mass[p] - (f.mass[p] - f.mass[i] - unresolved))) < \
+        1e-9 * f.mass[p]
     secondary = [i for i in range(f.n) if f.parent[i] >= 0 and f.child_first[f.parent[i]] != i]
     if secondary:
         s = secondary[0]
