@@ -40,9 +40,13 @@ def main(out_dir):
     every = [torch.zeros(2, dtype=torch.float64) for _ in range(world)]
     dist.all_gather(every, mine)
 
-    # One forest, split over the ranks.
+    # One forest, split over the ranks (with satellites, as the bench's: a
+    # satellite's phase and its host stay in their tree, so a share's
+    # satellite hosts are remapped into the share).
     table = CieTable()
-    whole = forest.build(params, n_trees=7, seed=3, root_mass_min=1e10, root_mass_max=3e11)
+    whole = forest.build(params, n_trees=7, seed=3, root_mass_min=1e10, root_mass_max=3e11,
+                         satellites=forest.SATELLITES_JIANG2008)
+    assert (whole.satellite_host >= 0).sum() > 0
     times = forest.output_times(params, n=5)
     part, idx = forest.partition(whole, rank, world)
     state = oracle.evolve_forest(params, table, part, forest.initial_state(params, part), times, brent=False)[0]
