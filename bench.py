@@ -62,8 +62,11 @@ GATES = (0.01, 0.003, 0.001, 0.0003, 0.0001)
 MLP_FLOPS = 2 * (3 * 64 + 64 * 64 + 64 * 64 + 64)  # per network evaluation
 # dram__bytes_read.sum + dram__bytes_write.sum of the headline launch (the
 # surrogate form's two kernels on this workload) from one ncu --set full
-# capture, per pass.
-HEADLINE_DRAM_BYTES = 8.895488e6 + 10.873344e6
+# capture, per pass, and the same capture's FP64 pipe utilisation
+# (sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active) of each
+# kernel, each timed alone.
+HEADLINE_DRAM_BYTES = 8.952064e6 + 10.888192e6
+HEADLINE_FP64_PIPE_PCT = {"network kernel": 3.17, "table kernel": 27.19}
 
 
 def parse():
@@ -828,7 +831,11 @@ def run_ours(args):
                                     "basis": "the MLP's flops (16,896 per evaluation) times the network evaluations "
                                              "per pass (one per node and RHS that used it), over the kernel time"},
                          "hbm": {"achieved": bytes_launch / (k_ms * 1e-3) / 1e9, "peak": peaks.get("hbm_gbs"),
-                                 "unit": "GB/s", "bytes_per_launch": bytes_launch}},
+                                 "unit": "GB/s", "bytes_per_launch": bytes_launch},
+                         "fp64_pipe": {"active_pct_of_peak": HEADLINE_FP64_PIPE_PCT,
+                                       "metric": "sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active",
+                                       "source": "ncu --set full capture of the headline split launch, each kernel "
+                                                 "timed alone, one GB300"}},
             "wall_ms_timed_region": headline["wall_ms"],
             "clocks": headline["clocks"],
             "cpu_baseline": cpu,
