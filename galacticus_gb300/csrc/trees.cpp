@@ -871,6 +871,13 @@ double gal_satellite_merging_time(const gal_params* p, double mass_host, double 
                         velocity_tangential, multiplier);
 }
 
+int gal_satellite_orbits(uint64_t seed, double mu, int64_t n, double* velocity_radial, double* velocity_tangential) {
+  if (n < 0 || !(mu > 0.0 && mu <= 1.0) || (n > 0 && (!velocity_radial || !velocity_tangential))) return GAL_ERR_ARGUMENT;
+  std::mt19937_64 rng(splitmix64(seed));
+  for (int64_t i = 0; i < n; ++i) benson2005_orbit(rng, mu, velocity_radial[i], velocity_tangential[i]);
+  return GAL_OK;
+}
+
 void gal_forest_free(gal_forest* f) { delete f; }
 
 }  // extern "C"

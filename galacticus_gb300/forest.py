@@ -58,6 +58,8 @@ def _declare(lib):
     lib.gal_forest_get_satellite_host.restype = ctypes.c_int
     lib.gal_satellite_merging_time.argtypes = [pp] + [ctypes.c_double] * 6
     lib.gal_satellite_merging_time.restype = ctypes.c_double
+    lib.gal_satellite_orbits.argtypes = [ctypes.c_uint64, ctypes.c_double, ctypes.c_int64, vp, vp]
+    lib.gal_satellite_orbits.restype = ctypes.c_int
     lib.gal_cosmic_time.argtypes = [pp, ctypes.c_double]
     lib.gal_cosmic_time.restype = ctypes.c_double
     lib.gal_redshift.argtypes = [pp, ctypes.c_double]
@@ -188,6 +190,17 @@ def build(params, n_trees, seed=3, root_mass_min=1e10, root_mass_max=1e14, root_
         lib.gal_forest_get_satellite_host(handle, _vp(host))
     lib.gal_forest_free(handle)
     return Forest(*arrays, host)
+
+
+def satellite_orbits(n, mu=1.0, seed=1):
+    """n orbits (radial, tangential velocity at the virial radius, units of
+    the host's virial velocity) from the builder's Benson (2005) sampler."""
+    lib = _declare(_abi.load_library())
+    ur, ut = np.zeros(n), np.zeros(n)
+    rc = lib.gal_satellite_orbits(seed, mu, n, _vp(ur), _vp(ut))
+    if rc:
+        raise RuntimeError(f"gal_satellite_orbits failed ({rc})")
+    return ur, ut
 
 
 def satellite_merging_time(params, mass_host, mass_satellite, t, velocity_radial, velocity_tangential,

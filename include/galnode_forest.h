@@ -132,6 +132,13 @@ void gal_forest_free(gal_forest* f);
 double gal_satellite_merging_time(const gal_params* p, double mass_host, double mass_satellite, double t,
                                   double velocity_radial, double velocity_tangential, double multiplier);
 
+/* n orbits from the builder's Benson (2005) sampler (satellites/merging/
+ * virial_orbits/Benson2005.F90): radial and tangential velocities at the
+ * host's virial radius in units of its virial velocity, bound for the
+ * specific reduced mass mu = M_host/(M_host + M_sat); one stream seeded by
+ * seed (for tests of the sampler against the published distribution). */
+int gal_satellite_orbits(uint64_t seed, double mu, int64_t n, double* velocity_radial, double* velocity_tangential);
+
 /* Cosmic time (Gyr) at redshift z and its inverse, in the cosmology of p. */
 double gal_cosmic_time(const gal_params* p, double z);
 double gal_redshift(const gal_params* p, double t);

@@ -151,3 +151,36 @@ def test_oracle_conserves_baryons_with_satellites(pair, params, table, oracle_mo
     idx = np.concatenate([d[f"Outputs/Output{k + 1}/nodeData/nodeIndex"] for k in range(len(times))])
     assert np.all(iso[f.satellite_host[idx] >= 0] == 0) and np.all(iso[f.satellite_host[idx] < 0] == 1)
     assert np.any(iso == 0)
+
+
+def benson2005_density(ur, ut):
+    """The Benson (2005) fit to the distribution of infall velocities (units
+    of the host's virial velocity), unnormalised."""
+    a = [3.90052, 2.47973, 10.2373, 0.683922, 0.353953, 1.07716, 0.509837, 0.206204, 0.314641]
+    b1 = a[2] * np.exp(-a[3] * (ut - a[4]) ** 2)
+    b2 = a[5] * np.exp(-a[6] * (ut - a[7]) ** 2)
+    return a[0] * ut * np.exp(-a[1] * (ut - a[8]) ** 2) * np.exp(-b1 * (ur - b2) ** 2)
+
+
+@pytest.mark.parametrize("mu", [1.0, 0.6])
+def test_orbit_sampler_follows_benson2005(mu):
+    """The builder's orbits against the published distribution restricted to
+    bound orbits (mu (ur^2 + ut^2)/2 < 1 - 1e-4), integrated on a grid: the
+    means and spreads of both velocities and the share of each quadrant of
+    the velocity plane."""
+    ur, ut = forest.satellite_orbits(400_000, mu=mu, seed=11)
+    assert np.all(0.5 * mu * (ur ** 2 + ut ** 2) < 1.0 - 1e-4)
+    assert np.all((ur >= 0) & (ur <= 3) & (ut >= 0) & (ut <= 3))
+    g = (np.arange(1200) + 0.5) * 3.0 / 1200
+    R, T = np.meshgrid(g, g, indexing="ij")
+    w = benson2005_density(R, T) * (0.5 * mu * (R ** 2 + T ** 2) < 1.0 - 1e-4)
+    w /= w.sum()
+    for sample, grid in ((ur, R), (ut, T)):
+        mean = (w * grid).sum()
+        sd = np.sqrt((w * (grid - mean) ** 2).sum())
+        assert abs(sample.mean() - mean) < 4 * sd / np.sqrt(len(sample)) + 1e-3
+        assert abs(sample.std() - sd) < 0.01 * sd
+    for r0 in (0.5, 1.0):
+        for t0 in (0.5, 1.0):
+            share = np.mean((ur < r0) & (ut < t0))
+            assert abs(share - w[(R < r0) & (T < t0)].sum()) < 0.005
