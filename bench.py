@@ -241,6 +241,16 @@ def run_reference(args):
         times.append(time.perf_counter() - t0)
         steps += int(counters[0].sum())
     value = steps / sum(times)
+    # The same passes with the closed-form cooling radius the GPU kernels use
+    # (exact for this cooling model; the reference finds it by Brent's
+    # method): the share of the GPU's speed-up that is the algorithm's.
+    tc, steps_c = 0.0, 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, _, _, counters = oracle.evolve_batch(params, table, batch.state, batch.param, batch.t_start, batch.t_end,
+                                                batch.step, threads=cores, brent=False)
+        tc += time.perf_counter() - t0
+        steps_c += int(counters[0].sum())
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
@@ -250,6 +260,10 @@ def run_reference(args):
                          "sample": f"{args.steps} passes over the {args.nodes}-halo batch; C++ restatement of the "
                                    "reference algorithm (the Fortran reference is not buildable here)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "closed_form_cooling_radius": {"value": steps_c / tc, "unit": UNIT,
+                                       "note": "the same passes with the GPU kernels' closed-form cooling radius "
+                                               "instead of the reference's Brent root (informative; value is the "
+                                               "reference's algorithm)"},
     }
     print(json.dumps(line), flush=True)
 
