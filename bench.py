@@ -428,6 +428,24 @@ def scale_record(args, params, table, net, gate):
            "nodes": f.n, "leaves": int((f.child_count == 0).sum()), "max_tree_nodes": int(np.bincount(f.tree).max()),
            "build_s": build_s, "timing": "host clock around one graph launch and its completion, after one warm-up",
            "forms": {}}
+    # The same builder with its branches grown on the GPU (keyed per-branch
+    # streams: other trees of the same distribution), host clock around the
+    # whole build (tables, roots, branching, spins, satellites, layout), and
+    # both builders without satellites (the branches alone).
+    ev = MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision="fp32")
+    builds = {}
+    for sat in sorted({args.satellites, "none"}):
+        for where in ("host", "gpu"):
+            if where == "host" and sat == args.satellites:
+                builds[f"{where}_{sat}"] = {"s": build_s, "nodes": f.n}
+                continue
+            tb = time.perf_counter()
+            fb = forest.build(params, n_trees=args.trees_scale, seed=5, redshift_max=10.0, satellites=SATELLITES[sat],
+                              gpu=ev if where == "gpu" else None)
+            builds[f"{where}_{sat}"] = {"s": time.perf_counter() - tb, "nodes": fb.n, **fb.build_stats}
+            del fb
+    ev.close()
+    out["tree_builds"] = builds
     states, counts = {}, {}
     for name, rates in (("plain", "fp64"), ("surrogate", "fp32")):
         ev = MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision=rates)

@@ -18,11 +18,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177"]
 SOURCES = ["galnode.cu", "evolve_plain.cu", "evolve_surrogate.cu", "evolve_fast.cu", "evolve_fast_surrogate.cu",
            "evolve_forest_plain.cu", "evolve_forest_fast.cu", "forest.cu", "calibrate.cu", "surrogate_train.cu",
-           "trees.cpp"]
+           "trees.cpp", "trees_gpu.cu"]
 # Host code whose FP64 results must match the oracle's bit for bit: no contraction.
 NO_CONTRACT = {"forest.cu"}
-# Host-only sources (compiled by nvcc through the host compiler) that use OpenMP.
-OPENMP = {"trees.cpp"}
+# Device code whose FP64 arithmetic follows the oracle's operation by operation: no FMA contraction.
+NO_FMAD = {"trees_gpu.cu"}
+# Sources whose host code uses OpenMP.
+OPENMP = {"trees.cpp", "trees_gpu.cu"}
 
 
 def nvcc():
@@ -39,6 +41,8 @@ def _compile(src, verbose):
         cmd[1:1] = ["-Xcompiler", "-fopenmp"]
     if src in NO_CONTRACT:
         cmd[1:1] = ["-Xcompiler", "-ffp-contract=off"]
+    if src in NO_FMAD:
+        cmd[1:1] = ["--fmad=false"]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -33,10 +33,14 @@
 #include <random>
 #include <vector>
 #include <algorithm>
+#include <chrono>
 
 #include "../../include/galnode_forest.h"
+#include "trees_internal.h"
 
 namespace {
+
+using gal::trees::GrownNode;
 
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kGravity = 6.673e-11 * 1.98892e30 / 1.0e6 / (1.0e6 * 3.08567758135e16);  // km^2 s^-2 Mpc / Msun
@@ -249,7 +253,7 @@ struct Rates {
   const SigmaTable& sig;
   gal_pch_params pch;
   double mRes;
-  static constexpr int kNq = 96;  // trapezoid points in ln q (1e-5 of the analytic rate)
+  static constexpr int kNq = gal::trees::kNq;  // trapezoid points in ln q (1e-5 of the analytic rate)
 
   // G without its w factor: G0 (sigma1/sigma2)^gamma1.
   double modifier_mass(double s1, double s2) const { return pch.g0 * std::pow(s1 / s2, pch.gamma1); }
@@ -351,10 +355,7 @@ struct Builder {
   gal_pch_params pch;
   double mRes, wMax;
   const RateTable& rt;
-  struct Node {
-    double mass, w;
-    int32_t parent, childFirst, childCount;
-  };
+  using Node = GrownNode;
 
   // Grow one tree from its root.
   void grow(double rootMass, double rootW, std::mt19937_64& rng, std::vector<Node>& nodes) const {
@@ -669,7 +670,160 @@ std::vector<int32_t> layout(const std::vector<SatNode>& nodes) {
 struct gal_forest {
   std::vector<int32_t> tree, parent, childFirst, childCount, satHost;
   std::vector<double> time, mass, spin;
+  double stats[7] = {0, 0, 0, 0, 0, 0, 0};  // gal_forest_build_stats
 };
+
+namespace {
+
+// The builder's tables as the device branching reads them.
+gal::trees::BranchTables branch_tables(const SigmaTable& sig, const RateTable& rt, const Builder& B,
+                                       const gal_pch_params& pch) {
+  return gal::trees::BranchTables{sig.lnMin, sig.dlnM, (int32_t)sig.lnSigma.size(), sig.lnSigma.data(), rt.lnMin,
+                                  rt.dlnM, rt.rows, rt.R.data(), rt.F.data(), rt.lnq.data(), rt.cdf.data(),
+                                  B.mRes, B.wMax, pch.gamma2, pch.accuracy_first, pch.accuracy_second};
+}
+
+// The forest of spec: branches grown on the host (ctx == nullptr: one
+// sequential stream per tree) or on the GPU of ctx (keyed streams).
+int build_forest(gal_ctx* ctx, const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec,
+                 gal_forest** out) {
+  const auto tStart = std::chrono::steady_clock::now();
+  auto since = [](std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  };
+  double stats[7] = {0, 0, 0, 0, 0, 0, 0};
+  if (!out) return GAL_ERR_ARGUMENT;
+  *out = nullptr;
+  if (!p || !pch || !spec || !valid_transfer(*pch) || spec->n_trees < 0 || !(spec->mass_resolution > 0.0) ||
+      !(spec->root_mass_min >= spec->mass_resolution) || !(spec->root_mass_max >= spec->root_mass_min) ||
+      !(spec->redshift_max > spec->root_redshift) || spec->root_redshift < 0.0 || spec->redshift_max > 30.0)
+    return GAL_ERR_ARGUMENT;
+  const Cosmo c = cosmo_of(p);
+  SigmaTable sig;
+  sig.build(c, *pch);
+  GrowthTable gt;
+  gt.build(c);
+  RateTable rt;
+  rt.build(Rates{sig, *pch, spec->mass_resolution}, spec->root_mass_max);
+  const Builder B{sig, *pch, spec->mass_resolution, gt.w_of_z(spec->redshift_max), rt};
+  stats[0] = since(tStart);
+  const int64_t nTrees = spec->n_trees;
+  if (spec->satellites != GAL_SATELLITES_NONE &&
+      !(spec->satellites == GAL_SATELLITES_JIANG2008 && spec->satellite_timescale_multiplier >= 0.0))
+    return GAL_ERR_ARGUMENT;
+  const bool satellites = spec->satellites == GAL_SATELLITES_JIANG2008;
+  std::vector<std::vector<Builder::Node>> trees((size_t)nTrees);
+  std::vector<std::vector<double>> spins((size_t)nTrees);
+  std::vector<std::vector<SatNode>> satTrees((size_t)(satellites ? nTrees : 0));
+  const double s = spec->root_mass_slope;
+  const double a = std::pow(spec->root_mass_min, s), b = std::pow(spec->root_mass_max, s);
+  const double wRoot = gt.w_of_z(spec->root_redshift);
+  const double tMaxTree = c.time(spec->redshift_max);
+  // dN/dln M ~ M^s on [min, max]: the root mass of a tree is the inverse of
+  // the cumulative M^s at the first draw of the tree's stream.
+  auto root_mass = [&](std::mt19937_64& rng) {
+    std::uniform_real_distribution<double> U(0.0, 1.0);
+    const double u = U(rng);
+    return std::fabs(s) < 1e-12 ? spec->root_mass_min * std::pow(spec->root_mass_max / spec->root_mass_min, u)
+                                : std::pow(a + u * (b - a), 1.0 / s);
+  };
+  auto tree_stream = [&](int64_t t) { return std::mt19937_64(splitmix64(spec->seed ^ splitmix64((uint64_t)t))); };
+  if (ctx) {
+    std::vector<double> roots((size_t)nTrees);
+#pragma omp parallel for schedule(static)
+    for (int64_t t = 0; t < nTrees; ++t) {
+      std::mt19937_64 rng = tree_stream(t);
+      roots[(size_t)t] = root_mass(rng);
+    }
+    const gal::trees::BranchTables tab = branch_tables(sig, rt, B, *pch);
+    double g[3] = {0, 0, 0};
+    const int rc = gal::trees::grow_forest_gpu(ctx, tab, roots.data(), nTrees, wRoot, spec->seed, trees, g);
+    if (rc != GAL_OK) return rc;
+    stats[1] = g[0];
+    stats[2] = g[1];
+    stats[5] = g[2];
+  }
+  const auto tLoop = std::chrono::steady_clock::now();
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t t = 0; t < nTrees; ++t) {
+    std::mt19937_64 rng = tree_stream(t);
+    const double M = root_mass(rng);
+    if (!ctx) B.grow(M, wRoot, rng, trees[(size_t)t]);
+    // Spins: log-normal about the peak of the Bett et al. (2007) distribution.
+    std::normal_distribution<double> N(0.0, 0.5);
+    spins[(size_t)t].resize(trees[(size_t)t].size());
+    for (double& x : spins[(size_t)t]) x = 0.04326 * std::exp(N(rng));
+    if (satellites) {
+      // Orbits drawn from the tree's stream after its spins.
+      TreeIn in{&trees[(size_t)t], std::vector<double>(trees[(size_t)t].size())};
+      for (size_t j = 0; j < in.time.size(); ++j) {
+        const double w = trees[(size_t)t][j].w;
+        in.time[j] = w >= B.wMax ? tMaxTree : c.time(gt.z_of_w(w));
+      }
+      add_satellites(in, spins[(size_t)t], c, spec->satellite_timescale_multiplier, rng, satTrees[(size_t)t]);
+    }
+  }
+  stats[3] = since(tLoop);
+  // Assembly, parallel over trees: each tree's nodes from its offset.
+  const auto tAsm = std::chrono::steady_clock::now();
+  gal_forest* f = new (std::nothrow) gal_forest();
+  if (!f) return GAL_ERR_ARGUMENT;
+  std::vector<size_t> first((size_t)nTrees + 1, 0);
+  for (int64_t t = 0; t < nTrees; ++t)
+    first[(size_t)t + 1] = first[(size_t)t] + (satellites ? satTrees[(size_t)t].size() : trees[(size_t)t].size());
+  const size_t total = first[(size_t)nTrees];
+  f->tree.resize(total);
+  f->parent.resize(total);
+  f->childFirst.resize(total);
+  f->childCount.resize(total);
+  f->time.resize(total);
+  f->mass.resize(total);
+  f->spin.resize(total);
+  f->satHost.assign(total, -1);
+  const double tMax = tMaxTree;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t t = 0; t < nTrees; ++t) {
+    const size_t off = first[(size_t)t];
+    if (satellites) {
+      const std::vector<SatNode>& tr = satTrees[(size_t)t];
+      const std::vector<int32_t> order = layout(tr);
+      std::vector<int32_t> at(tr.size());
+      for (size_t j = 0; j < order.size(); ++j) at[(size_t)order[j]] = (int32_t)j;
+      for (size_t j = 0; j < order.size(); ++j) {
+        const SatNode& nd = tr[(size_t)order[j]];
+        const size_t g = off + j;
+        f->tree[g] = (int32_t)t;
+        f->parent[g] = nd.parent < 0 ? -1 : (int32_t)(off + at[(size_t)nd.parent]);
+        f->childCount[g] = (int32_t)nd.children.size();
+        f->childFirst[g] = nd.children.empty() ? 0 : (int32_t)(off + at[(size_t)nd.children[0]]);
+        f->time[g] = nd.time;
+        f->mass[g] = nd.mass;
+        f->spin[g] = nd.spin;
+        f->satHost[g] = nd.satHost < 0 ? -1 : (int32_t)(off + at[(size_t)nd.satHost]);
+      }
+    } else {
+      const auto& tr = trees[(size_t)t];
+      for (size_t j = 0; j < tr.size(); ++j) {
+        const size_t g = off + j;
+        f->tree[g] = (int32_t)t;
+        f->parent[g] = tr[j].parent < 0 ? -1 : (int32_t)(off + tr[j].parent);
+        f->childFirst[g] = tr[j].childCount ? (int32_t)(off + tr[j].childFirst) : 0;
+        f->childCount[g] = tr[j].childCount;
+        // Nodes on the maximum-redshift boundary get exactly that time.
+        f->time[g] = tr[j].w >= B.wMax ? tMax : c.time(gt.z_of_w(tr[j].w));
+        f->mass[g] = tr[j].mass;
+        f->spin[g] = spins[(size_t)t][j];
+      }
+    }
+  }
+  stats[4] = since(tAsm);
+  stats[6] = since(tStart);
+  std::memcpy(f->stats, stats, sizeof stats);
+  *out = f;
+  return GAL_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -727,11 +881,23 @@ int gal_pch_branching_rates(const gal_pch_params* pch, double alpha, double sigm
 }
 
 int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec, gal_forest** out) {
-  if (!out) return GAL_ERR_ARGUMENT;
-  *out = nullptr;
-  if (!p || !pch || !spec || !valid_transfer(*pch) || spec->n_trees < 0 || !(spec->mass_resolution > 0.0) ||
-      !(spec->root_mass_min >= spec->mass_resolution) || !(spec->root_mass_max >= spec->root_mass_min) ||
-      !(spec->redshift_max > spec->root_redshift) || spec->root_redshift < 0.0 || spec->redshift_max > 30.0)
+  return build_forest(nullptr, p, pch, spec, out);
+}
+
+int gal_gpu_forest_build(gal_ctx* ctx, const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec,
+                         gal_forest** out) {
+  if (!ctx) {
+    if (out) *out = nullptr;
+    return GAL_ERR_ARGUMENT;
+  }
+  return build_forest(ctx, p, pch, spec, out);
+}
+
+int gal_pch_branch_tables(const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec, int32_t* sizes,
+                          double* meta, double* ln_sigma, double* rate, double* accretion, double* ln_q, double* cdf) {
+  if (!p || !pch || !spec || !sizes || !meta || !valid_transfer(*pch) || !(spec->mass_resolution > 0.0) ||
+      !(spec->root_mass_max >= spec->mass_resolution) || !(spec->redshift_max > spec->root_redshift) ||
+      spec->root_redshift < 0.0 || spec->redshift_max > 30.0)
     return GAL_ERR_ARGUMENT;
   const Cosmo c = cosmo_of(p);
   SigmaTable sig;
@@ -741,97 +907,26 @@ int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_f
   RateTable rt;
   rt.build(Rates{sig, *pch, spec->mass_resolution}, spec->root_mass_max);
   const Builder B{sig, *pch, spec->mass_resolution, gt.w_of_z(spec->redshift_max), rt};
-  const int64_t nTrees = spec->n_trees;
-  if (spec->satellites != GAL_SATELLITES_NONE &&
-      !(spec->satellites == GAL_SATELLITES_JIANG2008 && spec->satellite_timescale_multiplier >= 0.0))
-    return GAL_ERR_ARGUMENT;
-  const bool satellites = spec->satellites == GAL_SATELLITES_JIANG2008;
-  std::vector<std::vector<Builder::Node>> trees((size_t)nTrees);
-  std::vector<std::vector<double>> spins((size_t)nTrees);
-  std::vector<std::vector<SatNode>> satTrees((size_t)(satellites ? nTrees : 0));
-  const double s = spec->root_mass_slope;
-  const double a = std::pow(spec->root_mass_min, s), b = std::pow(spec->root_mass_max, s);
-  const double wRoot = gt.w_of_z(spec->root_redshift);
-  const double tMaxTree = c.time(spec->redshift_max);
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int64_t t = 0; t < nTrees; ++t) {
-    std::mt19937_64 rng(splitmix64(spec->seed ^ splitmix64((uint64_t)t)));
-    std::uniform_real_distribution<double> U(0.0, 1.0);
-    // dN/dln M ~ M^s on [min, max]: inverse of the cumulative M^s.
-    const double u = U(rng);
-    const double M = std::fabs(s) < 1e-12 ? spec->root_mass_min * std::pow(spec->root_mass_max / spec->root_mass_min, u)
-                                          : std::pow(a + u * (b - a), 1.0 / s);
-    B.grow(M, wRoot, rng, trees[(size_t)t]);
-    // Spins: log-normal about the peak of the Bett et al. (2007) distribution.
-    std::normal_distribution<double> N(0.0, 0.5);
-    spins[(size_t)t].resize(trees[(size_t)t].size());
-    for (double& x : spins[(size_t)t]) x = 0.04326 * std::exp(N(rng));
-    if (satellites) {
-      // Orbits drawn from the tree's stream after its spins.
-      TreeIn in{&trees[(size_t)t], std::vector<double>(trees[(size_t)t].size())};
-      for (size_t j = 0; j < in.time.size(); ++j) {
-        const double w = trees[(size_t)t][j].w;
-        in.time[j] = w >= B.wMax ? tMaxTree : c.time(gt.z_of_w(w));
-      }
-      add_satellites(in, spins[(size_t)t], c, spec->satellite_timescale_multiplier, rng, satTrees[(size_t)t]);
-    }
-  }
-  gal_forest* f = new (std::nothrow) gal_forest();
-  if (!f) return GAL_ERR_ARGUMENT;
-  size_t total = 0;
-  if (satellites)
-    for (const auto& tr : satTrees) total += tr.size();
-  else
-    for (const auto& tr : trees) total += tr.size();
-  f->tree.resize(total);
-  f->parent.resize(total);
-  f->childFirst.resize(total);
-  f->childCount.resize(total);
-  f->time.resize(total);
-  f->mass.resize(total);
-  f->spin.resize(total);
-  f->satHost.assign(total, -1);
-  size_t off = 0;
-  const double tMax = tMaxTree;
-  if (satellites) {
-    for (int64_t t = 0; t < nTrees; ++t) {
-      const std::vector<SatNode>& tr = satTrees[(size_t)t];
-      const std::vector<int32_t> order = layout(tr);
-      std::vector<int32_t> at(tr.size());
-      for (size_t j = 0; j < order.size(); ++j) at[(size_t)order[j]] = (int32_t)j;
-      for (size_t j = 0; j < order.size(); ++j) {
-        const SatNode& nd = tr[(size_t)order[j]];
-        const size_t g = off + j;
-        f->tree[g] = (int32_t)t;
-        f->parent[g] = nd.parent < 0 ? -1 : (int32_t)(off + at[(size_t)nd.parent]);
-        f->childCount[g] = (int32_t)nd.children.size();
-        f->childFirst[g] = nd.children.empty() ? 0 : (int32_t)(off + at[(size_t)nd.children[0]]);
-        f->time[g] = nd.time;
-        f->mass[g] = nd.mass;
-        f->spin[g] = nd.spin;
-        f->satHost[g] = nd.satHost < 0 ? -1 : (int32_t)(off + at[(size_t)nd.satHost]);
-      }
-      off += tr.size();
-    }
-    *out = f;
-    return GAL_OK;
-  }
-  for (int64_t t = 0; t < nTrees; ++t) {
-    const auto& tr = trees[(size_t)t];
-    for (size_t j = 0; j < tr.size(); ++j) {
-      const size_t g = off + j;
-      f->tree[g] = (int32_t)t;
-      f->parent[g] = tr[j].parent < 0 ? -1 : (int32_t)(off + tr[j].parent);
-      f->childFirst[g] = tr[j].childCount ? (int32_t)(off + tr[j].childFirst) : 0;
-      f->childCount[g] = tr[j].childCount;
-      // Nodes on the maximum-redshift boundary get exactly that time.
-      f->time[g] = tr[j].w >= B.wMax ? tMax : c.time(gt.z_of_w(tr[j].w));
-      f->mass[g] = tr[j].mass;
-      f->spin[g] = spins[(size_t)t][j];
-    }
-    off += tr.size();
-  }
-  *out = f;
+  const gal::trees::BranchTables t = branch_tables(sig, rt, B, *pch);
+  sizes[0] = t.nSigma;
+  sizes[1] = t.rows;
+  const double m[10] = {t.sigLnMin, t.sigDlnM, t.rtLnMin, t.rtDlnM, t.mRes, t.wMax, t.gamma2, t.accuracyFirst,
+                        t.accuracySecond, gt.w_of_z(spec->root_redshift)};
+  std::memcpy(meta, m, sizeof m);
+  auto put = [](double* dst, const double* src, size_t n) {
+    if (dst) std::memcpy(dst, src, n * sizeof(double));
+  };
+  put(ln_sigma, t.lnSigma, (size_t)t.nSigma);
+  put(rate, t.R, (size_t)t.rows);
+  put(accretion, t.F, (size_t)t.rows);
+  put(ln_q, t.lnq, (size_t)t.rows * gal::trees::kNq);
+  put(cdf, t.cdf, (size_t)t.rows * gal::trees::kNq);
+  return GAL_OK;
+}
+
+int gal_forest_build_stats(const gal_forest* f, double* stats) {
+  if (!f || !stats) return GAL_ERR_ARGUMENT;
+  std::memcpy(stats, f->stats, sizeof f->stats);
   return GAL_OK;
 }
 

@@ -71,6 +71,13 @@ def _declare(lib):
     dp = ctypes.POINTER(ctypes.c_double)
     lib.gal_pch_branching_rates.argtypes = [ctypes.POINTER(PchParams)] + [ctypes.c_double] * 5 + [dp, dp]
     lib.gal_pch_branching_rates.restype = ctypes.c_int
+    lib.gal_gpu_forest_build.argtypes = [vp, pp, ctypes.POINTER(PchParams), ctypes.POINTER(ForestSpec),
+                                         ctypes.POINTER(vp)]
+    lib.gal_gpu_forest_build.restype = ctypes.c_int
+    lib.gal_pch_branch_tables.argtypes = [pp, ctypes.POINTER(PchParams), ctypes.POINTER(ForestSpec)] + [vp] * 7
+    lib.gal_pch_branch_tables.restype = ctypes.c_int
+    lib.gal_forest_build_stats.argtypes = [vp, vp]
+    lib.gal_forest_build_stats.restype = ctypes.c_int
     lib.gal_gpu_forest_create.argtypes = [vp, ctypes.c_int64] + [vp] * 8 + [ctypes.c_int32, vp, ctypes.POINTER(vp)]
     lib.gal_gpu_forest_create.restype = ctypes.c_int
     for name in ("gal_gpu_forest_evolve", "gal_gpu_forest_sync"):
@@ -106,6 +113,9 @@ class Forest:
     # For a satellite's phase (from its infall to its merger), the node it
     # fell into; -1 for every other node.  None: no satellites.
     satellite_host: np.ndarray = None
+    # Where the build's time went (gal_forest_build_stats); None for forests
+    # not made by build().
+    build_stats: dict = None
 
     @property
     def n(self):
@@ -167,20 +177,33 @@ def pch_params():
     return p
 
 
-def build(params, n_trees, seed=3, root_mass_min=1e10, root_mass_max=1e14, root_mass_slope=-0.9, redshift_max=8.0,
-          mass_resolution=1e8, pch=None, satellites=SATELLITES_NONE, satellite_timescale_multiplier=0.75):
-    """Build a forest on the host (OpenMP over trees).  With
-    satellites=SATELLITES_JIANG2008 secondary progenitors orbit as
-    satellites until their merging time (timescaleMultiplier as in the
-    reference's quickTest, 0.75)."""
-    lib = _declare(_abi.load_library())
-    spec = ForestSpec(n_trees, seed, root_mass_min, root_mass_max, root_mass_slope, 0.0, redshift_max, mass_resolution,
+def _spec(n_trees, seed, root_mass_min, root_mass_max, root_mass_slope, redshift_max, mass_resolution, satellites,
+          satellite_timescale_multiplier):
+    return ForestSpec(n_trees, seed, root_mass_min, root_mass_max, root_mass_slope, 0.0, redshift_max, mass_resolution,
                       satellites, 0, satellite_timescale_multiplier)
+
+
+def build(params, n_trees, seed=3, root_mass_min=1e10, root_mass_max=1e14, root_mass_slope=-0.9, redshift_max=8.0,
+          mass_resolution=1e8, pch=None, satellites=SATELLITES_NONE, satellite_timescale_multiplier=0.75, gpu=None):
+    """Build a forest on the host (OpenMP over trees), or with its branches
+    grown on the GPU of ``gpu`` (an evolver; gal_gpu_forest_build: the same
+    builder with keyed per-branch streams, so other trees for the same
+    seed).  With satellites=SATELLITES_JIANG2008 secondary progenitors
+    orbit as satellites until their merging time (timescaleMultiplier as in
+    the reference's quickTest, 0.75)."""
+    lib = _declare(_abi.load_library())
+    spec = _spec(n_trees, seed, root_mass_min, root_mass_max, root_mass_slope, redshift_max, mass_resolution,
+                 satellites, satellite_timescale_multiplier)
     pch = pch or pch_params()
     handle = ctypes.c_void_p()
-    rc = lib.gal_forest_build(ctypes.byref(params), ctypes.byref(pch), ctypes.byref(spec), ctypes.byref(handle))
-    if rc:
-        raise RuntimeError(f"gal_forest_build failed ({rc})")
+    if gpu is None:
+        rc = lib.gal_forest_build(ctypes.byref(params), ctypes.byref(pch), ctypes.byref(spec), ctypes.byref(handle))
+        if rc:
+            raise RuntimeError(f"gal_forest_build failed ({rc})")
+    else:
+        from .evolver import _check
+        _check(gpu.lib, gpu.ctx, lib.gal_gpu_forest_build(gpu.ctx, ctypes.byref(params), ctypes.byref(pch),
+                                                          ctypes.byref(spec), ctypes.byref(handle)))
     n = lib.gal_forest_node_count(handle)
     arrays = [np.zeros(n, np.int32) for _ in range(4)] + [np.zeros(n) for _ in range(3)]
     lib.gal_forest_get(handle, *[_vp(a) for a in arrays])
@@ -188,8 +211,32 @@ def build(params, n_trees, seed=3, root_mass_min=1e10, root_mass_max=1e14, root_
     if satellites != SATELLITES_NONE:
         host = np.zeros(n, np.int32)
         lib.gal_forest_get_satellite_host(handle, _vp(host))
+    stats = np.zeros(7)
+    lib.gal_forest_build_stats(handle, _vp(stats))
     lib.gal_forest_free(handle)
-    return Forest(*arrays, host)
+    return Forest(*arrays, host, build_stats=dict(tables_s=stats[0], gpu_growth_s=stats[1], download_renumber_s=stats[2],
+                                                  per_tree_s=stats[3], assembly_s=stats[4], generations=int(stats[5]),
+                                                  total_s=stats[6]))
+
+
+def branch_tables(params, seed=3, root_mass_min=1e10, root_mass_max=1e14, redshift_max=8.0, mass_resolution=1e8,
+                  pch=None):
+    """The GPU branching's inputs for a forest (gal_pch_branch_tables): a
+    dict with ``sizes``, ``meta`` and the tables ``ln_sigma``, ``rate``,
+    ``accretion``, ``ln_q``, ``cdf``."""
+    lib = _declare(_abi.load_library())
+    spec = _spec(1, seed, root_mass_min, root_mass_max, -0.9, redshift_max, mass_resolution, SATELLITES_NONE, 0.75)
+    pch = pch or pch_params()
+    sizes, meta = np.zeros(2, np.int32), np.zeros(10)
+    args = (ctypes.byref(params), ctypes.byref(pch), ctypes.byref(spec))
+    rc = lib.gal_pch_branch_tables(*args, _vp(sizes), _vp(meta), None, None, None, None, None)
+    if rc:
+        raise RuntimeError(f"gal_pch_branch_tables failed ({rc})")
+    t = dict(sizes=sizes, meta=meta, ln_sigma=np.zeros(sizes[0]), rate=np.zeros(sizes[1]),
+             accretion=np.zeros(sizes[1]), ln_q=np.zeros(sizes[1] * 96), cdf=np.zeros(sizes[1] * 96))
+    lib.gal_pch_branch_tables(*args, _vp(sizes), _vp(meta), *[_vp(t[k]) for k in ("ln_sigma", "rate", "accretion",
+                                                                                    "ln_q", "cdf")])
+    return t
 
 
 def satellite_orbits(n, mu=1.0, seed=1):

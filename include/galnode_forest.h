@@ -100,7 +100,40 @@ void gal_pch_params_default(gal_pch_params* p);
  * OpenMP-parallel over trees; every tree is a deterministic function of
  * (seed, tree index). */
 int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec, gal_forest** out);
+/* The same builder with its branches grown on the GPU of ctx: the tables
+ * (sigma(M), the split and sub-resolution rates, the split's distribution
+ * in ln q) and each tree's root mass are those of gal_forest_build, and
+ * every branch is walked by the host builder's steps with the rates
+ * evaluated in FP32 (the mass and w accumulated in FP64); each branch draws
+ * from its own stream, keyed by its tree and its path from the root, so the
+ * trees are a deterministic function of (seed, tree index), of the host
+ * builder's distribution, but not the trees gal_forest_build makes from the
+ * same seed.  Spins and
+ * satellite orbits are drawn on the host as by gal_forest_build.  The
+ * Cole2000 builder's per-tree build (merger_trees/construct/builder/
+ * Cole2000/_class.F90:360-913), for a whole forest at once.  Errors are
+ * recorded in ctx. */
+int gal_gpu_forest_build(gal_ctx* ctx, const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec,
+                         gal_forest** out);
+/* The inputs of the GPU branching for a forest spec (for tests of it
+ * against a restatement of its walk): sizes[2] = {sigma rows, rate rows};
+ * meta[10] = {ln M of the first sigma row, its spacing in ln M, the same
+ * for the rate rows, mass resolution, w at the maximum redshift, gamma2,
+ * accuracy_first, accuracy_second, w at the roots' redshift}; and, where
+ * not NULL, ln_sigma[sizes[0]] (ln sigma(M) at z = 0), rate[sizes[1]] and
+ * accretion[sizes[1]] (without their (w/sigma)^gamma2 factor),
+ * ln_q[sizes[1]][96] and cdf[sizes[1]][96] (the split's cumulative
+ * distribution in ln q). */
+int gal_pch_branch_tables(const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec, int32_t* sizes,
+                          double* meta, double* ln_sigma, double* rate, double* accretion, double* ln_q, double* cdf);
 int64_t gal_forest_node_count(const gal_forest* f);
+/* Where a build's time went, host clock: stats[7] = {seconds building the
+ * tables, seconds of the GPU growth (its generations; 0 for
+ * gal_forest_build), seconds downloading and renumbering the GPU's nodes,
+ * seconds of the
+ * per-tree loop (root, growth on the host, spins, satellites), seconds of
+ * the assembly into the forest layout, GPU generations, total seconds}. */
+int gal_forest_build_stats(const gal_forest* f, double* stats);
 /* Copy the forest out in the layout above (any pointer may be NULL);
  * tree[n] receives the tree index of each node. */
 int gal_forest_get(const gal_forest* f, int32_t* tree, int32_t* parent, int32_t* child_first, int32_t* child_count,

@@ -1732,4 +1732,254 @@ int oracle_evolve_forest(const gal_params* p, const gal_cie_table* table, int64_
   return GAL_OK;
 }
 
+
+}  // extern "C"
+
+// ------------------------------------------------------------ tree branching
+//
+// One tree of the Cole et al. (2000) builder with the Parkinson, Cole &
+// Helly (2008) rates (merger_trees/construct/builder/Cole2000/
+// _class.F90:360-913, merger_trees/branching_probability/
+// Parkinson_Cole_Helly.F90:265-634), grown as the builder's GPU branching
+// grows it, sequentially: from the root back in w = delta_c0/D(z), each
+// step limited so that the split probability R dw, the sub-resolution mass
+// fraction F dw (both times (w/sigma)^gamma2) and dw/sqrt(2 (S(M/2) - S(M)))
+// stay below the accuracy parameters; a split draws q from the tabulated
+// distribution in ln q and makes two progenitors (the larger first) at
+// w + dw; a branch that falls below the resolution or reaches w_max ends in
+// a leaf.  The tables (sigma(M), R, F, the ln q distribution; inputs of the
+// walk, like the cooling table of the node evolution) come from the
+// builder.
+//
+// This is the GPU walk's specification: the rates in FP32 from FP32 copies
+// of the tables, its logarithm and exponential (Cody & Waite 1980 argument
+// reduction; the series of atanh to s^11 and of exp to r^7, evaluated with
+// fmaf), the mass and w accumulated in FP64, and each node's branch drawing
+// from its own SplitMix64 stream (Steele, Lea & Flood 2014) keyed by its
+// tree and its path from the root.  Every operation is IEEE-defined, so
+// the GPU's trees must equal these bit for bit.
+
+namespace orc {
+namespace branch {
+
+uint64_t mix64(uint64_t x) {
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+constexpr uint64_t kGamma = 0x9e3779b97f4a7c15ull;
+uint64_t root_key(uint64_t seed, int64_t tree) {
+  return mix64(seed + kGamma) ^ mix64((uint64_t)tree * 0xd1b54a32d192ed03ull + 0x5851f42d4c957f2dull);
+}
+uint64_t child_key(uint64_t k, int c) { return mix64(k ^ (0xa0761d6478bd642full * (uint64_t)(c + 1))); }
+double draw(uint64_t key, uint32_t k) { return (double)(mix64(key + (uint64_t)(k + 1) * kGamma) >> 11) * 0x1.0p-53; }
+
+constexpr float kLn2Hi = 0.693359375f;     // 355/512
+constexpr float kLn2Lo = -2.12194440e-4f;  // ln 2 - 355/512
+constexpr float kInvLn2 = 1.44269504f;
+
+float ln_pos(double x) {
+  int64_t b;
+  std::memcpy(&b, &x, sizeof b);
+  int e = (int)(b >> 52) - 1023;
+  const uint32_t fb = 0x3f800000u | (uint32_t)((b >> 29) & 0x7fffff);
+  float f;
+  std::memcpy(&f, &fb, sizeof f);
+  if (f > 1.41421354f) {
+    f *= 0.5f;
+    e += 1;
+  }
+  const float s = (f - 1.0f) / (f + 1.0f);
+  const float z = s * s;
+  float p = std::fmaf(1.0f / 11.0f, z, 1.0f / 9.0f);
+  p = std::fmaf(p, z, 1.0f / 7.0f);
+  p = std::fmaf(p, z, 1.0f / 5.0f);
+  p = std::fmaf(p, z, 1.0f / 3.0f);
+  p = std::fmaf(p, z, 1.0f);
+  const float ef = (float)e;
+  return std::fmaf(ef, kLn2Hi, std::fmaf(ef, kLn2Lo, (2.0f * s) * p));
+}
+
+float exp_f(float x) {
+  x = std::fmin(std::fmax(x, -80.0f), 80.0f);
+  const float k = std::rint(x * kInvLn2);
+  const float r = std::fmaf(-k, kLn2Lo, std::fmaf(-k, kLn2Hi, x));
+  float p = std::fmaf(1.0f / 5040.0f, r, 1.0f / 720.0f);
+  p = std::fmaf(p, r, 1.0f / 120.0f);
+  p = std::fmaf(p, r, 1.0f / 24.0f);
+  p = std::fmaf(p, r, 1.0f / 6.0f);
+  p = std::fmaf(p, r, 0.5f);
+  p = std::fmaf(p, r, 1.0f);
+  p = std::fmaf(p, r, 1.0f);
+  const uint32_t sb = (uint32_t)((int)k + 127) << 23;
+  float scale;
+  std::memcpy(&scale, &sb, sizeof scale);
+  return p * scale;
+}
+
+struct Tables {
+  std::vector<float> lnSigma, R, F;  // FP32 copies
+  const double *Rd, *lnq, *cdf;      // FP64 split tables
+  float sigLnMin, sigInv, halfShift, rtLnMin, rtInv, gamma2, acc1, acc2;
+  double mRes, wMax;
+  static constexpr int kNq = 96;
+};
+
+float interp(const std::vector<float>& t, float x) {
+  const int n = (int)t.size();
+  x = std::fmin(std::fmax(x, 0.0f), (float)(n - 1));
+  const int i = std::min((int)x, n - 2);
+  const float f = x - (float)i;
+  return t[(size_t)i] + f * (t[(size_t)i + 1] - t[(size_t)i]);
+}
+
+struct Node {
+  double mass, w;
+  int32_t parent, childFirst, childCount;
+  uint64_t key;
+};
+
+void grow(const Tables& t, double rootMass, double rootW, uint64_t rootKey, std::vector<Node>& nodes) {
+  constexpr int nq = Tables::kNq;
+  const int rows = (int)t.R.size();
+  nodes.assign(1, Node{rootMass, rootW, -1, 0, 0, rootKey});
+  std::vector<int32_t> stack{0};
+  while (!stack.empty()) {
+    const int32_t i = stack.back();
+    stack.pop_back();
+    const uint64_t key = nodes[(size_t)i].key;
+    double m = nodes[(size_t)i].mass, w = nodes[(size_t)i].w;
+    double mPrev = m, wPrev = w;
+    uint32_t k = 0;
+    bool split = false;
+    int guard = 0;
+    while (w < t.wMax && m >= t.mRes && ++guard < 100000) {
+      const float lm = ln_pos(m);
+      const float x = (lm - t.rtLnMin) * t.rtInv;
+      const float xs = (lm - t.sigLnMin) * t.sigInv;
+      const float lns2 = interp(t.lnSigma, xs);
+      const float S2 = exp_f(2.0f * lns2);
+      const float Sh = exp_f(2.0f * interp(t.lnSigma, xs - t.halfShift));
+      const float wf = exp_f(t.gamma2 * (ln_pos(w) - lns2));
+      const float xc = std::fmin(std::fmax(x, 0.0f), (float)(rows - 1));
+      const int j = std::min((int)xc, rows - 2);
+      const float fx = xc - (float)j;
+      const float R = m <= 2.0 * t.mRes ? 0.0f : wf * (t.R[(size_t)j] + fx * (t.R[(size_t)j + 1] - t.R[(size_t)j]));
+      const float F = wf * (t.F[(size_t)j] + fx * (t.F[(size_t)j + 1] - t.F[(size_t)j]));
+      float dwf = t.acc2 * std::sqrt(2.0f * std::fmax(Sh - S2, 0.0f));
+      if (R > 0.0f) dwf = std::fmin(dwf, t.acc1 / R);
+      if (F > 0.0f) dwf = std::fmin(dwf, t.acc1 / F);
+      if (!(dwf > 0.0f)) dwf = 1.0e-3f;
+      double dw = (double)dwf;
+      const double wStep = w + dw;
+      const bool last = wStep >= t.wMax;
+      if (last) dw = t.wMax - w;
+      const double wNext = last ? t.wMax : wStep;
+      mPrev = m;
+      wPrev = w;
+      if (R > 0.0f && draw(key, k++) < (double)R * dw) {
+        int row = fx < 0.5f ? j : j + 1;
+        if (!(t.Rd[row] > 0.0)) row = j + 1;
+        const double* cdf = t.cdf + (size_t)row * nq;
+        const double* lnq = t.lnq + (size_t)row * nq;
+        const double target = draw(key, k++);
+        const int kk = (int)(std::upper_bound(cdf, cdf + nq, target) - cdf);
+        const int k1 = std::min(std::max(kk, 1), nq - 1);
+        const double f = (target - cdf[k1 - 1]) / std::max(cdf[k1] - cdf[k1 - 1], 1e-300);
+        const double q = (double)exp_f((float)(lnq[k1 - 1] + f * (lnq[k1] - lnq[k1 - 1])));
+        const double m1 = q * m;
+        const double m2 = m * (1.0 - (double)F * dw) - m1;
+        const double big = std::max(m1, m2), small = std::min(m1, m2);
+        const int32_t first = (int32_t)nodes.size();
+        int32_t count = 0;
+        if (big >= t.mRes) nodes.push_back(Node{big, wNext, i, 0, 0, child_key(key, count++)});
+        if (small >= t.mRes) nodes.push_back(Node{small, wNext, i, 0, 0, child_key(key, count++)});
+        nodes[(size_t)i].childFirst = first;
+        nodes[(size_t)i].childCount = count;
+        for (int32_t c = count - 1; c >= 0; --c) stack.push_back(first + c);
+        split = true;
+        break;
+      }
+      m *= 1.0 - (double)F * dw;
+      w = wNext;
+      if (last) break;
+    }
+    if (!split) {
+      double lm = m, lw = w;
+      if (m < t.mRes) {
+        lm = mPrev;
+        lw = wPrev;
+      }
+      if (lw > nodes[(size_t)i].w && lm >= t.mRes) {
+        nodes[(size_t)i].childFirst = (int32_t)nodes.size();
+        nodes[(size_t)i].childCount = 1;
+        nodes.push_back(Node{lm, lw, i, 0, 0, child_key(key, 0)});
+      }
+    }
+  }
+}
+
+}  // namespace branch
+}  // namespace orc
+
+extern "C" {
+
+// The walk's FP32 logarithm (of doubles) and exponential, for n arguments.
+void oracle_branch_math(int64_t n, const double* x, float* ln_x, const float* y, float* exp_y) {
+  for (int64_t i = 0; i < n; ++i) {
+    ln_x[i] = orc::branch::ln_pos(x[i]);
+    exp_y[i] = orc::branch::exp_f(y[i]);
+  }
+}
+
+// Grow trees tree0..tree0+n-1 of seed from their root masses (at w =
+// meta[9]); meta[10], sizes[2] and the arrays as gal_pch_branch_tables
+// returns them.  Node arrays of capacity cap receive the trees one after
+// another, each in the builder's order (depth first, the larger progenitor
+// first); treeFirst[n] the first node of each.  Returns the node count, or
+// -(the count needed) when cap is too small.
+int64_t oracle_grow_trees(const double* meta, const int32_t* sizes, const double* lnSigma, const double* rate,
+                          const double* accretion, const double* lnq, const double* cdf, uint64_t seed, int64_t tree0,
+                          int64_t n, const double* rootMass, int64_t cap, double* mass, double* w, int32_t* parent,
+                          int32_t* childFirst, int32_t* childCount, int64_t* treeFirst) {
+  orc::branch::Tables t;
+  t.lnSigma.assign(lnSigma, lnSigma + sizes[0]);
+  t.R.assign(rate, rate + sizes[1]);
+  t.F.assign(accretion, accretion + sizes[1]);
+  if (sizes[0] < 2 || sizes[1] < 2) return 0;
+  t.Rd = rate;
+  t.lnq = lnq;
+  t.cdf = cdf;
+  t.sigLnMin = (float)meta[0];
+  t.sigInv = (float)(1.0 / meta[1]);
+  t.halfShift = (float)(0.6931471805599453 / meta[1]);
+  t.rtLnMin = (float)meta[2];
+  t.rtInv = (float)(1.0 / meta[3]);
+  t.mRes = meta[4];
+  t.wMax = meta[5];
+  t.gamma2 = (float)meta[6];
+  t.acc1 = (float)meta[7];
+  t.acc2 = (float)meta[8];
+  std::vector<std::vector<orc::branch::Node>> trees((size_t)n);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t j = 0; j < n; ++j)
+    orc::branch::grow(t, rootMass[j], meta[9], orc::branch::root_key(seed, tree0 + j), trees[(size_t)j]);
+  int64_t total = 0;
+  for (const auto& tr : trees) total += (int64_t)tr.size();
+  if (total > cap) return -total;
+  int64_t off = 0;
+  for (int64_t j = 0; j < n; ++j) {
+    treeFirst[j] = off;
+    for (const auto& nd : trees[(size_t)j]) {
+      mass[off] = nd.mass;
+      w[off] = nd.w;
+      parent[off] = nd.parent;
+      childFirst[off] = nd.childFirst;
+      childCount[off] = nd.childCount;
+      ++off;
+    }
+  }
+  return total;
+}
+
 }  // extern "C"

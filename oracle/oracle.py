@@ -176,3 +176,43 @@ def evolve_forest(params, table, forest, state0, output_times, threads=0, brent=
     if rc != 0:
         raise RuntimeError(f"oracle_evolve_forest failed with code {rc}")
     return state, status, counters, snap[:, :m]
+
+
+def grow_trees(tables, seed, root_masses, tree0=0):
+    """Grow trees tree0, tree0+1, ... of seed from their root masses with
+    the oracle's restatement of the GPU branching's walk, on the builder's
+    tables (forest.branch_tables).  Returns (mass, w, parent, child_first,
+    child_count, tree_first): the trees one after another, each in the
+    builder's order."""
+    l = lib()
+    vp = ctypes.c_void_p
+    l.oracle_grow_trees.argtypes = [vp] * 7 + [ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64, vp, ctypes.c_int64] + \
+        [vp] * 6
+    l.oracle_grow_trees.restype = ctypes.c_int64
+    roots = np.ascontiguousarray(root_masses, dtype=np.float64)
+    n = len(roots)
+    tree_first = np.zeros(n, np.int64)
+    cap = max(1024, 64 * n)
+    while True:
+        out = [np.zeros(cap), np.zeros(cap)] + [np.zeros(cap, np.int32) for _ in range(3)]
+        ptr = lambda a: a.ctypes.data_as(vp)
+        total = l.oracle_grow_trees(ptr(tables["meta"]), ptr(tables["sizes"]), ptr(tables["ln_sigma"]),
+                                    ptr(tables["rate"]), ptr(tables["accretion"]), ptr(tables["ln_q"]),
+                                    ptr(tables["cdf"]), seed, tree0, n, ptr(roots), cap, *[ptr(a) for a in out],
+                                    ptr(tree_first))
+        if total >= 0:
+            return tuple(a[:total] for a in out) + (tree_first,)
+        cap = -total
+
+
+def branch_math(x, y):
+    """The branching walk's FP32 ln (of positive doubles x) and exp (of floats y)."""
+    l = lib()
+    vp = ctypes.c_void_p
+    l.oracle_branch_math.argtypes = [ctypes.c_int64, vp, vp, vp, vp]
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    lx, ey = np.zeros(len(x), np.float32), np.zeros(len(y), np.float32)
+    l.oracle_branch_math(len(x), x.ctypes.data_as(vp), lx.ctypes.data_as(vp), y.ctypes.data_as(vp),
+                         ey.ctypes.data_as(vp))
+    return lx, ey

@@ -1,0 +1,95 @@
+"""The tree builder's branching on the GPU (gal_gpu_forest_build) against
+the oracle's restatement of its walk: on the same roots and tables, every
+tree is the oracle's bit for bit (topology, masses; the walk uses only
+IEEE-defined operations and neither side contracts to FMA), and its times
+are a function of the oracle's w.  Builds are deterministic, agree with the
+host builder in distribution, and forests with satellites come out valid
+and evolve."""
+
+import numpy as np
+import pytest
+
+from galacticus_gb300 import forest, workloads
+
+pytestmark = pytest.mark.gpu
+
+SPEC = dict(seed=3, root_mass_min=1e10, root_mass_max=1e13, mass_resolution=1e8)
+
+
+@pytest.fixture(scope="module")
+def params():
+    return workloads.isolated_params()
+
+
+@pytest.fixture(scope="module")
+def evolver(params, table):
+    from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
+    ev = MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision="fp32")
+    yield ev
+    ev.close()
+
+
+@pytest.fixture(scope="module")
+def built(params, evolver):
+    return forest.build(params, n_trees=1024, gpu=evolver, **SPEC)
+
+
+def _tree_slices(f):
+    starts = np.flatnonzero(np.diff(np.append(-1, f.tree)) != 0)
+    return starts, np.append(starts[1:], f.n)
+
+
+def test_gpu_branching_matches_the_oracle(built, params, oracle_mod):
+    f = built
+    starts, ends = _tree_slices(f)
+    assert len(starts) == 1024 and np.all(f.parent[starts] == -1)
+    tables = forest.branch_tables(params, **SPEC)
+    mass, w, parent, child_first, child_count, tree_first = oracle_mod.grow_trees(tables, SPEC["seed"], f.mass[starts])
+    o_ends = np.append(tree_first[1:], len(mass))
+    assert f.n == len(mass)
+    np.testing.assert_array_equal(starts, tree_first)
+    local = np.repeat(starts, ends - starts)
+    np.testing.assert_array_equal(np.where(f.parent >= 0, f.parent - local, -1), parent)
+    np.testing.assert_array_equal(f.child_count, child_count)
+    has = child_count > 0  # (a split with both progenitors unresolved leaves the oracle's first index set)
+    np.testing.assert_array_equal((f.child_first - local)[has], child_first[has])
+    np.testing.assert_array_equal(f.mass, mass)
+    # Times are a decreasing function of w (w = delta_c0/D grows into the
+    # past), equal w giving equal times.
+    order = np.argsort(w, kind="stable")
+    assert np.all(np.diff(f.time[order]) <= 0.0)
+    assert np.all(np.diff(f.time[order])[np.diff(w[order]) == 0.0] == 0.0)
+
+
+def test_gpu_branching_is_deterministic(built, params, evolver):
+    again = forest.build(params, n_trees=1024, gpu=evolver, **SPEC)
+    for name in ("parent", "child_first", "child_count", "mass", "time", "spin"):
+        np.testing.assert_array_equal(getattr(again, name), getattr(built, name))
+
+
+def test_gpu_branching_agrees_with_the_host_builder_in_distribution(built, params):
+    host = forest.build(params, n_trees=1024, **SPEC)
+    np.testing.assert_array_equal(host.mass[host.parent < 0], built.mass[built.parent < 0])
+    assert abs(built.n / host.n - 1.0) < 0.03, (built.n, host.n)
+    bins = np.linspace(8.0, 13.0, 11)
+    h_host = np.histogram(np.log10(host.mass[host.child_count == 0]), bins)[0]
+    h_gpu = np.histogram(np.log10(built.mass[built.child_count == 0]), bins)[0]
+    ok = (h_host + h_gpu) > 50
+    chi2 = np.sum((h_host - h_gpu)[ok] ** 2 / (h_host + h_gpu)[ok])
+    assert chi2 < 2.0 * ok.sum() + 10, (h_host, h_gpu)
+
+
+def test_gpu_built_forest_with_satellites_evolves(params, evolver, table):
+    f = forest.build(params, n_trees=64, gpu=evolver, satellites=forest.SATELLITES_JIANG2008, **SPEC)
+    host = f.satellite_host
+    phases = np.flatnonzero(host >= 0)
+    assert len(phases) > 100
+    assert np.all(f.time[phases] == f.time[host[phases]])
+    state0 = forest.initial_state(params, f)
+    times = forest.output_times(params)
+    fe = forest.ForestEvolver(evolver, f, state0, times)
+    fe.evolve()
+    state, status = fe.results()[:2]
+    fe.close()
+    assert np.all(status == 0)
+    assert np.all(np.isfinite(state))
