@@ -49,59 +49,63 @@ namespace trees {
 namespace {
 
 // ln 2 split for the Cody & Waite reduction: kLn2Hi = 355/512 (exact in 9
-// bits, so k kLn2Hi is exact for |k| < 2^15), kLn2Lo = ln 2 - kLn2Hi.
+// bits, so e kLn2Hi is exact for |e| < 2^15), kLn2Lo = ln 2 - kLn2Hi; the
+// same split of ln 2 / 32 for the exponential.
 constexpr float kLn2Hi = 0.693359375f;
 constexpr float kLn2Lo = -2.12194440e-4f;
-constexpr float kInvLn2 = 1.44269504f;
+constexpr float kLn2By32Hi = 0.0216674805f;   // 355/16384
+constexpr float kLn2By32Lo = -6.63107626e-6f;  // (ln 2 - 355/512)/32
+constexpr float k32ByLn2 = 46.1662445f;
 
-// ln x in FP32 for a positive normal double x: x = 2^e f with f from the
-// top 23 mantissa bits (truncated), moved into [sqrt(1/2), sqrt(2)); then
-// ln x = e ln 2 + 2 atanh(s), s = (f - 1)/(f + 1), |s| < 0.172, with the
-// series of atanh to s^11 (truncation < 3e-10).
-__device__ __forceinline__ float ln_pos(double x) {
+// The walk's function tables (shared memory): for the logarithm, ln c_j and
+// 1/c_j at c_j = 1 + (j + 1/2)/128; for the exponential, 2^(j/32).
+struct FnTables {
+  const float* lnc;
+  const float* invc;
+  const float* pow2;
+};
+
+// ln x in FP32 for a positive normal double x, after Tang (1990, ACM TOMS
+// 16, 378): x = 2^e f, f in [1, 2) (its top 23 mantissa bits, truncated),
+// c_j the centre of f's 1/128 interval, r = f/c_j - 1 (|r| < 2^-8), and
+// ln x = e ln 2 + ln c_j + ln(1 + r), ln(1 + r) = r - r^2/2 + r^3/3
+// (truncation < 1e-10).
+__device__ __forceinline__ float ln_pos(double x, const FnTables& t) {
   const long long b = __double_as_longlong(x);
-  int e = (int)(b >> 52) - 1023;
-  float f = __int_as_float(0x3f800000 | (int)((b >> 29) & 0x7fffff));
-  if (f > 1.41421354f) {
-    f *= 0.5f;
-    e += 1;
-  }
-  const float s = (f - 1.0f) / (f + 1.0f);
-  const float z = s * s;
-  float p = fmaf(1.0f / 11.0f, z, 1.0f / 9.0f);
-  p = fmaf(p, z, 1.0f / 7.0f);
-  p = fmaf(p, z, 1.0f / 5.0f);
-  p = fmaf(p, z, 1.0f / 3.0f);
-  p = fmaf(p, z, 1.0f);
+  const int e = (int)(b >> 52) - 1023;
+  const int j = (int)((b >> 45) & 127);
+  const float f = __int_as_float(0x3f800000 | (int)((b >> 29) & 0x7fffff));
+  const float r = fmaf(f, t.invc[j], -1.0f);
+  const float p = fmaf(fmaf(r, 1.0f / 3.0f, -0.5f), r * r, r);
   const float ef = (float)e;
-  return fmaf(ef, kLn2Hi, fmaf(ef, kLn2Lo, (2.0f * s) * p));
+  return fmaf(ef, kLn2Hi, fmaf(ef, kLn2Lo, t.lnc[j] + p));
 }
 
-// e^x in FP32 for |x| < 80: x = k ln 2 + r (Cody & Waite), |r| <= 0.347,
-// e^r from its Taylor series to r^7 (truncation < 6e-9), scaled by 2^k.
-__device__ __forceinline__ float exp_f(float x) {
+// e^x in FP32 for |x| < 80, after Tang (1989, ACM TOMS 15, 144): x =
+// (32 k + j) ln 2/32 + r, |r| <= ln 2/64, e^x = 2^k 2^(j/32) e^r with
+// e^r = 1 + r + r^2/2 + r^3/6 (truncation < 6e-10).
+__device__ __forceinline__ float exp_f(float x, const FnTables& t) {
   x = fminf(fmaxf(x, -80.0f), 80.0f);
-  const float k = rintf(x * kInvLn2);
-  const float r = fmaf(-k, kLn2Lo, fmaf(-k, kLn2Hi, x));
-  float p = fmaf(1.0f / 5040.0f, r, 1.0f / 720.0f);
-  p = fmaf(p, r, 1.0f / 120.0f);
-  p = fmaf(p, r, 1.0f / 24.0f);
-  p = fmaf(p, r, 1.0f / 6.0f);
-  p = fmaf(p, r, 0.5f);
-  p = fmaf(p, r, 1.0f);
-  p = fmaf(p, r, 1.0f);
-  return p * __int_as_float(((int)k + 127) << 23);
+  const float n = rintf(x * k32ByLn2);
+  const int ni = (int)n;
+  const int j = ni & 31;
+  const int k = ni >> 5;
+  const float r = fmaf(-n, kLn2By32Lo, fmaf(-n, kLn2By32Hi, x));
+  const float p = fmaf(fmaf(fmaf(r, 1.0f / 6.0f, 0.5f), r, 1.0f), r, 1.0f);
+  return (t.pow2[j] * p) * __int_as_float((k + 127) << 23);
 }
 
 struct DevTables {
-  // FP32 copies of ln sigma, R and F (staged in shared memory), the FP64
-  // split tables (read on splits only) and the walk's constants.
+  // FP32 copies of ln sigma, R and F and the function tables (staged in
+  // shared memory), the FP64 split tables (read on splits only) and the
+  // walk's constants.
+  const float* fn;  // [128 ln c_j][128 1/c_j][32 2^(j/32)]
   const float* lnSigma;
   const float* R;
   const float* F;
-  const double* Rd;
-  const double* lnq;
-  const double* cdf;
+  const float* lnqA;  // per rate row: ln q of its first point and the spacing in ln q
+  const float* lnqD;
+  const float* cdf;   // [rows][kNq]
   int32_t nSigma, rows;
   float sigLnMin, sigInv, halfShift, rtLnMin, rtInv, gamma2, accuracyFirst, accuracySecond;
   double mRes, mRes2, wMax;
@@ -154,15 +158,22 @@ __global__ void __launch_bounds__(128) grow_kernel(DevTables tab, DevNodes nd, c
                                                    int32_t nFrontier, int32_t* __restrict__ next,
                                                    unsigned long long* counters) {
   extern __shared__ float smem[];
-  float* lnSigma = smem;
+  float* fn = smem;
+  float* lnSigma = fn + kFnTable;
   float* Rt = lnSigma + tab.nSigma;
   float* Ft = Rt + tab.rows;
+  float* qA = Ft + tab.rows;
+  float* qD = qA + tab.rows;
+  for (int k = threadIdx.x; k < kFnTable; k += blockDim.x) fn[k] = tab.fn[k];
   for (int k = threadIdx.x; k < tab.nSigma; k += blockDim.x) lnSigma[k] = tab.lnSigma[k];
   for (int k = threadIdx.x; k < tab.rows; k += blockDim.x) {
     Rt[k] = tab.R[k];
     Ft[k] = tab.F[k];
+    qA[k] = tab.lnqA[k];
+    qD[k] = tab.lnqD[k];
   }
   __syncthreads();
+  const FnTables ft{fn, fn + 128, fn + 256};
   const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= nFrontier) return;
   int64_t i = frontier[slot];
@@ -177,36 +188,45 @@ __global__ void __launch_bounds__(128) grow_kernel(DevTables tab, DevNodes nd, c
     bool split = false;
     int guard = 0;
     while (bits(w) < bMax && bits(m) >= bRes && ++guard < 100000) {
-      const float lm = ln_pos(m);
+      const float lm = ln_pos(m, ft);
       const float x = (lm - tab.rtLnMin) * tab.rtInv;
       const float xs = (lm - tab.sigLnMin) * tab.sigInv;
       const float lns2 = interp(lnSigma, tab.nSigma, xs);
-      const float S2 = exp_f(2.0f * lns2);
-      const float Sh = exp_f(2.0f * interp(lnSigma, tab.nSigma, xs - tab.halfShift));
-      const float wf = exp_f(tab.gamma2 * (ln_pos(w) - lns2));
+      const float S2 = exp_f(2.0f * lns2, ft);
+      const float Sh = exp_f(2.0f * interp(lnSigma, tab.nSigma, xs - tab.halfShift), ft);
+      const float wf = exp_f(tab.gamma2 * (ln_pos(w, ft) - lns2), ft);
       const float xc = fminf(fmaxf(x, 0.0f), (float)(tab.rows - 1));
       const int j = min((int)xc, tab.rows - 2);
       const float fx = xc - (float)j;
       const float R = bits(m) <= bRes2 ? 0.0f : wf * (Rt[j] + fx * (Rt[j + 1] - Rt[j]));
       const float F = wf * (Ft[j] + fx * (Ft[j + 1] - Ft[j]));
+      // min(dw_sigma, acc/R, acc/F) with one division (acc/max(R, F) is the
+      // smaller quotient, rounding being monotone).
       float dwf = tab.accuracySecond * sqrtf(2.0f * fmaxf(Sh - S2, 0.0f));
-      if (R > 0.0f) dwf = fminf(dwf, tab.accuracyFirst / R);
-      if (F > 0.0f) dwf = fminf(dwf, tab.accuracyFirst / F);
+      const float RF = fmaxf(R, F);
+      if (RF > 0.0f) dwf = fminf(dwf, tab.accuracyFirst / RF);
       if (!(dwf > 0.0f)) dwf = 1.0e-3f;
       double dw = f2d_int(dwf);
       const double wStep = w + dw;
       const bool last = bits(wStep) >= bMax;
-      if (last) dw = tab.wMax - w;
+      if (last) {
+        dw = tab.wMax - w;
+        dwf = (float)dw;
+      }
       const double wNext = last ? tab.wMax : wStep;
+      // The mass kept over the step (the rest falls below the resolution).
+      const double keep = f2d_int(1.0f - F * dwf);
       mPrev = m;
       wPrev = w;
-      if (R > 0.0f && bits(draw(key, k++)) < bits(f2d_int(R) * dw)) {
+      if (R > 0.0f && draw24(key, k++) < R * dwf) {
+        // q from the split's distribution in ln q of the nearest row with
+        // a resolved split (its q range is that row's): the first point of
+        // the cumulative distribution above a second draw, and linear
+        // interpolation in ln q (the row's points are evenly spaced).
         int row = fx < 0.5f ? j : j + 1;
-        if (!(tab.Rd[row] > 0.0)) row = j + 1;
-        const double* cdf = tab.cdf + (size_t)row * kNq;
-        const double* lnq = tab.lnq + (size_t)row * kNq;
-        const double target = draw(key, k++);
-        // The first point of the cumulative distribution above target.
+        if (!(Rt[row] > 0.0f)) row = j + 1;
+        const float* cdf = tab.cdf + (size_t)row * kNq;
+        const float target = draw24(key, k++);
         int lo = 0, hi = kNq;
         while (lo < hi) {
           const int mid = (lo + hi) >> 1;
@@ -216,10 +236,11 @@ __global__ void __launch_bounds__(128) grow_kernel(DevTables tab, DevNodes nd, c
             lo = mid + 1;
         }
         const int k1 = min(max(lo, 1), kNq - 1);
-        const double f = (target - cdf[k1 - 1]) / fmax(cdf[k1] - cdf[k1 - 1], 1e-300);
-        const double q = f2d_int(exp_f((float)(lnq[k1 - 1] + f * (lnq[k1] - lnq[k1 - 1]))));
+        const float c0 = cdf[k1 - 1];
+        const float f = (target - c0) / fmaxf(cdf[k1] - c0, 1e-30f);
+        const double q = f2d_int(exp_f(fmaf((float)(k1 - 1) + f, qD[row], qA[row]), ft));
         const double m1 = q * m;
-        const double m2 = m * (1.0 - f2d_int(F) * dw) - m1;
+        const double m2 = m * keep - m1;
         const double big = fmax(m1, m2), small = fmin(m1, m2);
         const int count = (big >= tab.mRes) + (small >= tab.mRes);
         if (count > 0) {
@@ -238,7 +259,7 @@ __global__ void __launch_bounds__(128) grow_kernel(DevTables tab, DevNodes nd, c
         split = true;
         break;
       }
-      m *= 1.0 - f2d_int(F) * dw;
+      m *= keep;
       w = wNext;
       if (last) break;
     }
@@ -304,20 +325,22 @@ int grow_forest_gpu(gal_ctx* ctx, const BranchTables& tab, const double* rootMas
   {
     std::vector<float> ls(tab.lnSigma, tab.lnSigma + tab.nSigma), rf(tab.R, tab.R + tab.rows),
         ff(tab.F, tab.F + tab.rows);
-    float *a = nullptr, *c = nullptr, *d = nullptr;
-    double *rd = nullptr, *q = nullptr, *f = nullptr;
-    if ((e = tb.put(&a, ls.data(), ls.size())) != cudaSuccess || (e = tb.put(&c, rf.data(), rf.size())) != cudaSuccess ||
-        (e = tb.put(&d, ff.data(), ff.size())) != cudaSuccess ||
-        (e = tb.put(&rd, tab.R, (size_t)tab.rows)) != cudaSuccess ||
-        (e = tb.put(&q, tab.lnq, (size_t)tab.rows * kNq)) != cudaSuccess ||
-        (e = tb.put(&f, tab.cdf, (size_t)tab.rows * kNq)) != cudaSuccess)
+    const std::vector<float> fnt = function_tables();
+    std::vector<float> qa((size_t)tab.rows), qd((size_t)tab.rows), cdff((size_t)tab.rows * kNq);
+    split_tables(tab, qa.data(), qd.data(), cdff.data());
+    float *fnd = nullptr, *a = nullptr, *c = nullptr, *d = nullptr, *pa = nullptr, *pd = nullptr, *cf = nullptr;
+    if ((e = tb.put(&fnd, fnt.data(), fnt.size())) != cudaSuccess || (e = tb.put(&a, ls.data(), ls.size())) != cudaSuccess ||
+        (e = tb.put(&c, rf.data(), rf.size())) != cudaSuccess || (e = tb.put(&d, ff.data(), ff.size())) != cudaSuccess ||
+        (e = tb.put(&pa, qa.data(), qa.size())) != cudaSuccess || (e = tb.put(&pd, qd.data(), qd.size())) != cudaSuccess ||
+        (e = tb.put(&cf, cdff.data(), cdff.size())) != cudaSuccess)
       return fail(ctx, GAL_ERR_CUDA, "gal_gpu_forest_build: table upload failed: %s", cudaGetErrorString(e));
+    dt.fn = fnd;
     dt.lnSigma = a;
     dt.R = c;
     dt.F = d;
-    dt.Rd = rd;
-    dt.lnq = q;
-    dt.cdf = f;
+    dt.lnqA = pa;
+    dt.lnqD = pd;
+    dt.cdf = cf;
   }
   const WalkConstants wc = walk_constants(tab);
   dt.nSigma = tab.nSigma;
@@ -333,7 +356,7 @@ int grow_forest_gpu(gal_ctx* ctx, const BranchTables& tab, const double* rootMas
   dt.mRes = tab.mRes;
   dt.mRes2 = 2.0 * tab.mRes;
   dt.wMax = tab.wMax;
-  const size_t smem = (size_t)(tab.nSigma + 2 * tab.rows) * sizeof(float);
+  const size_t smem = (size_t)(kFnTable + tab.nSigma + 4 * tab.rows) * sizeof(float);
   if (tab.nSigma < 2 || tab.rows < 2 || smem > 200 * 1024)
     return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_build: branching tables too large for shared memory%s");
   if ((e = cudaFuncSetAttribute(grow_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)

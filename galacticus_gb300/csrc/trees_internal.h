@@ -15,6 +15,7 @@
 #ifndef GALNODE_TREES_INTERNAL_H
 #define GALNODE_TREES_INTERNAL_H
 
+#include <cmath>
 #include <cstdint>
 #include <vector>
 
@@ -70,9 +71,39 @@ GAL_HD uint64_t root_key(uint64_t seed, int64_t tree) {
 }
 // The key of progenitor c (0 the larger) of the node with key k.
 GAL_HD uint64_t child_key(uint64_t k, int c) { return mix64(k ^ (0xa0761d6478bd642full * (uint64_t)(c + 1))); }
-// The k-th uniform draw in [0, 1) of the stream with key `key`.
+// The k-th uniform draw in [0, 1) of the stream with key `key`, to 53 bits
+// (draw) or to 24 bits as a float (draw24).
 GAL_HD double draw(uint64_t key, uint32_t k) {
   return (double)(mix64(key + (uint64_t)(k + 1) * kGamma) >> 11) * 0x1.0p-53;
+}
+GAL_HD float draw24(uint64_t key, uint32_t k) {
+  return (float)(uint32_t)(mix64(key + (uint64_t)(k + 1) * kGamma) >> 40) * 0x1.0p-24f;
+}
+
+// The walk's function tables, as floats: ln c_j [128], 1/c_j [128] at
+// c_j = 1 + (j + 1/2)/128, then 2^(j/32) [32], rounded from FP64.
+constexpr int kFnTable = 128 + 128 + 32;
+inline std::vector<float> function_tables() {
+  std::vector<float> t(kFnTable);
+  for (int j = 0; j < 128; ++j) {
+    const double c = 1.0 + (j + 0.5) / 128.0;
+    t[(size_t)j] = (float)std::log(c);
+    t[(size_t)(128 + j)] = (float)(1.0 / c);
+  }
+  for (int j = 0; j < 32; ++j) t[(size_t)(256 + j)] = (float)std::exp2(j / 32.0);
+  return t;
+}
+
+// The FP32 split tables of the GPU walk: per rate row, ln q at its first
+// point and the spacing of its (evenly spaced) points in ln q, and the
+// cumulative distribution [rows][kNq], rounded from the FP64 tables.
+inline void split_tables(const BranchTables& t, float* lnqA, float* lnqD, float* cdf) {
+  for (int32_t r = 0; r < t.rows; ++r) {
+    const double* q = t.lnq + (size_t)r * kNq;
+    lnqA[r] = (float)q[0];
+    lnqD[r] = (float)((q[kNq - 1] - q[0]) / (kNq - 1));
+    for (int k = 0; k < kNq; ++k) cdf[(size_t)r * kNq + k] = (float)t.cdf[(size_t)r * kNq + k];
+  }
 }
 
 // The FP32 constants of the GPU walk, rounded from the FP64 tables' grid:

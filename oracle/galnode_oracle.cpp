@@ -1752,9 +1752,12 @@ int oracle_evolve_forest(const gal_params* p, const gal_cie_table* table, int64_
 // builder.
 //
 // This is the GPU walk's specification: the rates in FP32 from FP32 copies
-// of the tables, its logarithm and exponential (Cody & Waite 1980 argument
-// reduction; the series of atanh to s^11 and of exp to r^7, evaluated with
-// fmaf), the mass and w accumulated in FP64, and each node's branch drawing
+// of the tables, its table-driven logarithm and exponential (Tang 1990,
+// 1989; Cody & Waite 1980 argument reduction; short series evaluated with
+// fmaf), the step limit with one division, the split test on a 24-bit draw
+// and the kept mass fraction in FP32, the split's q from FP32 copies of its
+// distribution, the mass and w accumulated in FP64,
+// and each node's branch drawing
 // from its own SplitMix64 stream (Steele, Lea & Flood 2014) keyed by its
 // tree and its path from the root.  Every operation is IEEE-defined, so
 // the GPU's trees must equal these bit for bit.
@@ -1774,52 +1777,73 @@ uint64_t root_key(uint64_t seed, int64_t tree) {
 uint64_t child_key(uint64_t k, int c) { return mix64(k ^ (0xa0761d6478bd642full * (uint64_t)(c + 1))); }
 double draw(uint64_t key, uint32_t k) { return (double)(mix64(key + (uint64_t)(k + 1) * kGamma) >> 11) * 0x1.0p-53; }
 
-constexpr float kLn2Hi = 0.693359375f;     // 355/512
-constexpr float kLn2Lo = -2.12194440e-4f;  // ln 2 - 355/512
-constexpr float kInvLn2 = 1.44269504f;
+constexpr float kLn2Hi = 0.693359375f;          // 355/512
+constexpr float kLn2Lo = -2.12194440e-4f;       // ln 2 - 355/512
+constexpr float kLn2By32Hi = 0.0216674805f;     // 355/16384
+constexpr float kLn2By32Lo = -6.63107626e-6f;   // (ln 2 - 355/512)/32
+constexpr float k32ByLn2 = 46.1662445f;
 
+// Function tables: ln c_j and 1/c_j at c_j = 1 + (j + 1/2)/128 (Tang 1990,
+// ACM TOMS 16, 378), 2^(j/32) (Tang 1989, ACM TOMS 15, 144), as floats.
+struct FnTables {
+  float lnc[128], invc[128], pow2[32];
+  FnTables() {
+    for (int j = 0; j < 128; ++j) {
+      const double c = 1.0 + (j + 0.5) / 128.0;
+      lnc[j] = (float)std::log(c);
+      invc[j] = (float)(1.0 / c);
+    }
+    for (int j = 0; j < 32; ++j) pow2[j] = (float)std::exp2(j / 32.0);
+  }
+};
+const FnTables& fn_tables() {
+  static const FnTables t;
+  return t;
+}
+
+// ln x for a positive normal double: x = 2^e f, f in [1, 2) from its top 23
+// mantissa bits (truncated), r = f/c_j - 1 with c_j the centre of f's 1/128
+// interval, ln x = e ln 2 + ln c_j + r - r^2/2 + r^3/3.
 float ln_pos(double x) {
+  const FnTables& t = fn_tables();
   int64_t b;
   std::memcpy(&b, &x, sizeof b);
-  int e = (int)(b >> 52) - 1023;
+  const int e = (int)(b >> 52) - 1023;
+  const int j = (int)((b >> 45) & 127);
   const uint32_t fb = 0x3f800000u | (uint32_t)((b >> 29) & 0x7fffff);
   float f;
   std::memcpy(&f, &fb, sizeof f);
-  if (f > 1.41421354f) {
-    f *= 0.5f;
-    e += 1;
-  }
-  const float s = (f - 1.0f) / (f + 1.0f);
-  const float z = s * s;
-  float p = std::fmaf(1.0f / 11.0f, z, 1.0f / 9.0f);
-  p = std::fmaf(p, z, 1.0f / 7.0f);
-  p = std::fmaf(p, z, 1.0f / 5.0f);
-  p = std::fmaf(p, z, 1.0f / 3.0f);
-  p = std::fmaf(p, z, 1.0f);
+  const float r = std::fmaf(f, t.invc[j], -1.0f);
+  const float p = std::fmaf(std::fmaf(r, 1.0f / 3.0f, -0.5f), r * r, r);
   const float ef = (float)e;
-  return std::fmaf(ef, kLn2Hi, std::fmaf(ef, kLn2Lo, (2.0f * s) * p));
+  return std::fmaf(ef, kLn2Hi, std::fmaf(ef, kLn2Lo, t.lnc[j] + p));
 }
 
+// e^x for |x| < 80: x = (32 k + j) ln 2/32 + r, e^x = 2^k 2^(j/32) e^r with
+// e^r = 1 + r + r^2/2 + r^3/6.
 float exp_f(float x) {
+  const FnTables& t = fn_tables();
   x = std::fmin(std::fmax(x, -80.0f), 80.0f);
-  const float k = std::rint(x * kInvLn2);
-  const float r = std::fmaf(-k, kLn2Lo, std::fmaf(-k, kLn2Hi, x));
-  float p = std::fmaf(1.0f / 5040.0f, r, 1.0f / 720.0f);
-  p = std::fmaf(p, r, 1.0f / 120.0f);
-  p = std::fmaf(p, r, 1.0f / 24.0f);
-  p = std::fmaf(p, r, 1.0f / 6.0f);
-  p = std::fmaf(p, r, 0.5f);
-  p = std::fmaf(p, r, 1.0f);
-  p = std::fmaf(p, r, 1.0f);
-  const uint32_t sb = (uint32_t)((int)k + 127) << 23;
+  const float n = std::rint(x * k32ByLn2);
+  const int ni = (int)n;
+  const int j = ni & 31;
+  const int k = ni >> 5;
+  const float r = std::fmaf(-n, kLn2By32Lo, std::fmaf(-n, kLn2By32Hi, x));
+  const float p = std::fmaf(std::fmaf(std::fmaf(r, 1.0f / 6.0f, 0.5f), r, 1.0f), r, 1.0f);
+  const uint32_t sb = (uint32_t)(k + 127) << 23;
   float scale;
   std::memcpy(&scale, &sb, sizeof scale);
-  return p * scale;
+  return (t.pow2[j] * p) * scale;
+}
+
+float draw24(uint64_t key, uint32_t k) {
+  return (float)(uint32_t)(mix64(key + (uint64_t)(k + 1) * kGamma) >> 40) * 0x1.0p-24f;
 }
 
 struct Tables {
   std::vector<float> lnSigma, R, F;  // FP32 copies
-  const double *Rd, *lnq, *cdf;      // FP64 split tables
+  std::vector<float> lnqA, lnqD;     // per row: ln q of the first point, spacing in ln q
+  std::vector<float> cdf;            // [rows][kNq], FP32
   float sigLnMin, sigInv, halfShift, rtLnMin, rtInv, gamma2, acc1, acc2;
   double mRes, wMax;
   static constexpr int kNq = 96;
@@ -1867,28 +1891,32 @@ void grow(const Tables& t, double rootMass, double rootW, uint64_t rootKey, std:
       const float R = m <= 2.0 * t.mRes ? 0.0f : wf * (t.R[(size_t)j] + fx * (t.R[(size_t)j + 1] - t.R[(size_t)j]));
       const float F = wf * (t.F[(size_t)j] + fx * (t.F[(size_t)j + 1] - t.F[(size_t)j]));
       float dwf = t.acc2 * std::sqrt(2.0f * std::fmax(Sh - S2, 0.0f));
-      if (R > 0.0f) dwf = std::fmin(dwf, t.acc1 / R);
-      if (F > 0.0f) dwf = std::fmin(dwf, t.acc1 / F);
+      const float RF = std::fmax(R, F);
+      if (RF > 0.0f) dwf = std::fmin(dwf, t.acc1 / RF);
       if (!(dwf > 0.0f)) dwf = 1.0e-3f;
       double dw = (double)dwf;
       const double wStep = w + dw;
       const bool last = wStep >= t.wMax;
-      if (last) dw = t.wMax - w;
+      if (last) {
+        dw = t.wMax - w;
+        dwf = (float)dw;
+      }
       const double wNext = last ? t.wMax : wStep;
+      const double keep = (double)(1.0f - F * dwf);
       mPrev = m;
       wPrev = w;
-      if (R > 0.0f && draw(key, k++) < (double)R * dw) {
+      if (R > 0.0f && draw24(key, k++) < R * dwf) {
         int row = fx < 0.5f ? j : j + 1;
-        if (!(t.Rd[row] > 0.0)) row = j + 1;
-        const double* cdf = t.cdf + (size_t)row * nq;
-        const double* lnq = t.lnq + (size_t)row * nq;
-        const double target = draw(key, k++);
+        if (!(t.R[(size_t)row] > 0.0f)) row = j + 1;
+        const float* cdf = t.cdf.data() + (size_t)row * nq;
+        const float target = draw24(key, k++);
         const int kk = (int)(std::upper_bound(cdf, cdf + nq, target) - cdf);
         const int k1 = std::min(std::max(kk, 1), nq - 1);
-        const double f = (target - cdf[k1 - 1]) / std::max(cdf[k1] - cdf[k1 - 1], 1e-300);
-        const double q = (double)exp_f((float)(lnq[k1 - 1] + f * (lnq[k1] - lnq[k1 - 1])));
+        const float c0 = cdf[k1 - 1];
+        const float f = (target - c0) / std::fmax(cdf[k1] - c0, 1e-30f);
+        const double q = (double)exp_f(std::fmaf((float)(k1 - 1) + f, t.lnqD[(size_t)row], t.lnqA[(size_t)row]));
         const double m1 = q * m;
-        const double m2 = m * (1.0 - (double)F * dw) - m1;
+        const double m2 = m * keep - m1;
         const double big = std::max(m1, m2), small = std::min(m1, m2);
         const int32_t first = (int32_t)nodes.size();
         int32_t count = 0;
@@ -1900,7 +1928,7 @@ void grow(const Tables& t, double rootMass, double rootW, uint64_t rootKey, std:
         split = true;
         break;
       }
-      m *= 1.0 - (double)F * dw;
+      m *= keep;
       w = wNext;
       if (last) break;
     }
@@ -1947,9 +1975,14 @@ int64_t oracle_grow_trees(const double* meta, const int32_t* sizes, const double
   t.R.assign(rate, rate + sizes[1]);
   t.F.assign(accretion, accretion + sizes[1]);
   if (sizes[0] < 2 || sizes[1] < 2) return 0;
-  t.Rd = rate;
-  t.lnq = lnq;
-  t.cdf = cdf;
+  t.lnqA.resize((size_t)sizes[1]);
+  t.lnqD.resize((size_t)sizes[1]);
+  t.cdf.assign(cdf, cdf + (size_t)sizes[1] * orc::branch::Tables::kNq);
+  for (int32_t r = 0; r < sizes[1]; ++r) {
+    const double* q = lnq + (size_t)r * orc::branch::Tables::kNq;
+    t.lnqA[(size_t)r] = (float)q[0];
+    t.lnqD[(size_t)r] = (float)((q[orc::branch::Tables::kNq - 1] - q[0]) / (orc::branch::Tables::kNq - 1));
+  }
   t.sigLnMin = (float)meta[0];
   t.sigInv = (float)(1.0 / meta[1]);
   t.halfShift = (float)(0.6931471805599453 / meta[1]);

@@ -111,11 +111,12 @@ def test_gpu_build_needs_a_context(params):
 
 def test_walk_math_accuracy(oracle_mod):
     """The walk's FP32 ln and exp against numpy's FP64: ln to half an FP32
-    ulp of e ln 2 plus the mantissa's truncation, exp to ~1 FP32 ulp."""
+    ulp of e ln 2 plus the mantissa's truncation, exp to ~2 FP32 ulp (the
+    rounded 2^(j/32) table entry and two products)."""
     rng = np.random.default_rng(1)
     x = np.exp(rng.uniform(np.log(1e-3), np.log(1e17), 100_000))
     y = rng.uniform(-20.0, 20.0, 100_000).astype(np.float32)
     lx, ey = oracle_mod.branch_math(x, y)
     err = np.abs(lx.astype(np.float64) - np.log(x))
     assert np.all(err <= 2.5e-7 + 6.5e-8 * np.abs(np.log(x))), err.max()
-    assert np.max(np.abs(ey / np.exp(y.astype(np.float64)) - 1.0)) < 1.5e-7
+    assert np.max(np.abs(ey / np.exp(y.astype(np.float64)) - 1.0)) < 2.5e-7
