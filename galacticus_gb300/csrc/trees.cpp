@@ -513,10 +513,17 @@ void benson2005_orbit(std::mt19937_64& rng, double mu, double& ur, double& ut) {
   for (int attempt = 0; attempt < 1000000; ++attempt) {
     ur = U(rng) * velocityMax;
     ut = U(rng) * velocityMax;
+    const double y = pMax * U(rng);
+    // Unbound orbits and points above g >= f (the factor exp(-b1 (ur -
+    // b2)^2) <= 1 and rounding is monotone) are rejected before the rest of
+    // f is evaluated: the same decisions as the full test, on the same draws.
+    if (!(-1.0 + 0.5 * mu * (ur * ur + ut * ut) < -1.0e-4)) continue;
+    const double g = a[0] * ut * std::exp(-a[1] * (ut - a[8]) * (ut - a[8]));
+    if (!(y <= g)) continue;
     const double b1 = a[2] * std::exp(-a[3] * (ut - a[4]) * (ut - a[4]));
     const double b2 = a[5] * std::exp(-a[6] * (ut - a[7]) * (ut - a[7]));
-    const double f = a[0] * ut * std::exp(-a[1] * (ut - a[8]) * (ut - a[8])) * std::exp(-b1 * (ur - b2) * (ur - b2));
-    if (pMax * U(rng) <= f && -1.0 + 0.5 * mu * (ur * ur + ut * ut) < -1.0e-4) return;
+    const double f = g * std::exp(-b1 * (ur - b2) * (ur - b2));
+    if (y <= f) return;
   }
   ur = 0.0;  // not reached for the fit's distribution: a circular orbit
   ut = 1.0;
@@ -577,6 +584,25 @@ void add_satellites(const TreeIn& in, const std::vector<double>& spin, const Cos
   struct Event { double tm; int32_t sat; };
   std::vector<std::vector<Event>> events((size_t)n);  // merging events on each original node
   std::vector<int32_t> unmerged;
+  // Ancestor jumps for large trees: up[k][i] is the 2^k-th ancestor of i
+  // (-1 above the root); parents precede their progenitors in tr.
+  int levels = 0;
+  std::vector<int32_t> up;
+  if (n > 512) {
+    int32_t depth = 0;
+    std::vector<int32_t> dep((size_t)n, 0);
+    for (int32_t i = 0; i < n; ++i)
+      if (tr[i].parent >= 0) depth = std::max(depth, dep[(size_t)i] = dep[(size_t)tr[i].parent] + 1);
+    while ((1 << levels) <= depth) ++levels;
+    up.assign((size_t)levels * n, -1);
+    for (int32_t i = 0; i < n; ++i) {
+      up[(size_t)i] = tr[i].parent;
+      for (int k = 1; k < levels; ++k) {
+        const int32_t a = up[(size_t)(k - 1) * n + i];
+        up[(size_t)k * n + i] = a < 0 ? -1 : up[(size_t)(k - 1) * n + a];
+      }
+    }
+  }
   for (int32_t p = 0; p < n; ++p) {
     if (tr[p].childCount < 2) continue;
     const int32_t c0 = tr[p].childFirst;
@@ -603,9 +629,18 @@ void add_satellites(const TreeIn& in, const std::vector<double>& spin, const Cos
       const int32_t S = (int32_t)out.size();
       out.push_back(SatNode{ms, t[p], spin[s], -1, p, {s}});
       out[s].parent = S;
-      // The node alive at t_m on p's line of descendants.
+      // The node alive at t_m on p's line of descendants: the highest
+      // ancestor-or-self of p whose time is not after t_m (times grow
+      // towards the root, so jumps of 2^k ancestors find it).
       int32_t d = p;
-      while (tr[d].parent >= 0 && !(tm < t[tr[d].parent])) d = tr[d].parent;
+      if (up.empty()) {
+        while (tr[d].parent >= 0 && !(tm < t[tr[d].parent])) d = tr[d].parent;
+      } else {
+        for (int k = levels - 1; k >= 0; --k) {
+          const int32_t a = up[(size_t)k * n + d];
+          if (a >= 0 && !(tm < t[a])) d = a;
+        }
+      }
       if (tr[d].parent < 0 && !(tm < tEnd)) unmerged.push_back(S);
       else events[d].push_back(Event{tm, S});
     }
