@@ -437,7 +437,7 @@ def scale_record(args, params, table, net, gate):
     for sat in sorted({args.satellites, "none"}):
         for where in ("host", "gpu"):
             if where == "host" and sat == args.satellites:
-                builds[f"{where}_{sat}"] = {"s": build_s, "nodes": f.n}
+                builds[f"{where}_{sat}"] = {"s": build_s, "nodes": f.n, **f.build_stats}
                 continue
             tb = time.perf_counter()
             fb = forest.build(params, n_trees=args.trees_scale, seed=5, redshift_max=10.0, satellites=SATELLITES[sat],
