@@ -718,6 +718,14 @@ gal::trees::BranchTables branch_tables(const SigmaTable& sig, const RateTable& r
                                   B.mRes, B.wMax, pch.gamma2, pch.accuracy_first, pch.accuracy_second};
 }
 
+bool valid_spec(const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec) {
+  return p && pch && spec && valid_transfer(*pch) && spec->n_trees >= 0 && spec->mass_resolution > 0.0 &&
+         spec->root_mass_min >= spec->mass_resolution && spec->root_mass_max >= spec->root_mass_min &&
+         spec->redshift_max > spec->root_redshift && spec->root_redshift >= 0.0 && spec->redshift_max <= 30.0 &&
+         (spec->satellites == GAL_SATELLITES_NONE ||
+          (spec->satellites == GAL_SATELLITES_JIANG2008 && spec->satellite_timescale_multiplier >= 0.0));
+}
+
 // The forest of spec: branches grown on the host (ctx == nullptr: one
 // sequential stream per tree) or on the GPU of ctx (keyed streams).
 int build_forest(gal_ctx* ctx, const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec,
@@ -729,10 +737,7 @@ int build_forest(gal_ctx* ctx, const gal_params* p, const gal_pch_params* pch, c
   double stats[7] = {0, 0, 0, 0, 0, 0, 0};
   if (!out) return GAL_ERR_ARGUMENT;
   *out = nullptr;
-  if (!p || !pch || !spec || !valid_transfer(*pch) || spec->n_trees < 0 || !(spec->mass_resolution > 0.0) ||
-      !(spec->root_mass_min >= spec->mass_resolution) || !(spec->root_mass_max >= spec->root_mass_min) ||
-      !(spec->redshift_max > spec->root_redshift) || spec->root_redshift < 0.0 || spec->redshift_max > 30.0)
-    return GAL_ERR_ARGUMENT;
+  if (!valid_spec(p, pch, spec)) return GAL_ERR_ARGUMENT;
   const Cosmo c = cosmo_of(p);
   SigmaTable sig;
   sig.build(c, *pch);
@@ -743,9 +748,6 @@ int build_forest(gal_ctx* ctx, const gal_params* p, const gal_pch_params* pch, c
   const Builder B{sig, *pch, spec->mass_resolution, gt.w_of_z(spec->redshift_max), rt};
   stats[0] = since(tStart);
   const int64_t nTrees = spec->n_trees;
-  if (spec->satellites != GAL_SATELLITES_NONE &&
-      !(spec->satellites == GAL_SATELLITES_JIANG2008 && spec->satellite_timescale_multiplier >= 0.0))
-    return GAL_ERR_ARGUMENT;
   const bool satellites = spec->satellites == GAL_SATELLITES_JIANG2008;
   std::vector<std::vector<Builder::Node>> trees((size_t)nTrees);
   std::vector<std::vector<double>> spins((size_t)nTrees);
@@ -921,9 +923,10 @@ int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_f
 
 int gal_gpu_forest_build(gal_ctx* ctx, const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec,
                          gal_forest** out) {
-  if (!ctx) {
+  if (!ctx || !out || !valid_spec(p, pch, spec)) {
     if (out) *out = nullptr;
-    return GAL_ERR_ARGUMENT;
+    return ctx ? gal::trees::record_error(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_build: bad arguments")
+               : GAL_ERR_ARGUMENT;
   }
   return build_forest(ctx, p, pch, spec, out);
 }

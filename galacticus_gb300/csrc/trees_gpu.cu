@@ -312,6 +312,8 @@ struct Buffers {
 
 }  // namespace
 
+int record_error(gal_ctx* ctx, int code, const char* message) { return gal::host::fail(ctx, code, "%s", message); }
+
 int grow_forest_gpu(gal_ctx* ctx, const BranchTables& tab, const double* rootMass, int64_t n, double rootW,
                     uint64_t seed, std::vector<std::vector<GrownNode>>& trees, double* stats) {
   using gal::host::fail;

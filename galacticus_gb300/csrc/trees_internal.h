@@ -123,6 +123,10 @@ inline WalkConstants walk_constants(const BranchTables& t) {
 // trees[t] receives tree t in the host builder's order (depth first, the
 // larger progenitor first, a node's progenitors numbered when it splits).
 // Returns a GAL_* code (errors recorded in the context).
+// Record an error in the context (its message for gal_gpu_last_error) and
+// return code.
+int record_error(gal_ctx* ctx, int code, const char* message);
+
 // stats[3] receives the seconds of the device growth (its generations), of
 // the nodes' download and renumbering on the host, and the number of
 // generations.

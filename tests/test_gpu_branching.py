@@ -79,7 +79,12 @@ def test_gpu_branching_agrees_with_the_host_builder_in_distribution(built, param
     assert chi2 < 2.0 * ok.sum() + 10, (h_host, h_gpu)
 
 
-def test_gpu_built_forest_with_satellites_evolves(params, evolver, table):
+def test_gpu_built_forest_with_satellites_evolves(params, evolver, table, oracle_mod):
+    """A GPU-built forest with satellites through the whole pipeline: the
+    FP32-rate forest evolution against the oracle's evolution of the same
+    forest, node by node within the FP32-rate forms' bound."""
+    from oracle import compare
+    from galacticus_gb300 import _abi
     f = forest.build(params, n_trees=64, gpu=evolver, satellites=forest.SATELLITES_JIANG2008, **SPEC)
     host = f.satellite_host
     phases = np.flatnonzero(host >= 0)
@@ -92,4 +97,9 @@ def test_gpu_built_forest_with_satellites_evolves(params, evolver, table):
     state, status = fe.results()[:2]
     fe.close()
     assert np.all(status == 0)
-    assert np.all(np.isfinite(state))
+    ref, ref_status = oracle_mod.evolve_forest(params, table, f, state0, times, brent=False)[:2]
+    assert np.all(ref_status == 0)
+    param = np.zeros((_abi.NP, f.n))
+    param[_abi.P_MASS] = f.mass
+    within = np.all(np.abs(state - ref) <= compare.parity_bound(ref, ref, param, params), axis=0)
+    assert within.mean() > 0.995, within.mean()
