@@ -205,11 +205,12 @@ def build(params, n_trees, seed=3, root_mass_min=1e10, root_mass_max=1e14, root_
         _check(gpu.lib, gpu.ctx, lib.gal_gpu_forest_build(gpu.ctx, ctypes.byref(params), ctypes.byref(pch),
                                                           ctypes.byref(spec), ctypes.byref(handle)))
     n = lib.gal_forest_node_count(handle)
-    arrays = [np.zeros(n, np.int32) for _ in range(4)] + [np.zeros(n) for _ in range(3)]
+    # (every element is written by gal_forest_get)
+    arrays = [np.empty(n, np.int32) for _ in range(4)] + [np.empty(n) for _ in range(3)]
     lib.gal_forest_get(handle, *[_vp(a) for a in arrays])
     host = None
     if satellites != SATELLITES_NONE:
-        host = np.zeros(n, np.int32)
+        host = np.empty(n, np.int32)
         lib.gal_forest_get_satellite_host(handle, _vp(host))
     stats = np.zeros(7)
     lib.gal_forest_build_stats(handle, _vp(stats))
