@@ -535,12 +535,35 @@ struct TreeIn {
   std::vector<double> time;
 };
 
-// A node of a tree with satellites before it is laid out.
+// A node of a tree with satellites before it is laid out.  Its
+// progenitors form a list (primary first) linked through `next`, with its
+// first and last entries and its length.
 struct SatNode {
   double mass, time, spin;
   int32_t parent, satHost;  // satHost: the host at infall of a satellite phase, else -1
-  std::vector<int32_t> children;  // primary first
+  int32_t first = -1, last = -1, next = -1, count = 0;
 };
+
+SatNode sat_node(double mass, double time, double spin, int32_t parent, int32_t satHost) {
+  SatNode nd;
+  nd.mass = mass;
+  nd.time = time;
+  nd.spin = spin;
+  nd.parent = parent;
+  nd.satHost = satHost;
+  return nd;
+}
+
+// Append node c to the progenitors of node p.
+void append_child(std::vector<SatNode>& out, int32_t p, int32_t c) {
+  out[(size_t)c].next = -1;
+  if (out[(size_t)p].last < 0)
+    out[(size_t)p].first = c;
+  else
+    out[(size_t)out[(size_t)p].last].next = c;
+  out[(size_t)p].last = c;
+  ++out[(size_t)p].count;
+}
 
 // Satellites as the reference's tree evolver has them (merger_trees/
 // evolver/standard.F90: a secondary progenitor becomes a satellite at its
@@ -565,9 +588,9 @@ void add_satellites(const TreeIn& in, const std::vector<double>& spin, const Cos
   const std::vector<double>& t = in.time;
   out.clear();
   out.reserve((size_t)n * 2);
-  for (int32_t i = 0; i < n; ++i) out.push_back(SatNode{tr[i].mass, t[i], spin[i], tr[i].parent, -1, {}});
+  for (int32_t i = 0; i < n; ++i) out.push_back(sat_node(tr[i].mass, t[i], spin[i], tr[i].parent, -1));
   for (int32_t i = 0; i < n; ++i)
-    for (int32_t k = 0; k < tr[i].childCount; ++k) out[i].children.push_back(tr[i].childFirst + k);
+    for (int32_t k = 0; k < tr[i].childCount; ++k) append_child(out, i, tr[i].childFirst + k);
   // The halo mass a node reaches by time x (its mass line: a primary
   // progenitor grows by its parent's unresolved mass, others stay).
   auto massAt = [&](int32_t i, double x) {
@@ -627,7 +650,8 @@ void add_satellites(const TreeIn& in, const std::vector<double>& spin, const Cos
       }
       // The satellite phase S replaces s among p's progenitors.
       const int32_t S = (int32_t)out.size();
-      out.push_back(SatNode{ms, t[p], spin[s], -1, p, {s}});
+      out.push_back(sat_node(ms, t[p], spin[s], -1, p));
+      append_child(out, S, s);
       out[s].parent = S;
       // The node alive at t_m on p's line of descendants: the highest
       // ancestor-or-self of p whose time is not after t_m (times grow
@@ -644,7 +668,10 @@ void add_satellites(const TreeIn& in, const std::vector<double>& spin, const Cos
       if (tr[d].parent < 0 && !(tm < tEnd)) unmerged.push_back(S);
       else events[d].push_back(Event{tm, S});
     }
-    out[p].children = kept;  // the satellites' phases hang from their merging pieces
+    // The satellites' phases hang from their merging pieces.
+    out[p].first = out[p].last = -1;
+    out[p].count = 0;
+    for (int32_t k : kept) append_child(out, p, k);
   }
   // Cut each host node at its merging times.
   for (int32_t d = 0; d < n; ++d) {
@@ -652,36 +679,48 @@ void add_satellites(const TreeIn& in, const std::vector<double>& spin, const Cos
     if (ev.empty()) continue;
     std::stable_sort(ev.begin(), ev.end(), [](const Event& a, const Event& b) { return a.tm < b.tm; });
     const int32_t par = out[d].parent;
+    const int32_t dNext = out[d].next;  // d's place among its parent's progenitors
     int32_t prev = d;
     size_t j = 0;
     // Mergers at the node's own time join its progenitors directly.
     while (j < ev.size() && !(ev[j].tm > t[d])) {
       out[ev[j].sat].parent = d;
-      out[d].children.push_back(ev[j].sat);
+      append_child(out, d, ev[j].sat);
       ++j;
     }
+    if (j == ev.size()) continue;
     while (j < ev.size()) {
       const double tm = ev[j].tm;
       const int32_t J = (int32_t)out.size();
-      out.push_back(SatNode{massAt(d, tm), tm, spin[d], -1, -1, {prev}});
+      out.push_back(sat_node(massAt(d, tm), tm, spin[d], -1, -1));
+      append_child(out, J, prev);
       out[prev].parent = J;
       for (; j < ev.size() && ev[j].tm == tm; ++j) {
         out[ev[j].sat].parent = J;
-        out[J].children.push_back(ev[j].sat);
+        append_child(out, J, ev[j].sat);
       }
       prev = J;
     }
     // The last piece takes the node's place among its parent's progenitors.
     out[prev].parent = par;
-    if (par >= 0)
-      for (int32_t& ch : out[par].children)
-        if (ch == d) ch = prev;
+    if (par >= 0) {
+      out[prev].next = dNext;
+      if (out[par].first == d) {
+        out[par].first = prev;
+      } else {
+        int32_t q = out[par].first;
+        while (out[q].next != d) q = out[q].next;
+        out[q].next = prev;
+      }
+      if (out[par].last == d) out[par].last = prev;
+    }
   }
   // Satellites that outlive the tree: a root of their own at its final time.
   for (int32_t S : unmerged) {
     if (!(tEnd > out[S].time)) continue;  // fell in at the final time: S is the root
     const int32_t E = (int32_t)out.size();
-    out.push_back(SatNode{out[S].mass, tEnd, out[S].spin, -1, -1, {S}});
+    out.push_back(sat_node(out[S].mass, tEnd, out[S].spin, -1, -1));
+    append_child(out, E, S);
     out[S].parent = E;
   }
 }
@@ -696,7 +735,7 @@ std::vector<int32_t> layout(const std::vector<SatNode>& nodes) {
   for (int32_t i = 0; i < (int32_t)nodes.size(); ++i)
     if (nodes[i].parent < 0) order.push_back(i);
   for (size_t q = 0; q < order.size(); ++q)
-    for (int32_t ch : nodes[order[q]].children) order.push_back(ch);
+    for (int32_t ch = nodes[(size_t)order[q]].first; ch >= 0; ch = nodes[(size_t)ch].next) order.push_back(ch);
   return order;
 }
 
@@ -831,8 +870,8 @@ int build_forest(gal_ctx* ctx, const gal_params* p, const gal_pch_params* pch, c
         const size_t g = off + j;
         f->tree[g] = (int32_t)t;
         f->parent[g] = nd.parent < 0 ? -1 : (int32_t)(off + at[(size_t)nd.parent]);
-        f->childCount[g] = (int32_t)nd.children.size();
-        f->childFirst[g] = nd.children.empty() ? 0 : (int32_t)(off + at[(size_t)nd.children[0]]);
+        f->childCount[g] = nd.count;
+        f->childFirst[g] = nd.count == 0 ? 0 : (int32_t)(off + at[(size_t)nd.first]);
         f->time[g] = nd.time;
         f->mass[g] = nd.mass;
         f->spin[g] = nd.spin;
