@@ -24,7 +24,7 @@ NO_CONTRACT = {"forest.cu"}
 # Device code whose FP64 arithmetic follows the oracle's operation by operation: no FMA contraction.
 NO_FMAD = {"trees_gpu.cu"}
 # Sources whose host code uses OpenMP.
-OPENMP = {"trees.cpp", "trees_gpu.cu"}
+OPENMP = {"trees.cpp", "trees_gpu.cu", "forest.cu"}
 
 
 def nvcc():

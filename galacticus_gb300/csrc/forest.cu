@@ -23,6 +23,7 @@
 #include <new>
 #include <vector>
 #include <algorithm>
+#include <memory>
 
 #include "../../include/galnode_forest.h"
 #include "context.h"
@@ -46,9 +47,13 @@ struct HostCosmology {
   // (mergerTreeEvolveTimestepSimple, timesteps/simple.F90:124-161), H the
   // expansion rate of cosmologyFunctionsMatterLambda in 1/Gyr.
   double step_limit(double t, double relative, double absolute) const {
+    return relative > 0.0 ? step_limit_z(redshift(t), relative, absolute) : absolute;
+  }
+  // The same at a time whose redshift z is known.
+  double step_limit_z(double z, double relative, double absolute) const {
     if (!(relative > 0.0)) return absolute;
     const double hubbleGyr = h0 / (kMpc / 1.0e3 / kGyr);
-    const double zp = 1.0 + redshift(t);
+    const double zp = 1.0 + z;
     const double rate = hubbleGyr * std::sqrt(om * zp * zp * zp + ol);
     return std::min(relative / rate, absolute);
   }
@@ -64,12 +69,22 @@ struct HostCosmology {
 };
 
 template <class T>
-cudaError_t upload(T** dst, const std::vector<T>& src) {
+cudaError_t upload(T** dst, const T* src, size_t n) {
   *dst = nullptr;
-  if (src.empty()) return cudaSuccess;
-  cudaError_t e = cudaMalloc((void**)dst, src.size() * sizeof(T));
-  if (e == cudaSuccess) e = cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = cudaMalloc((void**)dst, n * sizeof(T));
+  if (e == cudaSuccess) e = cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
   return e;
+}
+template <class T>
+cudaError_t upload(T** dst, const std::vector<T>& src) {
+  return upload(dst, src.data(), src.size());
+}
+// A host array left uninitialised: the segment tables are written once, in
+// parallel, so the first touch of their pages is spread over the threads.
+template <class T>
+std::unique_ptr<T[]> scratch(size_t n) {
+  return std::unique_ptr<T[]>(new (std::nothrow) T[n > 0 ? n : 1]);
 }
 
 }  // namespace
@@ -202,17 +217,30 @@ int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const 
     return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: bad arguments%s");
   for (int32_t k = 1; k < nOut; ++k)
     if (!(tOut[k] > tOut[k - 1])) return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: output times must increase%s");
-  // Topology checks: parents in range and later, progenitors contiguous.
-  for (int64_t i = 0; i < n; ++i) {
+  // Topology checks (parents in range and later, progenitors contiguous,
+  // satellite hosts at the infall time), parallel over nodes; the first
+  // failing node is reported.
+  auto node_error = [&](int64_t i) -> int {
     const int32_t p = parent[i];
     if (p >= n || p < -1 || (p >= 0 && !(time[p] > time[i])) || childCount[i] < 0 ||
         (childCount[i] > 0 && (childFirst[i] < 0 || (int64_t)childFirst[i] + childCount[i] > n)))
-      return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: inconsistent forest topology%s");
+      return 1;
     for (int32_t c = 0; c < childCount[i]; ++c)
-      if (parent[childFirst[i] + c] != (int32_t)i)
-        return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: progenitors must be contiguous%s");
-    if (satHost && (satHost[i] < -1 || satHost[i] >= n || (satHost[i] >= 0 && time[satHost[i]] != time[i])))
-      return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: a satellite's host must be a node of its infall time%s");
+      if (parent[childFirst[i] + c] != (int32_t)i) return 2;
+    if (p >= 0 && !(childFirst[p] <= i && i < (int64_t)childFirst[p] + childCount[p])) return 2;
+    if (satHost && (satHost[i] < -1 || satHost[i] >= n || (satHost[i] >= 0 && time[satHost[i]] != time[i]))) return 3;
+    return 0;
+  };
+  int64_t firstBad = n;
+#pragma omp parallel for schedule(static) reduction(min : firstBad)
+  for (int64_t i = 0; i < n; ++i)
+    if (node_error(i) && i < firstBad) firstBad = i;
+  if (firstBad < n) {
+    const int code = node_error(firstBad);
+    return fail(ctx, GAL_ERR_ARGUMENT,
+                code == 1   ? "gal_gpu_forest_create: inconsistent forest topology%s"
+                : code == 2 ? "gal_gpu_forest_create: progenitors must be contiguous%s"
+                            : "gal_gpu_forest_create: a satellite's host must be a node of its infall time%s");
   }
   // The mass each node gains at its own time from the satellites that fall
   // into it (their halos join its halo there).
@@ -223,15 +251,75 @@ int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const 
   auto isSatellite = [&](int64_t i) { return satHost && satHost[i] >= 0; };
   const gal_params& p = ctx->params;
   const HostCosmology cos{p.omega_matter, p.omega_dark_energy, p.hubble_constant};
-  std::vector<int32_t> leaves, pending0(n), segFirst(n), segCount(n), snapInitial(n, -1), segSnap;
-  std::vector<double> segParam[GAL_NP], segT0, segT1;
   gal_forest_dev* f = new (std::nothrow) gal_forest_dev();
   if (!f) return fail(ctx, GAL_ERR_ARGUMENT, "out of host memory%s");
   f->n = n;
-  int32_t slot = 0;
+  // A node's evolve calls: from its time to its parent's, each ending at the
+  // first of the next output time, the parent's time and the timestep
+  // limit; seg(a, b, k, z) for each, k the output it ends at or -1, z the
+  // redshift at a when the timestep limit needed it (else NaN).
+  auto segments = [&](int64_t i, auto&& seg) {
+    const int32_t par = parent[i];
+    const double t0 = time[i], t1 = par >= 0 ? time[par] : time[i];
+    double a = t0;
+    int32_t k = (int32_t)(std::upper_bound(tOut, tOut + nOut, t0) - tOut);  // first output after t0
+    const bool relative = p.timestep_relative > 0.0;
+    while (a < t1) {
+      const double z = relative ? cos.redshift(a) : NAN;
+      const double limit = a + cos.step_limit_z(z, p.timestep_relative, p.timestep_absolute);
+      const bool atOutput = k < nOut && tOut[k] < t1 && !(limit < tOut[k]);
+      const double b = atOutput ? tOut[k] : std::min(limit, t1);
+      seg(a, b, atOutput ? k : -1, z);
+      if (atOutput) ++k;
+      a = b;
+    }
+  };
+  // The output at the node's own time, if any (a non-root only if it has an
+  // interval to evolve).
+  auto initial_output = [&](int64_t i) -> int32_t {
+    const int32_t par = parent[i];
+    const double t0 = time[i];
+    if (!(par < 0 || t0 < time[par])) return -1;
+    const double* it = std::lower_bound(tOut, tOut + nOut, t0);
+    return it != tOut + nOut && *it == t0 ? (int32_t)(it - tOut) : -1;
+  };
+  // Pass 1, parallel: evolve calls and snapshot slots per node; then their
+  // offsets in node order.
+  std::vector<int64_t> segBase((size_t)n + 1, 0), snapBase((size_t)n + 1, 0);
+#pragma omp parallel for schedule(dynamic, 4096)
   for (int64_t i = 0; i < n; ++i) {
-    pending0[i] = childCount[i];
-    if (childCount[i] == 0) leaves.push_back((int32_t)i);
+    int64_t ns = 0, nsnap = initial_output(i) >= 0 ? 1 : 0;
+    segments(i, [&](double, double, int32_t k, double) {
+      ++ns;
+      if (k >= 0) ++nsnap;
+    });
+    segBase[(size_t)i + 1] = ns;
+    snapBase[(size_t)i + 1] = nsnap;
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    segBase[(size_t)i + 1] += segBase[(size_t)i];
+    snapBase[(size_t)i + 1] += snapBase[(size_t)i];
+  }
+  const int64_t nSeg = segBase[(size_t)n], nSnap = snapBase[(size_t)n];
+  if (nSeg > (int64_t)INT32_MAX || nSnap > (int64_t)INT32_MAX) {
+    delete f;
+    return fail(ctx, GAL_ERR_TOO_LARGE, "gal_gpu_forest_create: more than 2^31 evolve calls or snapshots%s");
+  }
+  std::vector<int32_t> leaves, pending0((size_t)n), segFirst((size_t)n), segCount((size_t)n), snapInitial((size_t)n);
+  std::unique_ptr<int32_t[]> segSnap = scratch<int32_t>((size_t)nSeg);
+  std::unique_ptr<double[]> segParamFlat = scratch<double>((size_t)GAL_NP * nSeg), segT0 = scratch<double>((size_t)nSeg),
+                            segT1 = scratch<double>((size_t)nSeg);
+  if (!segSnap || !segParamFlat || !segT0 || !segT1) {
+    delete f;
+    return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: out of host memory%s");
+  }
+  f->snapNode.resize((size_t)nSnap);
+  f->snapOutput.resize((size_t)nSnap);
+  // Pass 2, parallel: each node's calls at its offsets (the same numbering as
+  // one pass in node order).
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (int64_t i = 0; i < n; ++i) {
+    pending0[(size_t)i] = childCount[i];
     const int32_t par = parent[i];
     const double t0 = time[i], t1 = par >= 0 ? time[par] : time[i];
     const bool primary = par >= 0 && childFirst[par] == (int32_t)i;
@@ -248,81 +336,91 @@ int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const 
     }
     // A satellite's virial scales are those of its infall time.
     const double zFrozen = isSatellite(i) ? cos.redshift(t0) : 0.0;
-    // Snapshot slots: outputs at the node's own time, then inside its interval.
-    for (int32_t k = 0; k < nOut; ++k)
-      if (tOut[k] == t0 && (par < 0 || t0 < t1)) {
-        snapInitial[i] = slot++;
-        f->snapNode.push_back((int32_t)i);
-        f->snapOutput.push_back(k);
-      }
-    segFirst[i] = (int32_t)segT0.size();
-    double a = t0;
-    int32_t k = 0;
-    while (k < nOut && !(tOut[k] > t0)) ++k;
-    while (a < t1) {
-      // The call ends at the first of: the next output time, the parent's
-      // time and the timestep limit.
-      const double limit = a + cos.step_limit(a, p.timestep_relative, p.timestep_absolute);
-      const bool atOutput = k < nOut && tOut[k] < t1 && !(limit < tOut[k]);
-      const double b = atOutput ? tOut[k] : std::min(limit, t1);
+    int64_t slot = snapBase[(size_t)i];
+    const int32_t k0 = initial_output(i);
+    snapInitial[(size_t)i] = -1;
+    if (k0 >= 0) {
+      snapInitial[(size_t)i] = (int32_t)slot;
+      f->snapNode[(size_t)slot] = (int32_t)i;
+      f->snapOutput[(size_t)slot] = k0;
+      ++slot;
+    }
+    int64_t sg = segBase[(size_t)i];
+    segFirst[(size_t)i] = (int32_t)sg;
+    segCount[(size_t)i] = (int32_t)(segBase[(size_t)i + 1] - sg);
+    segments(i, [&](double a, double b, int32_t k, double z) {
       const double M = mass[i] + (massEnd - mass[i]) * (a - t0) / (t1 - t0);
       double r, v;
-      cos.virial(M, isSatellite(i) ? zFrozen : cos.redshift(a), r, v);
-      segParam[GAL_P_MASS].push_back(M);
-      segParam[GAL_P_MASS_RATE].push_back(accretion);
-      segParam[GAL_P_RADIUS_VIRIAL].push_back(r);
-      segParam[GAL_P_VELOCITY_VIRIAL].push_back(v);
-      segParam[GAL_P_SPIN].push_back(spin[i]);
-      segT0.push_back(a);
-      segT1.push_back(b);
-      if (atOutput) {
-        segSnap.push_back(slot++);
-        f->snapNode.push_back((int32_t)i);
-        f->snapOutput.push_back(k);
-        ++k;
+      cos.virial(M, isSatellite(i) ? zFrozen : (z == z ? z : cos.redshift(a)), r, v);
+      segParamFlat[(size_t)GAL_P_MASS * nSeg + sg] = M;
+      segParamFlat[(size_t)GAL_P_MASS_RATE * nSeg + sg] = accretion;
+      segParamFlat[(size_t)GAL_P_RADIUS_VIRIAL * nSeg + sg] = r;
+      segParamFlat[(size_t)GAL_P_VELOCITY_VIRIAL * nSeg + sg] = v;
+      segParamFlat[(size_t)GAL_P_SPIN * nSeg + sg] = spin[i];
+      segT0[(size_t)sg] = a;
+      segT1[(size_t)sg] = b;
+      if (k >= 0) {
+        segSnap[(size_t)sg] = (int32_t)slot;
+        f->snapNode[(size_t)slot] = (int32_t)i;
+        f->snapOutput[(size_t)slot] = k;
+        ++slot;
       } else {
-        segSnap.push_back(-1);
+        segSnap[(size_t)sg] = -1;
       }
-      a = b;
-    }
-    segCount[i] = (int32_t)segT0.size() - segFirst[i];
+      ++sg;
+    });
   }
+  for (int64_t i = 0; i < n; ++i)
+    if (childCount[i] == 0) leaves.push_back((int32_t)i);
   // Longest chains first: a leaf's chain to its root is the sequence of
   // nodes that can only run one after another, so leaves are queued by the
   // number of their ancestors, largest first (ties in index order).  The
   // deep branches of the largest trees then start at once instead of
-  // setting the end of the evolution.
+  // setting the end of the evolution.  Depths by a walk down from each
+  // root, the order by a stable counting sort.
   {
-    std::vector<int64_t> byTime((size_t)n);
-    for (int64_t i = 0; i < n; ++i) byTime[(size_t)i] = i;
-    std::stable_sort(byTime.begin(), byTime.end(), [&](int64_t a, int64_t b) { return time[a] > time[b]; });
-    std::vector<int32_t> depth((size_t)n, 0);
-    for (int64_t i : byTime) depth[(size_t)i] = parent[i] < 0 ? 0 : depth[(size_t)parent[i]] + 1;
-    std::stable_sort(leaves.begin(), leaves.end(), [&](int32_t a, int32_t b) { return depth[(size_t)a] > depth[(size_t)b]; });
+    std::vector<int32_t> depth((size_t)n, 0), roots;
+    for (int64_t i = 0; i < n; ++i)
+      if (parent[i] < 0) roots.push_back((int32_t)i);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t r = 0; r < (int64_t)roots.size(); ++r) {
+      std::vector<int32_t> stack{roots[(size_t)r]};
+      while (!stack.empty()) {
+        const int32_t i = stack.back();
+        stack.pop_back();
+        for (int32_t c = 0; c < childCount[i]; ++c) {
+          depth[(size_t)(childFirst[i] + c)] = depth[(size_t)i] + 1;
+          stack.push_back(childFirst[i] + c);
+        }
+      }
+    }
+    int32_t maxDepth = 0;
+    for (int32_t l : leaves) maxDepth = std::max(maxDepth, depth[(size_t)l]);
+    std::vector<int64_t> at((size_t)maxDepth + 2, 0);
+    for (int32_t l : leaves) ++at[(size_t)(maxDepth - depth[(size_t)l]) + 1];
+    for (size_t d = 1; d < at.size(); ++d) at[d] += at[d - 1];
+    std::vector<int32_t> sorted(leaves.size());
+    for (int32_t l : leaves) sorted[(size_t)at[(size_t)(maxDepth - depth[(size_t)l])]++] = l;
+    leaves.swap(sorted);
   }
   f->nLeaves = (int64_t)leaves.size();
-  f->nSeg = (int64_t)segT0.size();
-  f->nSnap = slot;
-  std::vector<double> segParamFlat((size_t)GAL_NP * f->nSeg);
-  for (int v = 0; v < GAL_NP; ++v) std::copy(segParam[v].begin(), segParam[v].end(), segParamFlat.begin() + v * f->nSeg);
-  std::vector<double> st0((size_t)GAL_NY * n);
-  std::memcpy(st0.data(), state0, st0.size() * sizeof(double));
+  f->nSeg = nSeg;
+  f->nSnap = nSnap;
   cudaError_t e = cudaSetDevice(ctx->device);
-  std::vector<int32_t> par(parent, parent + n), cf(childFirst, childFirst + n), cc(childCount, childCount + n);
   if (e == cudaSuccess) e = upload(&f->dLeaves, leaves);
-  if (e == cudaSuccess) e = upload(&f->dParent, par);
-  if (e == cudaSuccess) e = upload(&f->dChildFirst, cf);
-  if (e == cudaSuccess) e = upload(&f->dChildCount, cc);
+  if (e == cudaSuccess) e = upload(&f->dParent, parent, (size_t)n);
+  if (e == cudaSuccess) e = upload(&f->dChildFirst, childFirst, (size_t)n);
+  if (e == cudaSuccess) e = upload(&f->dChildCount, childCount, (size_t)n);
   if (e == cudaSuccess) e = upload(&f->dPending0, pending0);
   if (e == cudaSuccess) e = upload(&f->dPending, pending0);
   if (e == cudaSuccess) e = upload(&f->dSegFirst, segFirst);
   if (e == cudaSuccess) e = upload(&f->dSegCount, segCount);
   if (e == cudaSuccess) e = upload(&f->dSnapInitial, snapInitial);
-  if (e == cudaSuccess) e = upload(&f->dSegSnap, segSnap);
-  if (e == cudaSuccess) e = upload(&f->dSegParam, segParamFlat);
-  if (e == cudaSuccess) e = upload(&f->dSegT0, segT0);
-  if (e == cudaSuccess) e = upload(&f->dSegT1, segT1);
-  if (e == cudaSuccess) e = upload(&f->dState0, st0);
+  if (e == cudaSuccess) e = upload(&f->dSegSnap, segSnap.get(), (size_t)nSeg);
+  if (e == cudaSuccess) e = upload(&f->dSegParam, segParamFlat.get(), (size_t)GAL_NP * nSeg);
+  if (e == cudaSuccess) e = upload(&f->dSegT0, segT0.get(), (size_t)nSeg);
+  if (e == cudaSuccess) e = upload(&f->dSegT1, segT1.get(), (size_t)nSeg);
+  if (e == cudaSuccess) e = upload(&f->dState0, state0, (size_t)GAL_NY * n);
   if (e == cudaSuccess) e = cudaMalloc(&f->dState, (size_t)GAL_NY * n * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&f->dStepOut, (size_t)n * sizeof(double));
   if (e == cudaSuccess && f->nSnap > 0) e = cudaMalloc(&f->dSnap, (size_t)GAL_NY * f->nSnap * sizeof(double));
