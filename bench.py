@@ -453,7 +453,9 @@ def scale_record(args, params, table, net, gate):
         if name == "surrogate" and gate is not None:
             net.build_error_map(table, tolerance=gate)
             net.install(ev)
+        tc = time.perf_counter()
         fe = forest.ForestEvolver(ev, f, state0, times)
+        create_s = time.perf_counter() - tc
         out["snapshots"] = fe.snapshot_count()
         fe.evolve()
         s0 = surrogate.stats(ev) if name == "surrogate" and gate is not None else (0, 0)
@@ -462,7 +464,8 @@ def scale_record(args, params, table, net, gate):
         dt = time.perf_counter() - tb
         state, status, counters = fe.results(snapshots=False)[:3]
         entry = {"value": float(counters[0].sum()) / dt, "s_per_evolution": dt, "accepted_steps": int(counters[0].sum()),
-                 "rhs_evaluations": int(counters[2].sum()), "failed_nodes": int((status != 0).sum())}
+                 "rhs_evaluations": int(counters[2].sum()), "failed_nodes": int((status != 0).sum()),
+                 "create_s": create_s}
         if name == "surrogate":
             s1 = surrogate.stats(ev) if gate is not None else (0, 0)
             served = s1[0] - s0[0]
