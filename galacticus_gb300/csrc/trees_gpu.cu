@@ -35,6 +35,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <utility>
 #include <vector>
@@ -376,9 +377,15 @@ int grow_forest_gpu(gal_ctx* ctx, const BranchTables& tab, const double* rootMas
   double guess = 0.0;
   for (int64_t t = 0; t < n; ++t) guess += 4.0 + 2.0 * std::pow(rootMass[t] / tab.mRes, 0.85);
   int64_t cap = (int64_t)std::min(std::max(guess, 1.0e6), (double)INT32_MAX);
+  // GALNODE_BRANCH_CAPACITY sets the first capacity instead (at least the
+  // roots): tests use it to run the overflow-and-repeat path.
+  if (const char* env = std::getenv("GALNODE_BRANCH_CAPACITY")) {
+    const long long c = std::atoll(env);
+    if (c > 0) cap = std::min<int64_t>(std::max<int64_t>(c, n), INT32_MAX);
+  }
   cudaStream_t s = ctx->stream;
   std::vector<unsigned long long> counters(kCounters);
-  for (int attempt = 0; attempt < 8; ++attempt) {
+  for (int attempt = 0; attempt < 16; ++attempt) {
     Buffers nb;
     DevNodes dn{nullptr, nullptr, nullptr, nullptr, nullptr, cap};
     int32_t *fa = nullptr, *fb = nullptr;

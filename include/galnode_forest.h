@@ -111,8 +111,11 @@ int gal_forest_build(const gal_params* p, const gal_pch_params* pch, const gal_f
  * same seed.  Spins and
  * satellite orbits are drawn on the host as by gal_forest_build.  The
  * Cole2000 builder's per-tree build (merger_trees/construct/builder/
- * Cole2000/_class.F90:360-913), for a whole forest at once.  Errors are
- * recorded in ctx. */
+ * Cole2000/_class.F90:360-913), for a whole forest at once.  The node
+ * arrays on the GPU are sized from the roots' masses and grown (the growth
+ * repeated) when a forest outgrows them; the environment variable
+ * GALNODE_BRANCH_CAPACITY sets their first size instead (for tests of that
+ * path).  Errors are recorded in ctx. */
 int gal_gpu_forest_build(gal_ctx* ctx, const gal_params* p, const gal_pch_params* pch, const gal_forest_spec* spec,
                          gal_forest** out);
 /* The inputs of the GPU branching for a forest spec (for tests of it

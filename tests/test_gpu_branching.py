@@ -103,3 +103,12 @@ def test_gpu_built_forest_with_satellites_evolves(params, evolver, table, oracle
     param[_abi.P_MASS] = f.mass
     within = np.all(np.abs(state - ref) <= compare.parity_bound(ref, ref, param, params), axis=0)
     assert within.mean() > 0.995, within.mean()
+
+
+def test_gpu_branching_grows_its_node_arrays(built, params, evolver, monkeypatch):
+    """A first capacity far below the forest's size: the growth overflows,
+    repeats with larger arrays and ends with the same forest."""
+    monkeypatch.setenv("GALNODE_BRANCH_CAPACITY", str(built.n // 6))
+    again = forest.build(params, n_trees=1024, gpu=evolver, **SPEC)
+    for name in ("parent", "child_first", "child_count", "mass", "time", "spin"):
+        np.testing.assert_array_equal(getattr(again, name), getattr(built, name))
