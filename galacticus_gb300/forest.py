@@ -178,13 +178,14 @@ def pch_params():
 
 
 def _spec(n_trees, seed, root_mass_min, root_mass_max, root_mass_slope, redshift_max, mass_resolution, satellites,
-          satellite_timescale_multiplier):
-    return ForestSpec(n_trees, seed, root_mass_min, root_mass_max, root_mass_slope, 0.0, redshift_max, mass_resolution,
-                      satellites, 0, satellite_timescale_multiplier)
+          satellite_timescale_multiplier, root_redshift=0.0):
+    return ForestSpec(n_trees, seed, root_mass_min, root_mass_max, root_mass_slope, root_redshift, redshift_max,
+                      mass_resolution, satellites, 0, satellite_timescale_multiplier)
 
 
 def build(params, n_trees, seed=3, root_mass_min=1e10, root_mass_max=1e14, root_mass_slope=-0.9, redshift_max=8.0,
-          mass_resolution=1e8, pch=None, satellites=SATELLITES_NONE, satellite_timescale_multiplier=0.75, gpu=None):
+          mass_resolution=1e8, pch=None, satellites=SATELLITES_NONE, satellite_timescale_multiplier=0.75, gpu=None,
+          root_redshift=0.0):
     """Build a forest on the host (OpenMP over trees), or with its branches
     grown on the GPU of ``gpu`` (an evolver; gal_gpu_forest_build: the same
     builder with keyed per-branch streams, so other trees for the same
@@ -193,7 +194,7 @@ def build(params, n_trees, seed=3, root_mass_min=1e10, root_mass_max=1e14, root_
     the reference's quickTest, 0.75)."""
     lib = _declare(_abi.load_library())
     spec = _spec(n_trees, seed, root_mass_min, root_mass_max, root_mass_slope, redshift_max, mass_resolution,
-                 satellites, satellite_timescale_multiplier)
+                 satellites, satellite_timescale_multiplier, root_redshift)
     pch = pch or pch_params()
     handle = ctypes.c_void_p()
     if gpu is None:
@@ -221,12 +222,13 @@ def build(params, n_trees, seed=3, root_mass_min=1e10, root_mass_max=1e14, root_
 
 
 def branch_tables(params, seed=3, root_mass_min=1e10, root_mass_max=1e14, redshift_max=8.0, mass_resolution=1e8,
-                  pch=None):
+                  pch=None, root_redshift=0.0):
     """The GPU branching's inputs for a forest (gal_pch_branch_tables): a
     dict with ``sizes``, ``meta`` and the tables ``ln_sigma``, ``rate``,
     ``accretion``, ``ln_q``, ``cdf``."""
     lib = _declare(_abi.load_library())
-    spec = _spec(1, seed, root_mass_min, root_mass_max, -0.9, redshift_max, mass_resolution, SATELLITES_NONE, 0.75)
+    spec = _spec(1, seed, root_mass_min, root_mass_max, -0.9, redshift_max, mass_resolution, SATELLITES_NONE, 0.75,
+                 root_redshift)
     pch = pch or pch_params()
     sizes, meta = np.zeros(2, np.int32), np.zeros(10)
     args = (ctypes.byref(params), ctypes.byref(pch), ctypes.byref(spec))

@@ -112,3 +112,26 @@ def test_gpu_branching_grows_its_node_arrays(built, params, evolver, monkeypatch
     again = forest.build(params, n_trees=1024, gpu=evolver, **SPEC)
     for name in ("parent", "child_first", "child_count", "mass", "time", "spin"):
         np.testing.assert_array_equal(getattr(again, name), getattr(built, name))
+
+
+@pytest.mark.parametrize("case", [
+    dict(pch=dict(g0=1.0, gamma1=0.0, gamma2=0.0), spec=dict(mass_resolution=1e9)),           # plain EPS rates
+    dict(pch=dict(accuracy_first=0.05, accuracy_second=0.05), spec=dict(redshift_max=12.0)),  # finer steps
+    dict(pch=dict(gamma2=-0.1), spec=dict(root_redshift=1.0, root_mass_max=1e12)),             # roots at z = 1
+])
+def test_gpu_branching_matches_the_oracle_for_other_parameters(case, params, evolver, oracle_mod):
+    pch = forest.pch_params()
+    for k, v in case["pch"].items():
+        setattr(pch, k, v)
+    spec = dict(seed=9, root_mass_min=1e11, root_mass_max=1e13, mass_resolution=1e8, redshift_max=8.0)
+    spec.update(case["spec"])
+    root_redshift = spec.pop("root_redshift", 0.0)
+    f = forest.build(params, n_trees=128, gpu=evolver, pch=pch, root_redshift=root_redshift, **spec)
+    starts, ends = _tree_slices(f)
+    tables = forest.branch_tables(params, pch=pch, root_redshift=root_redshift, **spec)
+    mass, w, parent, child_first, child_count, tree_first = oracle_mod.grow_trees(tables, spec["seed"], f.mass[starts])
+    assert f.n == len(mass) and np.array_equal(starts, tree_first)
+    local = np.repeat(starts, ends - starts)
+    np.testing.assert_array_equal(np.where(f.parent >= 0, f.parent - local, -1), parent)
+    np.testing.assert_array_equal(f.child_count, child_count)
+    np.testing.assert_array_equal(f.mass, mass)
