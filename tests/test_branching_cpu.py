@@ -120,3 +120,14 @@ def test_walk_math_accuracy(oracle_mod):
     err = np.abs(lx.astype(np.float64) - np.log(x))
     assert np.all(err <= 2.5e-7 + 6.5e-8 * np.abs(np.log(x))), err.max()
     assert np.max(np.abs(ey / np.exp(y.astype(np.float64)) - 1.0)) < 2.5e-7
+
+
+def test_build_stats(params):
+    """Where a host build's time went: every phase timed, none of them the
+    GPU's, and the phases within the total."""
+    f = forest.build(params, n_trees=64, seed=5, root_mass_min=1e10, root_mass_max=1e12,
+                     satellites=forest.SATELLITES_JIANG2008)
+    s = f.build_stats
+    assert s["gpu_growth_s"] == 0.0 and s["download_renumber_s"] == 0.0 and s["generations"] == 0
+    assert s["tables_s"] > 0.0 and s["per_tree_s"] > 0.0 and s["assembly_s"] > 0.0
+    assert s["tables_s"] + s["per_tree_s"] + s["assembly_s"] <= s["total_s"] * (1 + 1e-9)
