@@ -24,6 +24,7 @@
 #include <vector>
 #include <algorithm>
 #include <memory>
+#include <type_traits>
 
 #include "../../include/galnode_forest.h"
 #include "context.h"
@@ -38,33 +39,29 @@ constexpr double kG = 6.673e-11 * 1.98892e30 / 1.0e6 / kMpc;  // km^2 s^-2 Mpc /
 
 struct HostCosmology {
   double om, ol, h0;
-  double redshift(double t) const {
+  __host__ __device__ double redshift(double t) const {
     const double hubbleGyr = h0 / (kMpc / 1.0e3 / kGyr);
-    const double x = std::sinh(1.5 * hubbleGyr * std::sqrt(ol) * t);
-    return 1.0 / std::pow(x / std::sqrt(ol / om), 2.0 / 3.0) - 1.0;
+    const double x = sinh(1.5 * hubbleGyr * sqrt(ol) * t);
+    return 1.0 / pow(x / sqrt(ol / om), 2.0 / 3.0) - 1.0;
   }
-  // The longest evolve call from time t: min(relative / H(t), absolute)
-  // (mergerTreeEvolveTimestepSimple, timesteps/simple.F90:124-161), H the
-  // expansion rate of cosmologyFunctionsMatterLambda in 1/Gyr.
-  double step_limit(double t, double relative, double absolute) const {
-    return relative > 0.0 ? step_limit_z(redshift(t), relative, absolute) : absolute;
-  }
-  // The same at a time whose redshift z is known.
-  double step_limit_z(double z, double relative, double absolute) const {
+  // The longest evolve call from a time at redshift z: min(relative / H,
+  // absolute) (mergerTreeEvolveTimestepSimple, timesteps/simple.F90:124-161),
+  // H the expansion rate of cosmologyFunctionsMatterLambda in 1/Gyr.
+  __host__ __device__ double step_limit_z(double z, double relative, double absolute) const {
     if (!(relative > 0.0)) return absolute;
     const double hubbleGyr = h0 / (kMpc / 1.0e3 / kGyr);
     const double zp = 1.0 + z;
-    const double rate = hubbleGyr * std::sqrt(om * zp * zp * zp + ol);
-    return std::min(relative / rate, absolute);
+    const double rate = hubbleGyr * sqrt(om * zp * zp * zp + ol);
+    return fmin(relative / rate, absolute);
   }
-  void virial(double M, double z, double& r, double& v) const {
+  __host__ __device__ void virial(double M, double z, double& r, double& v) const {
     const double zp = (1.0 + z) * (1.0 + z) * (1.0 + z);
     const double omz = om * zp / (om * zp + ol);
     const double x = omz - 1.0;
     const double contrast = (18.0 * M_PI * M_PI + 82.0 * x - 39.0 * x * x) / (x + 1.0);
     const double rhoMean = om * 3.0 * h0 * h0 / (8.0 * M_PI * kG) * zp;
-    r = std::cbrt(3.0 * M / (4.0 * M_PI * contrast * rhoMean));
-    v = std::sqrt(kG * M / r);
+    r = cbrt(3.0 * M / (4.0 * M_PI * contrast * rhoMean));
+    v = sqrt(kG * M / r);
   }
 };
 
@@ -80,11 +77,214 @@ template <class T>
 cudaError_t upload(T** dst, const std::vector<T>& src) {
   return upload(dst, src.data(), src.size());
 }
-// A host array left uninitialised: the segment tables are written once, in
-// parallel, so the first touch of their pages is spread over the threads.
-template <class T>
-std::unique_ptr<T[]> scratch(size_t n) {
-  return std::unique_ptr<T[]>(new (std::nothrow) T[n > 0 ? n : 1]);
+
+// ---------------------------------------------------------------- segment table on the GPU
+//
+// The segment table (one row per evolve call) built on the device, one
+// thread per node: a first kernel counts each node's evolve calls and
+// snapshots, a scan turns the counts into offsets, and a second kernel
+// writes each node's rows at its offsets.  The rules are those of the tree
+// evolver (merger_trees/evolver/standard.F90:762-1035): a node evolves from
+// its time to its parent's in calls that end at the first of the next
+// output time, the parent's time and the mergerTreeEvolveTimestepSimple
+// limit (merger_trees/evolve/timesteps/simple.F90:124-161); each call's
+// halo mass follows the node's mass line and its virial scales are those of
+// its start (a satellite's, those of its infall).
+struct SegmentInputs {
+  HostCosmology cos;
+  double relative, absolute;
+  int64_t n;
+  int32_t nOut;
+  const double* tOut;
+  const double* time;
+  const double* mass;
+  const double* spin;
+  const double* massIn;
+  const int32_t* parent;
+  const int32_t* childFirst;
+  const int32_t* childCount;
+  const int32_t* satHost;  // may be null
+};
+
+// Calls per node are bounded (a node past the bound is flagged, not looped).
+constexpr int64_t kMaxCallsPerNode = 1 << 24;
+
+__device__ __forceinline__ int32_t first_output_after(const SegmentInputs& in, double t) {
+  int32_t lo = 0, hi = in.nOut;  // first k with tOut[k] > t
+  while (lo < hi) {
+    const int32_t mid = (lo + hi) >> 1;
+    if (in.tOut[mid] > t)
+      hi = mid;
+    else
+      lo = mid + 1;
+  }
+  return lo;
+}
+
+// The output at the node's own time, if any (a non-root only if it has an
+// interval to evolve).
+__device__ __forceinline__ int32_t initial_output_dev(const SegmentInputs& in, int64_t i) {
+  const int32_t par = in.parent[i];
+  const double t0 = in.time[i];
+  if (!(par < 0 || t0 < in.time[par])) return -1;
+  int32_t lo = 0, hi = in.nOut;  // first k with tOut[k] >= t0
+  while (lo < hi) {
+    const int32_t mid = (lo + hi) >> 1;
+    if (in.tOut[mid] >= t0)
+      hi = mid;
+    else
+      lo = mid + 1;
+  }
+  return lo < in.nOut && in.tOut[lo] == t0 ? lo : -1;
+}
+
+// seg(a, b, k, z) for each evolve call of node i (k the output it ends at
+// or -1, z the redshift at a or NaN); returns false past the bound.
+template <class F>
+__device__ __forceinline__ bool node_calls(const SegmentInputs& in, int64_t i, F&& seg) {
+  const int32_t par = in.parent[i];
+  const double t0 = in.time[i], t1 = par >= 0 ? in.time[par] : t0;
+  double a = t0;
+  int32_t k = first_output_after(in, t0);
+  const bool relative = in.relative > 0.0;
+  int64_t calls = 0;
+  while (a < t1) {
+    if (++calls > kMaxCallsPerNode) return false;
+    const double z = relative ? in.cos.redshift(a) : __longlong_as_double(0x7ff8000000000000ll);
+    const double limit = a + in.cos.step_limit_z(z, in.relative, in.absolute);
+    const bool atOutput = k < in.nOut && in.tOut[k] < t1 && !(limit < in.tOut[k]);
+    const double b = atOutput ? in.tOut[k] : fmin(limit, t1);
+    seg(a, b, atOutput ? k : -1, z);
+    if (atOutput) ++k;
+    a = b;
+  }
+  return true;
+}
+
+__global__ void count_calls_kernel(SegmentInputs in, int32_t* segCount, int32_t* snapCount, int* flag) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < in.n; i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t ns = 0, nsnap = initial_output_dev(in, i) >= 0 ? 1 : 0;
+    const bool ok = node_calls(in, i, [&](double, double, int32_t k, double) {
+      ++ns;
+      if (k >= 0) ++nsnap;
+    });
+    if (!ok || ns > INT32_MAX) {
+      atomicExch(flag, 1);
+      ns = nsnap = 0;
+    }
+    segCount[i] = (int32_t)ns;
+    snapCount[i] = (int32_t)nsnap;
+  }
+}
+
+// Exclusive scan of two count arrays, 1,024 entries per block; the block
+// totals are scanned on the host and added by add_offsets_kernel.
+__global__ void __launch_bounds__(1024) scan_blocks_kernel(const int32_t* a, const int32_t* b, int64_t n, int64_t* oa,
+                                                           int64_t* ob, int64_t* totals) {
+  __shared__ int64_t sa[1024], sb[1024];
+  const int64_t i = blockIdx.x * 1024ll + threadIdx.x;
+  const int64_t va = i < n ? a[i] : 0, vb = i < n ? b[i] : 0;
+  sa[threadIdx.x] = va;
+  sb[threadIdx.x] = vb;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const int64_t ta = threadIdx.x >= off ? sa[threadIdx.x - off] : 0;
+    const int64_t tb = threadIdx.x >= off ? sb[threadIdx.x - off] : 0;
+    __syncthreads();
+    sa[threadIdx.x] += ta;
+    sb[threadIdx.x] += tb;
+    __syncthreads();
+  }
+  if (i < n) {
+    oa[i] = sa[threadIdx.x] - va;
+    ob[i] = sb[threadIdx.x] - vb;
+  }
+  if (threadIdx.x == 1023) {
+    totals[2 * blockIdx.x] = sa[1023];
+    totals[2 * blockIdx.x + 1] = sb[1023];
+  }
+}
+
+__global__ void add_offsets_kernel(int64_t* oa, int64_t* ob, int64_t n, const int64_t* blockOffsets) {
+  const int64_t i = blockIdx.x * 1024ll + threadIdx.x;
+  if (i < n) {
+    oa[i] += blockOffsets[2 * blockIdx.x];
+    ob[i] += blockOffsets[2 * blockIdx.x + 1];
+  }
+}
+
+struct SegmentOutputs {
+  int64_t nSeg, nSnap;
+  const int64_t* segBase;
+  const int64_t* snapBase;
+  const int32_t* segCount;
+  int32_t* segFirst;
+  int32_t* snapInitial;
+  int32_t* snapNode;
+  int32_t* snapOutput;
+  double* segParam;  // [GAL_NP][nSeg]
+  double* segT0;
+  double* segT1;
+  int32_t* segSnap;
+};
+
+__global__ void fill_calls_kernel(SegmentInputs in, SegmentOutputs out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < in.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t par = in.parent[i];
+    const double t0 = in.time[i], t1 = par >= 0 ? in.time[par] : t0;
+    const bool satellite = in.satHost && in.satHost[i] >= 0;
+    // The primary progenitor grows by its parent's unresolved mass (the
+    // parent's mass beyond its progenitors' and the satellites falling in);
+    // other progenitors and satellites keep theirs and accrete nothing.
+    double massEnd = in.mass[i], accretion = 0.0;
+    if (par >= 0 && in.childFirst[par] == (int32_t)i && t1 > t0 && !satellite) {
+      double brought = in.massIn[par];
+      for (int32_t c = 0; c < in.childCount[par]; ++c) {
+        const int32_t s = in.childFirst[par] + c;
+        if (!(in.satHost && in.satHost[s] >= 0)) brought += in.mass[s];
+      }
+      accretion = fmax(in.mass[par] - brought, 0.0) / (t1 - t0);
+      massEnd = in.mass[i] + accretion * (t1 - t0);
+    }
+    // A satellite's virial scales are those of its infall time.
+    const double zFrozen = satellite ? in.cos.redshift(t0) : 0.0;
+    int64_t slot = out.snapBase[i];
+    const int64_t slotEnd = i + 1 < in.n ? out.snapBase[i + 1] : out.nSnap;
+    const int32_t k0 = initial_output_dev(in, i);
+    out.snapInitial[i] = -1;
+    if (k0 >= 0 && slot < slotEnd) {
+      out.snapInitial[i] = (int32_t)slot;
+      out.snapNode[slot] = (int32_t)i;
+      out.snapOutput[slot] = k0;
+      ++slot;
+    }
+    int64_t sg = out.segBase[i];
+    const int64_t sgEnd = sg + out.segCount[i];
+    out.segFirst[i] = (int32_t)sg;
+    const double m0 = in.mass[i], sp = in.spin[i];
+    node_calls(in, i, [&](double a, double b, int32_t k, double z) {
+      if (sg >= sgEnd) return;  // (the count pass made room for exactly these)
+      const double M = m0 + (massEnd - m0) * (a - t0) / (t1 - t0);
+      double r, v;
+      in.cos.virial(M, satellite ? zFrozen : (z == z ? z : in.cos.redshift(a)), r, v);
+      out.segParam[(size_t)GAL_P_MASS * out.nSeg + sg] = M;
+      out.segParam[(size_t)GAL_P_MASS_RATE * out.nSeg + sg] = accretion;
+      out.segParam[(size_t)GAL_P_RADIUS_VIRIAL * out.nSeg + sg] = r;
+      out.segParam[(size_t)GAL_P_VELOCITY_VIRIAL * out.nSeg + sg] = v;
+      out.segParam[(size_t)GAL_P_SPIN * out.nSeg + sg] = sp;
+      out.segT0[sg] = a;
+      out.segT1[sg] = b;
+      if (k >= 0 && slot < slotEnd) {
+        out.segSnap[sg] = (int32_t)slot;
+        out.snapNode[slot] = (int32_t)i;
+        out.snapOutput[slot] = k;
+        ++slot;
+      } else {
+        out.segSnap[sg] = -1;
+      }
+      ++sg;
+    });
+  }
 }
 
 }  // namespace
@@ -100,8 +300,8 @@ struct gal_forest_dev {
   int32_t* dStatus = nullptr;
   uint32_t* dCounters = nullptr;
   unsigned long long* dHead = nullptr;
-  // host copies of the snapshot labels
-  std::vector<int32_t> snapNode, snapOutput;
+  // snapshot labels: node and output index of each slot
+  int32_t *dSnapNode = nullptr, *dSnapOutput = nullptr;
   // the captured evolution and the form/shape it was captured for
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -118,7 +318,7 @@ void release(gal_forest_dev* f) {
   if (f->done) cudaEventDestroy(f->done);
   void* ptrs[] = {f->dLeaves, f->dParent, f->dChildFirst, f->dChildCount, f->dPending, f->dPending0, f->dSegFirst,
                   f->dSegCount, f->dSnapInitial, f->dSegSnap, f->dSegParam, f->dSegT0, f->dSegT1, f->dState0,
-                  f->dState, f->dStepOut, f->dSnap, f->dStatus, f->dCounters, f->dHead};
+                  f->dState, f->dStepOut, f->dSnap, f->dStatus, f->dCounters, f->dHead, f->dSnapNode, f->dSnapOutput};
   for (void* p : ptrs) cudaFree(p);
   delete f;
 }
@@ -248,128 +448,108 @@ int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const 
   if (satHost)
     for (int64_t i = 0; i < n; ++i)
       if (satHost[i] >= 0) massIn[(size_t)satHost[i]] += mass[i];
-  auto isSatellite = [&](int64_t i) { return satHost && satHost[i] >= 0; };
   const gal_params& p = ctx->params;
   const HostCosmology cos{p.omega_matter, p.omega_dark_energy, p.hubble_constant};
   gal_forest_dev* f = new (std::nothrow) gal_forest_dev();
   if (!f) return fail(ctx, GAL_ERR_ARGUMENT, "out of host memory%s");
   f->n = n;
-  // A node's evolve calls: from its time to its parent's, each ending at the
-  // first of the next output time, the parent's time and the timestep
-  // limit; seg(a, b, k, z) for each, k the output it ends at or -1, z the
-  // redshift at a when the timestep limit needed it (else NaN).
-  auto segments = [&](int64_t i, auto&& seg) {
-    const int32_t par = parent[i];
-    const double t0 = time[i], t1 = par >= 0 ? time[par] : time[i];
-    double a = t0;
-    int32_t k = (int32_t)(std::upper_bound(tOut, tOut + nOut, t0) - tOut);  // first output after t0
-    const bool relative = p.timestep_relative > 0.0;
-    while (a < t1) {
-      const double z = relative ? cos.redshift(a) : NAN;
-      const double limit = a + cos.step_limit_z(z, p.timestep_relative, p.timestep_absolute);
-      const bool atOutput = k < nOut && tOut[k] < t1 && !(limit < tOut[k]);
-      const double b = atOutput ? tOut[k] : std::min(limit, t1);
-      seg(a, b, atOutput ? k : -1, z);
-      if (atOutput) ++k;
-      a = b;
-    }
+  // The segment table on the GPU: the node arrays the kernels read, the
+  // counts and their offsets (freed at the end), then the table itself.
+  cudaStream_t st = ctx->stream;
+  double *dTime = nullptr, *dMass = nullptr, *dSpin = nullptr, *dMassIn = nullptr, *dTOut = nullptr;
+  int32_t *dSatHost = nullptr, *dSnapCount = nullptr;
+  int64_t *dSegBase = nullptr, *dSnapBase = nullptr, *dTotals = nullptr;
+  int* dFlag = nullptr;
+  auto cleanup = [&]() {
+    void* tmp[] = {dTime, dMass, dSpin, dMassIn, dTOut, dSatHost, dSnapCount, dSegBase, dSnapBase, dTotals, dFlag};
+    for (void* q : tmp) cudaFree(q);
   };
-  // The output at the node's own time, if any (a non-root only if it has an
-  // interval to evolve).
-  auto initial_output = [&](int64_t i) -> int32_t {
-    const int32_t par = parent[i];
-    const double t0 = time[i];
-    if (!(par < 0 || t0 < time[par])) return -1;
-    const double* it = std::lower_bound(tOut, tOut + nOut, t0);
-    return it != tOut + nOut && *it == t0 ? (int32_t)(it - tOut) : -1;
+  auto put = [&](auto** dst, const auto* src, size_t count) {
+    using T = std::remove_const_t<std::remove_pointer_t<decltype(src)>>;
+    cudaError_t r = cudaMalloc((void**)dst, std::max<size_t>(count, 1) * sizeof(T));
+    if (r == cudaSuccess && count) r = cudaMemcpyAsync(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice, st);
+    return r;
   };
-  // Pass 1, parallel: evolve calls and snapshot slots per node; then their
-  // offsets in node order.
-  std::vector<int64_t> segBase((size_t)n + 1, 0), snapBase((size_t)n + 1, 0);
-#pragma omp parallel for schedule(dynamic, 4096)
-  for (int64_t i = 0; i < n; ++i) {
-    int64_t ns = 0, nsnap = initial_output(i) >= 0 ? 1 : 0;
-    segments(i, [&](double, double, int32_t k, double) {
-      ++ns;
-      if (k >= 0) ++nsnap;
-    });
-    segBase[(size_t)i + 1] = ns;
-    snapBase[(size_t)i + 1] = nsnap;
+  auto give_up = [&](cudaError_t err) {
+    cudaGetLastError();
+    cleanup();
+    release(f);
+    return fail(ctx, GAL_ERR_CUDA, "gal_gpu_forest_create: segment table on the GPU failed: %s", cudaGetErrorString(err));
+  };
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = put(&f->dParent, parent, (size_t)n);
+  if (e == cudaSuccess) e = put(&f->dChildFirst, childFirst, (size_t)n);
+  if (e == cudaSuccess) e = put(&f->dChildCount, childCount, (size_t)n);
+  if (e == cudaSuccess) e = put(&dTime, time, (size_t)n);
+  if (e == cudaSuccess) e = put(&dMass, mass, (size_t)n);
+  if (e == cudaSuccess) e = put(&dSpin, spin, (size_t)n);
+  if (e == cudaSuccess) e = put(&dMassIn, massIn.data(), (size_t)n);
+  if (e == cudaSuccess) e = put(&dTOut, tOut, (size_t)nOut);
+  if (e == cudaSuccess && satHost) e = put(&dSatHost, satHost, (size_t)n);
+  if (e == cudaSuccess) e = cudaMalloc(&f->dSegCount, (size_t)n * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&dSnapCount, (size_t)n * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&dSegBase, (size_t)n * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&dSnapBase, (size_t)n * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&dFlag, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(dFlag, 0, sizeof(int), st);
+  if (e != cudaSuccess) return give_up(e);
+  const SegmentInputs in{cos,   p.timestep_relative, p.timestep_absolute, n,       nOut,           dTOut,
+                         dTime, dMass,               dSpin,              dMassIn, f->dParent,     f->dChildFirst,
+                         f->dChildCount, dSatHost};
+  const int threads = 256;
+  const int grid = (int)std::min<int64_t>((n + threads - 1) / threads, (int64_t)std::max(ctx->smCount, 1) * 16);
+  count_calls_kernel<<<grid, threads, 0, st>>>(in, f->dSegCount, dSnapCount, dFlag);
+  const int64_t nb = (n + 1023) / 1024;
+  if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaMalloc(&dTotals, (size_t)2 * nb * sizeof(int64_t))) != cudaSuccess)
+    return give_up(e);
+  scan_blocks_kernel<<<(unsigned)nb, 1024, 0, st>>>(f->dSegCount, dSnapCount, n, dSegBase, dSnapBase, dTotals);
+  std::vector<int64_t> totals((size_t)2 * nb);
+  int flag = 0;
+  if ((e = cudaGetLastError()) != cudaSuccess ||
+      (e = cudaMemcpyAsync(totals.data(), dTotals, totals.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, st)) !=
+          cudaSuccess ||
+      (e = cudaMemcpyAsync(&flag, dFlag, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess)
+    return give_up(e);
+  if (flag) {
+    cleanup();
+    release(f);
+    return fail(ctx, GAL_ERR_TOO_LARGE, "gal_gpu_forest_create: a node needs more than 2^24 evolve calls%s");
   }
-  for (int64_t i = 0; i < n; ++i) {
-    segBase[(size_t)i + 1] += segBase[(size_t)i];
-    snapBase[(size_t)i + 1] += snapBase[(size_t)i];
+  int64_t nSeg = 0, nSnap = 0;
+  for (int64_t b = 0; b < nb; ++b) {
+    const int64_t ts = totals[(size_t)(2 * b)], tn = totals[(size_t)(2 * b + 1)];
+    totals[(size_t)(2 * b)] = nSeg;
+    totals[(size_t)(2 * b + 1)] = nSnap;
+    nSeg += ts;
+    nSnap += tn;
   }
-  const int64_t nSeg = segBase[(size_t)n], nSnap = snapBase[(size_t)n];
   if (nSeg > (int64_t)INT32_MAX || nSnap > (int64_t)INT32_MAX) {
-    delete f;
+    cleanup();
+    release(f);
     return fail(ctx, GAL_ERR_TOO_LARGE, "gal_gpu_forest_create: more than 2^31 evolve calls or snapshots%s");
   }
-  std::vector<int32_t> leaves, pending0((size_t)n), segFirst((size_t)n), segCount((size_t)n), snapInitial((size_t)n);
-  std::unique_ptr<int32_t[]> segSnap = scratch<int32_t>((size_t)nSeg);
-  std::unique_ptr<double[]> segParamFlat = scratch<double>((size_t)GAL_NP * nSeg), segT0 = scratch<double>((size_t)nSeg),
-                            segT1 = scratch<double>((size_t)nSeg);
-  if (!segSnap || !segParamFlat || !segT0 || !segT1) {
-    delete f;
-    return fail(ctx, GAL_ERR_ARGUMENT, "gal_gpu_forest_create: out of host memory%s");
-  }
-  f->snapNode.resize((size_t)nSnap);
-  f->snapOutput.resize((size_t)nSnap);
-  // Pass 2, parallel: each node's calls at its offsets (the same numbering as
-  // one pass in node order).
-#pragma omp parallel for schedule(dynamic, 4096)
-  for (int64_t i = 0; i < n; ++i) {
-    pending0[(size_t)i] = childCount[i];
-    const int32_t par = parent[i];
-    const double t0 = time[i], t1 = par >= 0 ? time[par] : time[i];
-    const bool primary = par >= 0 && childFirst[par] == (int32_t)i;
-    // The primary progenitor grows by its parent's unresolved mass (the
-    // parent's mass beyond its progenitors' and the satellites falling in);
-    // other progenitors and satellites keep theirs and accrete nothing.
-    double massEnd = mass[i], accretion = 0.0;
-    if (primary && t1 > t0 && !isSatellite(i)) {
-      double brought = massIn[(size_t)par];
-      for (int32_t c = 0; c < childCount[par]; ++c)
-        if (!isSatellite(childFirst[par] + c)) brought += mass[childFirst[par] + c];
-      accretion = std::max(mass[par] - brought, 0.0) / (t1 - t0);
-      massEnd = mass[i] + accretion * (t1 - t0);
-    }
-    // A satellite's virial scales are those of its infall time.
-    const double zFrozen = isSatellite(i) ? cos.redshift(t0) : 0.0;
-    int64_t slot = snapBase[(size_t)i];
-    const int32_t k0 = initial_output(i);
-    snapInitial[(size_t)i] = -1;
-    if (k0 >= 0) {
-      snapInitial[(size_t)i] = (int32_t)slot;
-      f->snapNode[(size_t)slot] = (int32_t)i;
-      f->snapOutput[(size_t)slot] = k0;
-      ++slot;
-    }
-    int64_t sg = segBase[(size_t)i];
-    segFirst[(size_t)i] = (int32_t)sg;
-    segCount[(size_t)i] = (int32_t)(segBase[(size_t)i + 1] - sg);
-    segments(i, [&](double a, double b, int32_t k, double z) {
-      const double M = mass[i] + (massEnd - mass[i]) * (a - t0) / (t1 - t0);
-      double r, v;
-      cos.virial(M, isSatellite(i) ? zFrozen : (z == z ? z : cos.redshift(a)), r, v);
-      segParamFlat[(size_t)GAL_P_MASS * nSeg + sg] = M;
-      segParamFlat[(size_t)GAL_P_MASS_RATE * nSeg + sg] = accretion;
-      segParamFlat[(size_t)GAL_P_RADIUS_VIRIAL * nSeg + sg] = r;
-      segParamFlat[(size_t)GAL_P_VELOCITY_VIRIAL * nSeg + sg] = v;
-      segParamFlat[(size_t)GAL_P_SPIN * nSeg + sg] = spin[i];
-      segT0[(size_t)sg] = a;
-      segT1[(size_t)sg] = b;
-      if (k >= 0) {
-        segSnap[(size_t)sg] = (int32_t)slot;
-        f->snapNode[(size_t)slot] = (int32_t)i;
-        f->snapOutput[(size_t)slot] = k;
-        ++slot;
-      } else {
-        segSnap[(size_t)sg] = -1;
-      }
-      ++sg;
-    });
-  }
+  if ((e = cudaMemcpyAsync(dTotals, totals.data(), totals.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st)) !=
+      cudaSuccess)
+    return give_up(e);
+  add_offsets_kernel<<<(unsigned)nb, 1024, 0, st>>>(dSegBase, dSnapBase, n, dTotals);
+  if ((e = cudaGetLastError()) != cudaSuccess) return give_up(e);
+  if ((e = cudaMalloc(&f->dSegFirst, (size_t)n * sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&f->dSnapInitial, (size_t)n * sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&f->dSnapNode, (size_t)std::max<int64_t>(nSnap, 1) * sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&f->dSnapOutput, (size_t)std::max<int64_t>(nSnap, 1) * sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&f->dSegParam, (size_t)GAL_NP * std::max<int64_t>(nSeg, 1) * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&f->dSegT0, (size_t)std::max<int64_t>(nSeg, 1) * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&f->dSegT1, (size_t)std::max<int64_t>(nSeg, 1) * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&f->dSegSnap, (size_t)std::max<int64_t>(nSeg, 1) * sizeof(int32_t))) != cudaSuccess)
+    return give_up(e);
+  const SegmentOutputs outs{nSeg,          nSnap,         dSegBase,        dSnapBase,       f->dSegCount,
+                            f->dSegFirst,  f->dSnapInitial, f->dSnapNode,  f->dSnapOutput,  f->dSegParam,
+                            f->dSegT0,     f->dSegT1,     f->dSegSnap};
+  fill_calls_kernel<<<grid, threads, 0, st>>>(in, outs);
+  if ((e = cudaGetLastError()) != cudaSuccess) return give_up(e);
+  ctx->launches += 4;
+  std::vector<int32_t> leaves;
   for (int64_t i = 0; i < n; ++i)
     if (childCount[i] == 0) leaves.push_back((int32_t)i);
   // Longest chains first: a leaf's chain to its root is the sequence of
@@ -406,21 +586,16 @@ int gal_gpu_forest_create(gal_ctx* ctx, int64_t n, const int32_t* parent, const 
   f->nLeaves = (int64_t)leaves.size();
   f->nSeg = nSeg;
   f->nSnap = nSnap;
-  cudaError_t e = cudaSetDevice(ctx->device);
-  if (e == cudaSuccess) e = upload(&f->dLeaves, leaves);
-  if (e == cudaSuccess) e = upload(&f->dParent, parent, (size_t)n);
-  if (e == cudaSuccess) e = upload(&f->dChildFirst, childFirst, (size_t)n);
-  if (e == cudaSuccess) e = upload(&f->dChildCount, childCount, (size_t)n);
-  if (e == cudaSuccess) e = upload(&f->dPending0, pending0);
-  if (e == cudaSuccess) e = upload(&f->dPending, pending0);
-  if (e == cudaSuccess) e = upload(&f->dSegFirst, segFirst);
-  if (e == cudaSuccess) e = upload(&f->dSegCount, segCount);
-  if (e == cudaSuccess) e = upload(&f->dSnapInitial, snapInitial);
-  if (e == cudaSuccess) e = upload(&f->dSegSnap, segSnap.get(), (size_t)nSeg);
-  if (e == cudaSuccess) e = upload(&f->dSegParam, segParamFlat.get(), (size_t)GAL_NP * nSeg);
-  if (e == cudaSuccess) e = upload(&f->dSegT0, segT0.get(), (size_t)nSeg);
-  if (e == cudaSuccess) e = upload(&f->dSegT1, segT1.get(), (size_t)nSeg);
-  if (e == cudaSuccess) e = upload(&f->dState0, state0, (size_t)GAL_NY * n);
+  if (e == cudaSuccess) e = put(&f->dLeaves, leaves.data(), leaves.size());
+  if (e == cudaSuccess) e = cudaMalloc(&f->dPending0, (size_t)n * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&f->dPending, (size_t)n * sizeof(int32_t));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(f->dPending0, f->dChildCount, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(f->dPending, f->dChildCount, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = put(&f->dState0, state0, (size_t)GAL_NY * n);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cleanup();
   if (e == cudaSuccess) e = cudaMalloc(&f->dState, (size_t)GAL_NY * n * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&f->dStepOut, (size_t)n * sizeof(double));
   if (e == cudaSuccess && f->nSnap > 0) e = cudaMalloc(&f->dSnap, (size_t)GAL_NY * f->nSnap * sizeof(double));
@@ -475,9 +650,11 @@ int gal_gpu_forest_results(gal_ctx* ctx, gal_forest_dev* f, double* state, int32
     e = cudaMemcpy(counters, f->dCounters, (size_t)3 * n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && snapshot && f->nSnap > 0)
     e = cudaMemcpy(snapshot, f->dSnap, (size_t)GAL_NY * f->nSnap * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && snapNode && f->nSnap > 0)
+    e = cudaMemcpy(snapNode, f->dSnapNode, (size_t)f->nSnap * sizeof(int32_t), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && snapOutput && f->nSnap > 0)
+    e = cudaMemcpy(snapOutput, f->dSnapOutput, (size_t)f->nSnap * sizeof(int32_t), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return fail(ctx, GAL_ERR_CUDA, "gal_gpu_forest_results: %s", cudaGetErrorString(e));
-  if (snapNode && f->nSnap > 0) std::memcpy(snapNode, f->snapNode.data(), f->nSnap * sizeof(int32_t));
-  if (snapOutput && f->nSnap > 0) std::memcpy(snapOutput, f->snapOutput.data(), f->nSnap * sizeof(int32_t));
   return GAL_OK;
 }
 
