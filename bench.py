@@ -462,10 +462,12 @@ def scale_record(args, params, table, net, gate):
         tb = time.perf_counter()
         fe.evolve()
         dt = time.perf_counter() - tb
+        tr = time.perf_counter()
         state, status, counters = fe.results(snapshots=False)[:3]
+        results_s = time.perf_counter() - tr
         entry = {"value": float(counters[0].sum()) / dt, "s_per_evolution": dt, "accepted_steps": int(counters[0].sum()),
                  "rhs_evaluations": int(counters[2].sum()), "failed_nodes": int((status != 0).sum()),
-                 "create_s": create_s}
+                 "create_s": create_s, "results_s": results_s}
         if name == "surrogate":
             s1 = surrogate.stats(ev) if gate is not None else (0, 0)
             served = s1[0] - s0[0]
