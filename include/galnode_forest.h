@@ -201,7 +201,7 @@ typedef struct gal_forest_dev gal_forest_dev;  /* a forest resident on the GPU o
 
 /* Upload a forest and its output times (sorted, Gyr) to the context's GPU:
  * the segment table (per piece: halo mass, accretion rate, virial radius
- * and velocity, spin, start and end time) is built on the host, and
+ * and velocity, spin, start and end time) is built on the GPU, and
  * state0[GAL_NY][n] holds the initial states (only progenitor-less nodes
  * are read).  A node's halo mass grows by the mass its parent holds beyond
  * its progenitors' (the unresolved mass, over the node's interval) when it
