@@ -209,8 +209,20 @@ def test_forest_rejects_bad_topology(params, table):
                         f.mass.copy(), f.spin.copy())
     i = int(np.flatnonzero(bad.parent >= 0)[0])
     bad.time[i] = bad.time[bad.parent[i]] + 1.0  # a progenitor after its parent
-    with pytest.raises(RuntimeError):
+    with pytest.raises(RuntimeError, match="inconsistent forest topology"):
         forest.ForestEvolver(ev, bad, forest.initial_state(params, bad), forest.output_times(params))
+    # A node whose parent does not list it among its progenitors.
+    orphan = forest.Forest(f.tree.copy(), f.parent.copy(), f.child_first.copy(), f.child_count.copy(), f.time.copy(),
+                           f.mass.copy(), f.spin.copy())
+    p = int(np.flatnonzero(orphan.child_count > 1)[0])
+    orphan.child_count[p] -= 1
+    with pytest.raises(RuntimeError, match="progenitors must be contiguous"):
+        forest.ForestEvolver(ev, orphan, forest.initial_state(params, orphan), forest.output_times(params))
+    # The context stays usable.
+    fe = forest.ForestEvolver(ev, f, forest.initial_state(params, f), forest.output_times(params))
+    fe.evolve()
+    assert np.all(fe.results()[1] == 0)
+    fe.close()
     ev.close()
 
 
