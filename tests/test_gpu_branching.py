@@ -135,3 +135,30 @@ def test_gpu_branching_matches_the_oracle_for_other_parameters(case, params, evo
     np.testing.assert_array_equal(np.where(f.parent >= 0, f.parent - local, -1), parent)
     np.testing.assert_array_equal(f.child_count, child_count)
     np.testing.assert_array_equal(f.mass, mass)
+
+
+def test_gpu_built_forest_plain_form_matches_the_oracle(params, evolver, table, oracle_mod):
+    """The plain FP64 form on a GPU-built forest with satellites: every node
+    within ten times the tolerance of the oracle (allowing, as for the host
+    builder's forests, for nodes whose oracle answer itself moves with the
+    tolerance), the snapshot labels exactly."""
+    from oracle import compare
+    from galacticus_gb300 import _abi
+    from galacticus_gb300.evolver import MergerTreeNodeEvolverStandard
+    f = forest.build(params, n_trees=32, gpu=evolver, satellites=forest.SATELLITES_JIANG2008, **SPEC)
+    state0 = forest.initial_state(params, f)
+    times = forest.output_times(params)
+    plain = MergerTreeNodeEvolverStandard(params=params, table=table, ratePrecision="fp64")
+    fe = forest.ForestEvolver(plain, f, state0, times)
+    fe.evolve()
+    state, status, _, snaps, snap_node, _ = fe.results()
+    fe.close()
+    plain.close()
+    ref, ref_status, _, ref_snaps = oracle_mod.evolve_forest(params, table, f, state0, times, brent=False)
+    assert np.all(status == 0) and np.all(ref_status == 0)
+    first, m = oracle_mod.forest_snapshots(f, times)
+    np.testing.assert_array_equal(snap_node, np.repeat(np.arange(f.n), np.diff(np.append(first, m))))
+    param = np.zeros((_abi.NP, f.n))
+    param[_abi.P_MASS] = f.mass
+    within = np.all(np.abs(state - ref) <= compare.parity_bound(ref, ref, param, params), axis=0)
+    assert within.mean() > 0.998, within.mean()
